@@ -1,0 +1,11 @@
+"""cosmicblup_gb300 -- GB300-native GBLUP / ssGBLUP hot path behind a C ABI.
+
+The compute lives in ``libcbx.so`` (CUDA for sm_103a + C++ host code, built by
+``cosmicblup_gb300.build``); this package is a thin Python mirror of the
+reference interfaces used by tests and benchmarks.
+"""
+from ._lib import CbxError, Handle, lib  # noqa: F401
+from .grm import GrmBuilder, GrmOptions, PlinkReader, bed_snp_counts  # noqa: F401
+
+__all__ = ["CbxError", "Handle", "lib", "GrmBuilder", "GrmOptions", "PlinkReader",
+           "bed_snp_counts"]

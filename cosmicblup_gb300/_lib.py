@@ -1,0 +1,121 @@
+"""ctypes binding of libcbx.so (the C ABI declared in include/cbx.h).
+
+The library is loaded from the package directory.  There is no fallback:
+if it is missing or cannot be loaded, every entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libcbx.so")
+
+CBX_OK = 0
+STATUS_NAMES = {
+    1: "CBX_ERR_ARG", 2: "CBX_ERR_CUDA", 3: "CBX_ERR_FORMAT", 4: "CBX_ERR_TIMEOUT",
+    5: "CBX_ERR_BREAKDOWN", 6: "CBX_ERR_NONFINITE", 7: "CBX_ERR_NOTCONV", 8: "CBX_ERR_FACTOR",
+    9: "CBX_ERR_STATE", 10: "CBX_ERR_UNSUPPORTED",
+}
+
+_lib = None
+
+i32p = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+i64p = np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")
+f64p = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+f32p = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
+u8p = np.ctypeslib.ndpointer(dtype=np.uint8, flags="C_CONTIGUOUS")
+
+# (name, restype, argtypes) for every C ABI entry point
+SIGNATURES = [
+    ("cbx_version", C.c_int, []),
+    ("cbx_create", C.c_int, [C.c_int, C.POINTER(C.c_void_p)]),
+    ("cbx_destroy", C.c_int, [C.c_void_p]),
+    ("cbx_last_error", C.c_char_p, [C.c_void_p]),
+    ("cbx_launch_count", C.c_int64, [C.c_void_p]),
+    ("cbx_sync", C.c_int, [C.c_void_p]),
+    ("cbx_bed_snp_counts", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_int64,
+                                     C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("cbx_grm_bed", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.c_float,
+                              C.c_int, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
+                              C.POINTER(C.c_double), C.POINTER(C.c_int64)]),
+    # self-test export (not in the public header)
+    ("cbx_selftest_umma", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+]
+
+
+class CbxError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{STATUS_NAMES.get(code, code)}: {msg}")
+        self.code = code
+
+
+def lib() -> C.CDLL:
+    """Load libcbx.so once; raise if it is not built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is not built; run `python -m cosmicblup_gb300.build`")
+        L = C.CDLL(LIB_PATH)
+        for name, res, args in SIGNATURES:
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def ptr(a: np.ndarray | None) -> C.c_void_p | None:
+    if a is None:
+        return None
+    assert a.flags["C_CONTIGUOUS"], "arrays passed to libcbx must be C-contiguous"
+    return C.c_void_p(a.ctypes.data)
+
+
+class Handle:
+    """Owns one cbx_handle (one CUDA stream on one device)."""
+
+    def __init__(self, device: int = 0):
+        self._h = C.c_void_p()
+        rc = lib().cbx_create(device, C.byref(self._h))
+        if rc != CBX_OK:
+            msg = lib().cbx_last_error(self._h).decode() if self._h else "cbx_create failed"
+            if self._h:
+                lib().cbx_destroy(self._h)
+            self._h = None
+            raise CbxError(rc, msg)
+
+    @property
+    def raw(self) -> C.c_void_p:
+        if self._h is None:
+            raise RuntimeError("handle closed")
+        return self._h
+
+    def check(self, rc: int) -> None:
+        if rc != CBX_OK:
+            raise CbxError(rc, lib().cbx_last_error(self._h).decode())
+
+    def launches(self) -> int:
+        return int(lib().cbx_launch_count(self.raw))
+
+    def sync(self) -> None:
+        self.check(lib().cbx_sync(self.raw))
+
+    def close(self) -> None:
+        if self._h is not None:
+            lib().cbx_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,84 @@
+// Handle lifetime and bookkeeping entry points of the C ABI.
+#include "handle.h"
+
+void cbx_handle::check_status(const char* what) {
+  int st = 0;
+  CBX_CUDA(cudaMemcpyAsync(&st, status.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
+  CBX_CUDA(cudaStreamSynchronize(stream));
+  if (st != cbx::DEV_OK) {
+    CBX_CUDA(cudaMemsetAsync(status.p, 0, sizeof(int), stream));
+    CBX_CUDA(cudaStreamSynchronize(stream));
+    if (st == cbx::DEV_TIMEOUT)
+      throw cbx::Error(CBX_ERR_TIMEOUT, std::string(what) + ": device-side wait timed out");
+    if (st == cbx::DEV_BREAKDOWN)
+      throw cbx::Error(CBX_ERR_BREAKDOWN, std::string(what) + ": breakdown");
+    if (st == cbx::DEV_NONFINITE)
+      throw cbx::Error(CBX_ERR_NONFINITE, std::string(what) + ": non-finite values");
+    throw cbx::Error(CBX_ERR_CUDA, std::string(what) + ": device status " + std::to_string(st));
+  }
+}
+
+extern "C" {
+
+int cbx_version(void) { return 100; }  // 0.1.0
+
+int cbx_create(int device, cbx_handle** out) {
+  if (!out) return CBX_ERR_ARG;
+  *out = nullptr;
+  auto* h = new cbx_handle();
+  int rc = cbx_guard(h, [&] {
+    int ndev = 0;
+    CBX_CUDA(cudaGetDeviceCount(&ndev));
+    CBX_REQUIRE(device >= 0 && device < ndev, CBX_ERR_ARG, "device index out of range");
+    cudaDeviceProp prop{};
+    CBX_CUDA(cudaGetDeviceProperties(&prop, device));
+    CBX_REQUIRE(prop.major == 10 && prop.minor == 3, CBX_ERR_CUDA,
+                "libcbx is built for sm_103a (GB300); found sm_" + std::to_string(prop.major) +
+                    std::to_string(prop.minor));
+    CBX_CUDA(cudaSetDevice(device));
+    h->device = device;
+    h->num_sms = prop.multiProcessorCount;
+    CBX_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    h->status.resize(4);
+    h->status.zero(h->stream);
+    CBX_CUDA(cudaStreamSynchronize(h->stream));
+  });
+  if (rc != CBX_OK) {
+    // keep the handle so the caller can read cbx_last_error, then destroy it
+    *out = h;
+    return rc;
+  }
+  *out = h;
+  return CBX_OK;
+}
+
+int cbx_destroy(cbx_handle* h) {
+  if (!h) return CBX_ERR_ARG;
+  if (h->stream) {
+    cudaSetDevice(h->device);
+    cudaStreamSynchronize(h->stream);
+  }
+  {
+    cbx_handle* tmp = h;
+    tmp->G.release();
+    tmp->status.release();
+    if (tmp->stream) cudaStreamDestroy(tmp->stream);
+  }
+  delete h;
+  return CBX_OK;
+}
+
+const char* cbx_last_error(const cbx_handle* h) {
+  return h ? h->last_error.c_str() : "null handle";
+}
+
+int64_t cbx_launch_count(const cbx_handle* h) { return h ? h->launches : -1; }
+
+int cbx_sync(cbx_handle* h) {
+  return cbx_guard(h, [&] {
+    CBX_CUDA(cudaSetDevice(h->device));
+    CBX_CUDA(cudaStreamSynchronize(h->stream));
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,88 @@
+/*
+ * cbx.h -- C ABI of the GB300 (sm_103a) GBLUP / ssGBLUP engine.
+ *
+ * Each entry point replaces one piece of the CosmicBLUP CPU path (the
+ * reference file:line it stands in for is given beside it).  Conventions:
+ *
+ *  - plain C: opaque handle, int32 status (CBX_OK == 0), no exceptions cross
+ *    the boundary; cbx_last_error(h) returns the message of the last failure;
+ *  - one CUDA stream per handle; a handle is not thread-safe (the reference is
+ *    driven from one host thread too);
+ *  - matrices are dense column-major FP64 unless stated (Eigen's default
+ *    storage); symmetric matrices are stored in full;
+ *  - every buffer argument is HOST memory unless the name ends in "_dev".
+ *
+ * There is no CPU fallback: if the CUDA runtime or an sm_103a device is not
+ * available, cbx_create fails with CBX_ERR_CUDA.
+ */
+#ifndef CBX_H_
+#define CBX_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  CBX_OK = 0,
+  CBX_ERR_ARG = 1,         /* invalid argument (std::invalid_argument in the reference) */
+  CBX_ERR_CUDA = 2,        /* CUDA runtime / library failure */
+  CBX_ERR_FORMAT = 3,      /* malformed input file bytes (bad BED magic, truncated, ...) */
+  CBX_ERR_TIMEOUT = 4,     /* a device-side wait gave up (bounded spin) */
+  CBX_ERR_BREAKDOWN = 5,   /* PCG breakdown twice in a row (|p'Ap| < 1e-300) */
+  CBX_ERR_NONFINITE = 6,   /* NaN / Inf in inputs or iterates */
+  CBX_ERR_NOTCONV = 7,     /* iteration limit reached without convergence */
+  CBX_ERR_FACTOR = 8,      /* dense factorization failed (not positive definite) */
+  CBX_ERR_STATE = 9,       /* call order violated (e.g. solve before upload) */
+  CBX_ERR_UNSUPPORTED = 10 /* option the GPU path does not implement */
+};
+
+typedef struct cbx_handle cbx_handle;
+
+/* ---- lifetime ----------------------------------------------------------- */
+int cbx_create(int device, cbx_handle** out);
+int cbx_destroy(cbx_handle* h);
+const char* cbx_last_error(const cbx_handle* h);
+int cbx_version(void);                                /* 10000*major + 100*minor + patch */
+/* Kernel launches issued by this handle since creation (for benchmarks). */
+int64_t cbx_launch_count(const cbx_handle* h);
+/* Synchronize the handle's stream. */
+int cbx_sync(cbx_handle* h);
+
+/* ---- PLINK BED statistics ------------------------------------------------
+ * Replaces the per-SNP stats pass of GrmBuilder::compute
+ * (src/core/grm_builder.cpp:175-263) on top of PlinkReader::openBed's checks
+ * (src/core/plink_reader.cpp:66-91).  bed points at the whole .bed file
+ * (3-byte magic included), bed_bytes is its size.  Outputs (length m, int32):
+ * observed calls, sum of allele-1 copies, counts of codes 00 / 10 / 11.
+ * Any output pointer may be NULL. */
+int cbx_bed_snp_counts(cbx_handle* h, const uint8_t* bed, int64_t bed_bytes,
+                       int64_t n, int64_t m, int32_t* n_obs, int32_t* sum_x,
+                       int32_t* n_hom1, int32_t* n_het, int32_t* n_hom2);
+
+/* ---- Genomic relationship matrix -----------------------------------------
+ * Replaces GrmBuilder::compute(const PlinkReader&) for algorithm 1 (VanRaden)
+ * with one population, no SNP weights and no HWE filter
+ * (src/core/grm_builder.cpp:63-405; accessors getGrm / getSum2pq /
+ * getTotalSnps / getAlleleFreqs, src/core/grm_builder.h:51-58).
+ *   min_maf     : GrmBuilder::Options::min_maf (0.01f by default)
+ *   algorithm   : must be 1 (others return CBX_ERR_UNSUPPORTED)
+ *   block_size  : GrmBuilder::Options::block_size; only changes the order in
+ *                 which sum 2pq is accumulated, exactly as the reference does
+ * Outputs (each may be NULL):
+ *   G           : n*n FP64, G = Z Z^T / sum_2pq
+ *   xx_counts   : n*n int32, sum over MAF-valid SNPs of x_i x_k (missing = 0),
+ *                 the exact integer cross-products formed on the tensor cores
+ *   allele_freqs: m floats, (float)freq or -1 for filtered SNPs
+ *   sum2pq, n_valid: scalars
+ * G is also kept on the device inside the handle (see cbx_invert_psd_g). */
+int cbx_grm_bed(cbx_handle* h, const uint8_t* bed, int64_t bed_bytes, int64_t n,
+                int64_t m, float min_maf, int algorithm, int64_t block_size,
+                double* G, int32_t* xx_counts, float* allele_freqs,
+                double* sum2pq, int64_t* n_valid);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CBX_H_ */
