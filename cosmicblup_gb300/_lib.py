@@ -41,6 +41,14 @@ SIGNATURES = [
     ("cbx_grm_bed", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.c_float,
                               C.c_int, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
                               C.POINTER(C.c_double), C.POINTER(C.c_int64)]),
+    ("cbx_mme_create", C.c_int, [C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.c_void_p, C.c_void_p,
+                                 C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("cbx_mme_set_qinv_dense", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64]),
+    ("cbx_mme_set_qinv_split", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                         C.c_int64, C.c_void_p]),
+    ("cbx_pcg_solve", C.c_int, [C.c_void_p, C.c_double, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32,
+                                C.c_double, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]),
+    ("cbx_qinv_apply", C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
     # self-test export (not in the public header)
     ("cbx_selftest_umma", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
 ]

@@ -5,8 +5,11 @@
 //
 // The reference forms Z (n x m, FP64) with Z_ij = x_ij - mu_j for observed
 // calls and 0 for missing ones, then G = Z Z^T / sum_2pq (FP64 GEMM, :351).
-// Here the same quantity is computed EXACTLY in integer arithmetic on the
-// f16 tensor cores and rounded once at the end:
+// Here the same quantity is computed in integer arithmetic on the f16 tensor
+// cores and rounded once at the end.  XX and L are exact; Q uses mu_j^2
+// rounded to a multiple of 2^-45, so |G - G_exact| <= n_valid 2^-46 / sum_2pq
+// (plus the final rounding) -- below the FP64 GEMM rounding of the reference
+// for realistic SNP counts:
 //
 //   (Z Z^T)_ik = XX_ik - L_ik 2^-29 + Q_ik 2^-45, with
 //   XX_ik = sum_j x_ij x_kj                               (integer cross-products)

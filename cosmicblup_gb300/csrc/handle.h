@@ -5,40 +5,10 @@
 #include <vector>
 #include <cuda_runtime.h>
 #include "cbx_common.cuh"
+#include "devbuf.h"
+#include "mme.h"
+#include <memory>
 
-namespace cbx {
-
-// RAII device buffer (cudaMalloc / cudaFree, no pooling; the handle owns them).
-template <typename T>
-struct DevBuf {
-  T* p = nullptr;
-  size_t n = 0;
-  DevBuf() = default;
-  DevBuf(const DevBuf&) = delete;
-  DevBuf& operator=(const DevBuf&) = delete;
-  DevBuf(DevBuf&& o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
-  DevBuf& operator=(DevBuf&& o) noexcept {
-    if (this != &o) { release(); p = o.p; n = o.n; o.p = nullptr; o.n = 0; }
-    return *this;
-  }
-  ~DevBuf() { release(); }
-  void release() {
-    if (p) cudaFree(p);
-    p = nullptr;
-    n = 0;
-  }
-  void resize(size_t count) {
-    if (count == n && p) return;
-    release();
-    if (count) CBX_CUDA(cudaMalloc(&p, count * sizeof(T)));
-    n = count;
-  }
-  void zero(cudaStream_t s) {
-    if (n) CBX_CUDA(cudaMemsetAsync(p, 0, n * sizeof(T), s));
-  }
-};
-
-}  // namespace cbx
 
 struct cbx_handle {
   int device = 0;
@@ -48,9 +18,14 @@ struct cbx_handle {
   int64_t launches = 0;
   cbx::DevBuf<int> status;  // device-side error word(s)
 
-  // Genomic relationship matrix kept on the device after cbx_grm_bed.
+  // Genomic relationship matrix kept on the device after cbx_grm_bed, and its
+  // eigen-bent inverse after cbx_invert_psd_g.
   cbx::DevBuf<double> G;
   int64_t G_n = 0;
+  cbx::DevBuf<double> Ginv;
+  int64_t Ginv_n = 0;
+  // mixed-model equations and REML state
+  std::unique_ptr<cbx::Mme> mme;
 
   // count a kernel launch and check the launch error
   void launched(const char* what) {

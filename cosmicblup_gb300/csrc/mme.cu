@@ -1,0 +1,852 @@
+// Mixed-model equations on the device and the multi-RHS PCG solver.
+//
+// Replaces, for one random component:
+//  * MMELHSBuilder::initialize / build_lhs / build_rhs
+//    (src/core/mme_builder.cpp:72-387): W'W and W'y are assembled on the host
+//    in the reference's record order and uploaded once; lambda Qinv is applied
+//    on the fly instead of being copied into the CSR;
+//  * DenseMatrixAdapter / SplitMatrixAdapter products
+//    (src/core/matrix_adapter.h:116-153, 232-373);
+//  * PCGSolver::solve with the block-Jacobi preconditioner
+//    (src/core/pcg_solver.h:60-128, 436-536) and MatrixFreePCG's absolute stop
+//    (src/core/matrix_free_pcg.h:20-66).
+#include <algorithm>
+#include <cmath>
+#include <vector>
+#include "handle.h"
+#include "pcg.h"
+#include "solver.cuh"
+
+namespace cbx {
+namespace sv {
+
+__global__ void k_resid_records(int64_t n_rec, int64_t p, const double* __restrict__ y,
+                                const int32_t* __restrict__ aid, int64_t q,
+                                const int32_t* __restrict__ xp, const int32_t* __restrict__ xc,
+                                const double* __restrict__ xv, const double* __restrict__ sol,
+                                double* __restrict__ e, double* __restrict__ part) {
+  __shared__ double red[NT];
+  double acc = 0;
+  for (int64_t i = blockIdx.x * (int64_t)NT + threadIdx.x; i < n_rec; i += (int64_t)gridDim.x * NT) {
+    double t = 0.0;
+    for (int32_t j = xp[i]; j < xp[i + 1]; ++j)
+      if (xc[j] < p) t += xv[j] * sol[xc[j]];
+    const int32_t a = aid[i];
+    if (a > 0 && a <= q) t += sol[p + a - 1];
+    const double ev = y[i] - t;
+    if (e) e[i] = ev;
+    acc += ev * ev;
+  }
+  const double s = block_sum_cols<1>(acc, red);
+  if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+}  // namespace sv
+
+// ---------------------------------------------------------------------------
+// helper kernels
+template <typename A, typename B>
+__global__ void k_convert(const A* __restrict__ a, B* __restrict__ b, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    b[i] = static_cast<B>(a[i]);
+}
+
+// dst[i * ld + k] = src[i * n + k] (k < n), 0 in the padding
+template <typename T>
+__global__ void k_pitch_copy(const double* __restrict__ src, int64_t n, int64_t ld, T* __restrict__ dst) {
+  const int64_t total = n * ld;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = idx / ld, k = idx - i * ld;
+    dst[idx] = k < n ? static_cast<T>(src[i * n + k]) : T(0);
+  }
+}
+
+// column-major (dim x ncols) -> interleaved (dim x S), zero in unused columns
+__global__ void k_to_inter(const double* __restrict__ cm, int64_t dim, int ncols, int S,
+                           double* __restrict__ it) {
+  const int64_t total = dim * S;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = idx / S;
+    const int c = (int)(idx - i * S);
+    it[idx] = c < ncols ? cm[(int64_t)c * dim + i] : 0.0;
+  }
+}
+__global__ void k_from_inter(const double* __restrict__ it, int64_t dim, int ncols, int S,
+                             double* __restrict__ cm) {
+  const int64_t total = dim * ncols;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = idx / dim, i = idx - c * dim;
+    cm[idx] = it[i * S + c];
+  }
+}
+
+template <typename T>
+__global__ void k_dinv(const double* __restrict__ diagD, const double* __restrict__ diagQ, int64_t p,
+                       int64_t q, double lam, T* __restrict__ dinv) {
+  for (int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; u < q; u += (int64_t)gridDim.x * blockDim.x) {
+    const double d = diagD[p + u] + lam * diagQ[u];
+    dinv[u] = static_cast<T>(fabs(d) > 1e-12 ? 1.0 / d : 1.0);
+  }
+}
+
+// r32 = (float)(r64 / s_c) for columns with s_c > 0, else 0
+__global__ void k_scale_down(const double* __restrict__ r64, const double* __restrict__ sc, int64_t dim,
+                             int S, float* __restrict__ r32) {
+  const int64_t total = dim * S;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int c = (int)(idx % S);
+    r32[idx] = sc[c] > 0 ? (float)(r64[idx] / sc[c]) : 0.0f;
+  }
+}
+// x64 += s_c * d32
+__global__ void k_accumulate(double* __restrict__ x64, const float* __restrict__ d32,
+                             const double* __restrict__ sc, int64_t dim, int S) {
+  const int64_t total = dim * S;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int c = (int)(idx % S);
+    if (sc[c] > 0) x64[idx] += sc[c] * (double)d32[idx];
+  }
+}
+// R = B - Y
+__global__ void k_sub(const double* __restrict__ B, const double* __restrict__ Y, int64_t n,
+                      double* __restrict__ R) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    R[i] = B[i] - Y[i];
+}
+
+static inline unsigned grid_for(int64_t n, int threads, int cap) {
+  int64_t g = (n + threads - 1) / threads;
+  if (g < 1) g = 1;
+  if (g > cap) g = cap;
+  return (unsigned)g;
+}
+
+// ---------------------------------------------------------------------------
+template <typename T>
+sv::OpView<T> make_view(Mme& m, const T* dinv);
+template <>
+sv::OpView<double> make_view<double>(Mme& m, const double* dinv) {
+  sv::OpView<double> v{};
+  v.p = m.p; v.q = m.q; v.dim = m.dim;
+  v.Dptr = m.D64.ptr.p; v.Dcol = m.D64.col.p; v.Dval = m.D64.val.p;
+  if (m.has_sparse) { v.Sptr = m.Qs64.ptr.p; v.Scol = m.Qs64.col.p; v.Sval = m.Qs64.val.p; }
+  if (m.has_dense) { v.Qd = m.Qd64.p; v.ng = m.ng; v.ld = m.ld; v.gmap = m.gmap.p; v.ginv = m.ginv.p; }
+  v.A11inv = m.A11inv64.p;
+  v.dinv = dinv;
+  return v;
+}
+template <>
+sv::OpView<float> make_view<float>(Mme& m, const float* dinv) {
+  sv::OpView<float> v{};
+  v.p = m.p; v.q = m.q; v.dim = m.dim;
+  v.Dptr = m.D32.ptr.p; v.Dcol = m.D32.col.p; v.Dval = m.D32.val.p;
+  if (m.has_sparse) { v.Sptr = m.Qs32.ptr.p; v.Scol = m.Qs32.col.p; v.Sval = m.Qs32.val.p; }
+  if (m.has_dense) { v.Qd = m.Qd32.p; v.ng = m.ng; v.ld = m.ld; v.gmap = m.gmap.p; v.ginv = m.ginv.p; }
+  v.A11inv = m.A11inv32.p;
+  v.dinv = dinv;
+  return v;
+}
+
+// rows per warp of the dense kernel: RPW * S accumulators <= 64 doubles / 128 floats
+template <typename T, int S>
+constexpr int rpw() {
+  return sizeof(T) == 8 ? (S <= 8 ? 8 : (S == 16 ? 4 : 2)) : (S <= 16 ? 8 : 4);
+}
+
+template <typename T, int S>
+struct Workspace {
+  DevBuf<T> R, Z, P, Q, Vt, Tout, X;
+  DevBuf<double> part, pq_part, rz_fix, tol;
+  DevBuf<sv::Col> col;
+  DevBuf<int> active;
+  int nblk_vec = 0, nblk_spmv = 0;
+  int64_t dim = -1;
+  void alloc(const Mme& m, int num_sms) {
+    if (dim == m.dim && (!m.has_dense || Vt.n == (size_t)S * m.ld)) return;
+    const int64_t n = m.dim * S;
+    R.resize(n); Z.resize(n); P.resize(n); Q.resize(n); X.resize(n);
+    if (m.has_dense) { Vt.resize((size_t)S * m.ld); Tout.resize((size_t)m.ng * S); }
+    nblk_vec = (int)grid_for(n, sv::NT, 2 * num_sms);
+    nblk_spmv = (int)m.p + (int)grid_for(m.dim - m.p, 8, 8 * num_sms);
+    part.resize((size_t)nblk_vec * 3 * S);
+    pq_part.resize((size_t)nblk_spmv * S);
+    rz_fix.resize((size_t)std::max<int64_t>(m.p, 1) * S);
+    tol.resize(S);
+    col.resize(S);
+    active.resize(1);
+    dim = m.dim;
+  }
+};
+
+template <typename T, int S>
+void matvec(cbx_handle* h, const sv::OpView<T>& op, Workspace<T, S>& w, const T* X, T* Y, double lam, int use_D,
+            const T* P, double* pq_part, const int* active) {
+  cudaStream_t s = h->stream;
+  if (op.Qd) {
+    sv::k_gather_t<T, S><<<grid_for(S * op.ld, 256, 4 * h->num_sms), 256, 0, s>>>(X, w.Vt.p, op.p, op.ng, op.ld,
+                                                                               op.gmap, active);
+    h->launched("k_gather_t");
+    constexpr int R = rpw<T, S>();
+    constexpr int KT = 32 * sv::Vec16<T>::n * 4;
+    const int smem = S * KT * (int)sizeof(T);
+    CBX_CUDA(cudaFuncSetAttribute(sv::k_dense<T, S, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    sv::k_dense<T, S, R><<<(unsigned)((op.ng + 8 * R - 1) / (8 * R)), 256, smem, s>>>(op.Qd, op.ng, op.ld, w.Vt.p,
+                                                                                     w.Tout.p, active);
+    h->launched("k_dense");
+  }
+  sv::k_spmv<T, S><<<w.nblk_spmv, sv::NT, 0, s>>>(op, X, w.Tout.p, (T)lam, use_D, Y, P, pq_part, active);
+  h->launched("k_spmv");
+}
+
+// Multi-RHS PCG in precision T on interleaved vectors; X receives the solution
+// (holds x0 when use_x0).  tol_col: per-column tolerance.
+template <typename T, int S>
+void run_pcg(cbx_handle* h, Mme& m, const sv::OpView<T>& op, Workspace<T, S>& w, double lam, const T* B, T* X,
+             int ncols, const double* tol_col, int abs_tol, int maxit, bool use_x0, std::vector<sv::Col>& out,
+             int64_t& matvecs) {
+  cudaStream_t s = h->stream;
+  const int64_t n = m.dim * S;
+  if (use_x0) {
+    matvec<T, S>(h, op, w, X, w.Q.p, lam, 1, nullptr, nullptr, nullptr);
+    ++matvecs;
+  } else {
+    CBX_CUDA(cudaMemsetAsync(X, 0, n * sizeof(T), s));
+  }
+  sv::k_init_resid<T, S><<<w.nblk_vec, sv::NT, 0, s>>>(op, B, w.Q.p, use_x0 ? 1 : 0, w.R.p, w.Z.p, w.part.p);
+  h->launched("k_init_resid");
+  if (m.p > 0) {
+    sv::k_fixed<T, S><<<(unsigned)m.p, sv::NT, 0, s>>>(op, w.R.p, w.Z.p, nullptr, w.rz_fix.p);
+    h->launched("k_fixed");
+  }
+  std::vector<double> tolv(S, 1.0);
+  for (int c = 0; c < ncols; ++c) tolv[c] = tol_col[c];
+  CBX_CUDA(cudaMemcpyAsync(w.tol.p, tolv.data(), S * sizeof(double), cudaMemcpyHostToDevice, s));
+  sv::k_scalar_init<S><<<1, 32, 0, s>>>(w.col.p, ncols, w.part.p, w.nblk_vec, w.rz_fix.p, m.p, abs_tol, w.active.p);
+  h->launched("k_scalar_init");
+  CBX_CUDA(cudaMemcpyAsync(w.P.p, w.Z.p, n * sizeof(T), cudaMemcpyDeviceToDevice, s));
+  int host_active = 1;
+  const int CHECK = 8;
+  for (int it = 0; it < maxit && host_active; it += CHECK) {
+    for (int j = 0; j < CHECK; ++j) {
+      matvec<T, S>(h, op, w, w.P.p, w.Q.p, lam, 1, w.P.p, w.pq_part.p, w.active.p);
+      sv::k_scalar_alpha<S><<<1, 32, 0, s>>>(w.col.p, w.pq_part.p, w.nblk_spmv);
+      h->launched("k_scalar_alpha");
+      sv::k_update<T, S><<<w.nblk_vec, sv::NT, 0, s>>>(op, w.col.p, X, w.R.p, w.Z.p, w.P.p, w.Q.p, w.part.p);
+      h->launched("k_update");
+      if (m.p > 0) {
+        sv::k_fixed<T, S><<<(unsigned)m.p, sv::NT, 0, s>>>(op, w.R.p, w.Z.p, w.col.p, w.rz_fix.p);
+        h->launched("k_fixed");
+      }
+      sv::k_scalar_beta<S><<<1, 32, 0, s>>>(w.col.p, w.part.p, w.nblk_vec, w.rz_fix.p, m.p, w.tol.p, abs_tol,
+                                            maxit, w.active.p);
+      h->launched("k_scalar_beta");
+      sv::k_pupdate<T, S><<<w.nblk_vec, sv::NT, 0, s>>>(m.dim, w.col.p, w.Z.p, w.P.p);
+      h->launched("k_pupdate");
+      ++matvecs;
+    }
+    CBX_CUDA(cudaMemcpyAsync(&host_active, w.active.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CBX_CUDA(cudaStreamSynchronize(s));
+  }
+  out.resize(S);
+  CBX_CUDA(cudaMemcpyAsync(out.data(), w.col.p, S * sizeof(sv::Col), cudaMemcpyDeviceToHost, s));
+  CBX_CUDA(cudaStreamSynchronize(s));
+}
+
+template <int S>
+struct Solver : public SolverBase {
+  Workspace<double, S> w64;
+  Workspace<float, S> w32;
+  DevBuf<double> dinv64, Bi, Xi, R64, Y64, part, scale;
+  DevBuf<float> dinv32, R32, D32;
+  double dinv_lam = std::nan("");
+
+  void prepare(cbx_handle* h, Mme& m, double lam, bool need32) {
+    cudaStream_t s = h->stream;
+    w64.alloc(m, h->num_sms);
+    const int64_t n = m.dim * S;
+    Bi.resize(n); Xi.resize(n); R64.resize(n); Y64.resize(n);
+    part.resize((size_t)w64.nblk_vec * S);
+    scale.resize(S);
+    if (!(dinv_lam == lam) || dinv64.n != (size_t)m.q) {
+      dinv64.resize(m.q);
+      k_dinv<double><<<grid_for(m.q, 256, 1024), 256, 0, s>>>(m.diagD.p, m.diagQ.p, m.p, m.q, lam, dinv64.p);
+      h->launched("k_dinv");
+      dinv32.resize(m.q);
+      k_dinv<float><<<grid_for(m.q, 256, 1024), 256, 0, s>>>(m.diagD.p, m.diagQ.p, m.p, m.q, lam, dinv32.p);
+      h->launched("k_dinv");
+      dinv_lam = lam;
+    }
+    if (need32) {
+      w32.alloc(m, h->num_sms);
+      R32.resize(n);
+      D32.resize(n);
+    }
+  }
+
+  // column norms of an interleaved FP64 block
+  std::vector<double> norms(cbx_handle* h, Mme& m, const double* V) {
+    cudaStream_t s = h->stream;
+    sv::k_colnorm2<S><<<w64.nblk_vec, sv::NT, 0, s>>>(V, m.dim, part.p);
+    h->launched("k_colnorm2");
+    std::vector<double> ph((size_t)w64.nblk_vec * S);
+    CBX_CUDA(cudaMemcpyAsync(ph.data(), part.p, ph.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+    CBX_CUDA(cudaStreamSynchronize(s));
+    std::vector<double> r(S, 0.0);
+    for (int c = 0; c < S; ++c) {
+      double t = 0;
+      for (int b = 0; b < w64.nblk_vec; ++b) t += ph[(size_t)b * S + c];
+      r[c] = std::sqrt(t);
+    }
+    return r;
+  }
+
+  // R64 = B - A X in FP64; returns ||R64|| per column
+  std::vector<double> residual(cbx_handle* h, Mme& m, const sv::OpView<double>& op, double lam, int64_t& mv) {
+    cudaStream_t s = h->stream;
+    matvec<double, S>(h, op, w64, Xi.p, Y64.p, lam, 1, nullptr, nullptr, nullptr);
+    ++mv;
+    const int64_t n = m.dim * S;
+    k_sub<<<grid_for(n, 256, 4 * h->num_sms), 256, 0, s>>>(Bi.p, Y64.p, n, R64.p);
+    h->launched("k_sub");
+    return norms(h, m, R64.p);
+  }
+
+  void solve(cbx_handle* h, Mme& m, double lam, int ncols, bool use_x0, double tol, int maxit, int abs_tol,
+             int precision, PcgResult& res) {
+    cudaStream_t s = h->stream;
+    prepare(h, m, lam, precision != 0);
+    auto op64 = make_view<double>(m, dinv64.p);
+    res.iters.assign(ncols, 0);
+    res.status.assign(ncols, 0);
+    res.relres.assign(ncols, 0.0);
+    res.refinements = 0;
+    res.matvecs = 0;
+    std::vector<double> tolv(ncols, tol);
+    if (precision == 0) {
+      std::vector<sv::Col> cols;
+      run_pcg<double, S>(h, m, op64, w64, lam, Bi.p, Xi.p, ncols, tolv.data(), abs_tol, maxit, use_x0, cols,
+                         res.matvecs);
+      bool need_true = false;
+      for (int c = 0; c < ncols; ++c) need_true |= cols[c].status != sv::COL_CONVERGED;
+      std::vector<double> rn, bn;
+      if (need_true) {
+        rn = residual(h, m, op64, lam, res.matvecs);
+        bn = norms(h, m, Bi.p);
+      }
+      for (int c = 0; c < ncols; ++c) {
+        res.iters[c] = cols[c].iters;
+        res.status[c] = cols[c].status;
+        const double b = cols[c].bnorm2 > 0 ? std::sqrt(cols[c].bnorm2) : 1.0;
+        if (cols[c].status == sv::COL_CONVERGED)
+          res.relres[c] = abs_tol ? std::sqrt(cols[c].rr) : std::sqrt(cols[c].rr) / b;
+        else
+          res.relres[c] = abs_tol ? rn[c] : (bn[c] > 0 ? rn[c] / bn[c] : 0.0);
+      }
+      return;
+    }
+    // ---- mixed precision: FP32 PCG on A d = r, x += d, r = b - A x in FP64
+    auto op32 = make_view<float>(m, dinv32.p);
+    const int64_t n = m.dim * S;
+    if (!use_x0) CBX_CUDA(cudaMemsetAsync(Xi.p, 0, n * sizeof(double), s));
+    std::vector<double> bn = norms(h, m, Bi.p);
+    for (auto& b : bn) if (!(b > 0)) b = 1.0;
+    std::vector<double> rn = residual(h, m, op64, lam, res.matvecs);
+    std::vector<int> done(ncols, 0);
+    for (int c = 0; c < ncols; ++c)
+      if ((abs_tol ? rn[c] : rn[c] / bn[c]) < tol) done[c] = 1;
+    for (int outer = 0; outer < 60; ++outer) {
+      std::vector<double> sc(S, 0.0), itol(S, 1.0);
+      int inner_max = 0;
+      for (int c = 0; c < ncols; ++c)
+        if (!done[c] && res.iters[c] < maxit) {
+          sc[c] = rn[c] > 0 ? rn[c] : 1.0;
+          const double need = abs_tol ? tol / rn[c] : tol * bn[c] / rn[c];
+          itol[c] = std::min(1e-2, std::max(1e-5, 0.5 * need));
+          inner_max = std::max(inner_max, maxit - res.iters[c]);
+        }
+      if (inner_max == 0) break;
+      CBX_CUDA(cudaMemcpyAsync(scale.p, sc.data(), S * sizeof(double), cudaMemcpyHostToDevice, s));
+      k_scale_down<<<grid_for(n, 256, 4 * h->num_sms), 256, 0, s>>>(R64.p, scale.p, m.dim, S, R32.p);
+      h->launched("k_scale_down");
+      std::vector<sv::Col> cols;
+      run_pcg<float, S>(h, m, op32, w32, lam, R32.p, D32.p, ncols, itol.data(), 0, inner_max, false, cols,
+                        res.matvecs);
+      k_accumulate<<<grid_for(n, 256, 4 * h->num_sms), 256, 0, s>>>(Xi.p, D32.p, scale.p, m.dim, S);
+      h->launched("k_accumulate");
+      res.refinements += 1;
+      std::vector<double> rn_new = residual(h, m, op64, lam, res.matvecs);
+      for (int c = 0; c < ncols; ++c) {
+        if (sc[c] <= 0) continue;
+        res.iters[c] += cols[c].iters;
+        const double rel = abs_tol ? rn_new[c] : rn_new[c] / bn[c];
+        if (rel < tol) done[c] = 1;
+        else if (!(rn_new[c] < 0.9 * rn[c])) done[c] = 2;  // FP32 refinement stalled
+        rn[c] = rn_new[c];
+      }
+    }
+    for (int c = 0; c < ncols; ++c) {
+      res.relres[c] = abs_tol ? rn[c] : rn[c] / bn[c];
+      res.status[c] = done[c] == 1 ? sv::COL_CONVERGED : sv::COL_MAXIT;
+    }
+  }
+
+  // Y = Qinv X on interleaved blocks (u part only is meaningful)
+  void qinv(cbx_handle* h, Mme& m) {
+    prepare(h, m, 1.0, false);
+    auto op = make_view<double>(m, dinv64.p);
+    matvec<double, S>(h, op, w64, Xi.p, Y64.p, 1.0, 0, nullptr, nullptr, nullptr);
+  }
+};
+
+template <int S>
+static Solver<S>& solver_for(Mme& m) {
+  constexpr int idx = S == 1 ? 0 : S == 2 ? 1 : S == 4 ? 2 : S == 8 ? 3 : S == 16 ? 4 : 5;
+  if (!m.solvers[idx]) m.solvers[idx].reset(new Solver<S>());
+  return *static_cast<Solver<S>*>(m.solvers[idx].get());
+}
+
+static int block_width(int ncols) {
+  int S = 1;
+  while (S < ncols && S < 32) S <<= 1;
+  return S;
+}
+
+template <int S>
+static void solve_chunk(cbx_handle* h, Mme& m, double lam, int nc, const double* B_cm, double* X_cm, bool use_x0,
+                        double tol, int maxit, int abs_tol, int precision, PcgResult& r) {
+  Solver<S>& sv_ = solver_for<S>(m);
+  sv_.prepare(h, m, lam, precision != 0);
+  cudaStream_t s = h->stream;
+  const int64_t n = m.dim * S;
+  k_to_inter<<<grid_for(n, 256, 4 * h->num_sms), 256, 0, s>>>(B_cm, m.dim, nc, S, sv_.Bi.p);
+  h->launched("k_to_inter");
+  if (use_x0) {
+    k_to_inter<<<grid_for(n, 256, 4 * h->num_sms), 256, 0, s>>>(X_cm, m.dim, nc, S, sv_.Xi.p);
+    h->launched("k_to_inter");
+  }
+  sv_.solve(h, m, lam, nc, use_x0, tol, maxit, abs_tol, precision, r);
+  k_from_inter<<<grid_for(m.dim * nc, 256, 4 * h->num_sms), 256, 0, s>>>(sv_.Xi.p, m.dim, nc, S, X_cm);
+  h->launched("k_from_inter");
+}
+
+void pcg_solve(cbx_handle* h, double lam, int ncols, const double* B_cm, double* X_cm, bool use_x0, double tol,
+               int maxit, int abs_tol, int precision, PcgResult& res) {
+  CBX_REQUIRE(h->mme, CBX_ERR_STATE, "no mixed-model equations on this handle (cbx_mme_create)");
+  Mme& m = *h->mme;
+  CBX_REQUIRE(m.has_dense || m.has_sparse, CBX_ERR_STATE, "Qinv not set (cbx_mme_set_qinv_*)");
+  res = PcgResult{};
+  for (int c0 = 0; c0 < ncols; c0 += 32) {
+    const int nc = std::min(32, ncols - c0);
+    PcgResult r;
+    const double* B = B_cm + (int64_t)c0 * m.dim;
+    double* X = X_cm + (int64_t)c0 * m.dim;
+    switch (block_width(nc)) {
+      case 1: solve_chunk<1>(h, m, lam, nc, B, X, use_x0, tol, maxit, abs_tol, precision, r); break;
+      case 2: solve_chunk<2>(h, m, lam, nc, B, X, use_x0, tol, maxit, abs_tol, precision, r); break;
+      case 4: solve_chunk<4>(h, m, lam, nc, B, X, use_x0, tol, maxit, abs_tol, precision, r); break;
+      case 8: solve_chunk<8>(h, m, lam, nc, B, X, use_x0, tol, maxit, abs_tol, precision, r); break;
+      case 16: solve_chunk<16>(h, m, lam, nc, B, X, use_x0, tol, maxit, abs_tol, precision, r); break;
+      default: solve_chunk<32>(h, m, lam, nc, B, X, use_x0, tol, maxit, abs_tol, precision, r); break;
+    }
+    res.iters.insert(res.iters.end(), r.iters.begin(), r.iters.end());
+    res.status.insert(res.status.end(), r.status.begin(), r.status.end());
+    res.relres.insert(res.relres.end(), r.relres.begin(), r.relres.end());
+    res.refinements += r.refinements;
+    res.matvecs += r.matvecs;
+  }
+}
+
+template <int S>
+static void qinv_chunk(cbx_handle* h, Mme& m, int nc, const double* X_cm, double* Y_cm) {
+  Solver<S>& sv_ = solver_for<S>(m);
+  sv_.prepare(h, m, 1.0, false);
+  cudaStream_t s = h->stream;
+  const int64_t n = m.dim * S;
+  // place the q-vectors in rows [p, dim) of a dim x nc column-major scratch
+  DevBuf<double>& tmp = m.io_x;
+  tmp.resize((size_t)m.dim * nc);
+  CBX_CUDA(cudaMemsetAsync(tmp.p, 0, (size_t)m.dim * nc * sizeof(double), s));
+  CBX_CUDA(cudaMemcpy2DAsync(tmp.p + m.p, m.dim * sizeof(double), X_cm, m.q * sizeof(double), m.q * sizeof(double),
+                             nc, cudaMemcpyDeviceToDevice, s));
+  k_to_inter<<<grid_for(n, 256, 4 * h->num_sms), 256, 0, s>>>(tmp.p, m.dim, nc, S, sv_.Xi.p);
+  h->launched("k_to_inter");
+  sv_.qinv(h, m);
+  k_from_inter<<<grid_for(m.dim * nc, 256, 4 * h->num_sms), 256, 0, s>>>(sv_.Y64.p, m.dim, nc, S, tmp.p);
+  h->launched("k_from_inter");
+  CBX_CUDA(cudaMemcpy2DAsync(Y_cm, m.q * sizeof(double), tmp.p + m.p, m.dim * sizeof(double), m.q * sizeof(double),
+                             nc, cudaMemcpyDeviceToDevice, s));
+}
+
+void qinv_apply(cbx_handle* h, int ncols, const double* X_cm, double* Y_cm) {
+  CBX_REQUIRE(h->mme, CBX_ERR_STATE, "no mixed-model equations on this handle");
+  Mme& m = *h->mme;
+  for (int c0 = 0; c0 < ncols; c0 += 32) {
+    const int nc = std::min(32, ncols - c0);
+    const double* X = X_cm + (int64_t)c0 * m.q;
+    double* Y = Y_cm + (int64_t)c0 * m.q;
+    switch (block_width(nc)) {
+      case 1: qinv_chunk<1>(h, m, nc, X, Y); break;
+      case 2: qinv_chunk<2>(h, m, nc, X, Y); break;
+      case 4: qinv_chunk<4>(h, m, nc, X, Y); break;
+      case 8: qinv_chunk<8>(h, m, nc, X, Y); break;
+      case 16: qinv_chunk<16>(h, m, nc, X, Y); break;
+      default: qinv_chunk<32>(h, m, nc, X, Y); break;
+    }
+  }
+}
+
+double record_residual(cbx_handle* h, const double* sol_dev, double* e_dev) {
+  Mme& m = *h->mme;
+  cudaStream_t s = h->stream;
+  const unsigned g = grid_for(m.n_rec, sv::NT, 2 * h->num_sms);
+  DevBuf<double> part;
+  part.resize(g);
+  sv::k_resid_records<<<g, sv::NT, 0, s>>>(m.n_rec, m.p, m.y.p, m.aid.p, m.q, m.x_ptr.p, m.x_col.p, m.x_val.p,
+                                           sol_dev, e_dev, part.p);
+  h->launched("k_resid_records");
+  std::vector<double> ph(g);
+  CBX_CUDA(cudaMemcpyAsync(ph.data(), part.p, g * sizeof(double), cudaMemcpyDeviceToHost, s));
+  CBX_CUDA(cudaStreamSynchronize(s));
+  double t = 0;
+  for (double v : ph) t += v;
+  return t;
+}
+
+// ---------------------------------------------------------------------------
+// host assembly helpers
+struct Trip {
+  int64_t r, c;
+  double v;
+};
+
+template <typename T>
+static void upload_csr(cudaStream_t s, int64_t rows, const std::vector<int32_t>& ptr, const std::vector<int32_t>& col,
+                       const std::vector<double>& val, Csr<T>& out) {
+  out.rows = (int32_t)rows;
+  out.nnz = (int64_t)col.size();
+  out.ptr.resize(rows + 1);
+  out.col.resize(std::max<size_t>(col.size(), 1));
+  out.val.resize(std::max<size_t>(val.size(), 1));
+  CBX_CUDA(cudaMemcpyAsync(out.ptr.p, ptr.data(), (rows + 1) * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+  if (!col.empty()) {
+    CBX_CUDA(cudaMemcpyAsync(out.col.p, col.data(), col.size() * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+    std::vector<T> tv(val.begin(), val.end());
+    CBX_CUDA(cudaMemcpyAsync(out.val.p, tv.data(), tv.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+    CBX_CUDA(cudaStreamSynchronize(s));
+  }
+}
+
+// Sort triplets by (row, col) keeping insertion order among duplicates, then sum duplicates.
+static void triplets_to_csr(int64_t rows, std::vector<Trip>& t, std::vector<int32_t>& ptr, std::vector<int32_t>& col,
+                            std::vector<double>& val) {
+  std::stable_sort(t.begin(), t.end(), [](const Trip& a, const Trip& b) { return a.r != b.r ? a.r < b.r : a.c < b.c; });
+  ptr.assign(rows + 1, 0);
+  col.clear();
+  val.clear();
+  for (size_t k = 0; k < t.size();) {
+    size_t e = k;
+    double v = 0.0;
+    while (e < t.size() && t[e].r == t[k].r && t[e].c == t[k].c) v += t[e++].v;
+    col.push_back((int32_t)t[k].c);
+    val.push_back(v);
+    ptr[t[k].r + 1]++;
+    k = e;
+  }
+  for (int64_t i = 0; i < rows; ++i) ptr[i + 1] += ptr[i];
+}
+
+// In-place Cholesky inverse of an SPD matrix (row-major n x n); false if not SPD.
+static bool spd_inverse(std::vector<double>& A, int64_t n) {
+  std::vector<double> L(A);
+  for (int64_t j = 0; j < n; ++j) {
+    double d = L[j * n + j];
+    for (int64_t k = 0; k < j; ++k) d -= L[j * n + k] * L[j * n + k];
+    if (!(d > 0)) return false;
+    d = std::sqrt(d);
+    L[j * n + j] = d;
+    for (int64_t i = j + 1; i < n; ++i) {
+      double v = L[i * n + j];
+      for (int64_t k = 0; k < j; ++k) v -= L[i * n + k] * L[j * n + k];
+      L[i * n + j] = v / d;
+    }
+  }
+  // inverse via solves with identity columns
+  std::vector<double> inv(n * n, 0.0), y(n);
+  for (int64_t c = 0; c < n; ++c) {
+    for (int64_t i = 0; i < n; ++i) {
+      double v = (i == c) ? 1.0 : 0.0;
+      for (int64_t k = 0; k < i; ++k) v -= L[i * n + k] * y[k];
+      y[i] = v / L[i * n + i];
+    }
+    for (int64_t i = n - 1; i >= 0; --i) {
+      double v = y[i];
+      for (int64_t k = i + 1; k < n; ++k) v -= L[k * n + i] * inv[k * n + c];
+      inv[i * n + c] = v / L[i * n + i];
+    }
+  }
+  A.swap(inv);
+  return true;
+}
+
+}  // namespace cbx
+
+using namespace cbx;
+
+extern "C" int cbx_mme_create(cbx_handle* h, int64_t n_rec, int64_t p, int64_t q, const double* y,
+                              const int32_t* aid, const int64_t* fx_ptr, const int32_t* fx_col,
+                              const double* fx_val) {
+  return cbx_guard(h, [&] {
+    CBX_REQUIRE(n_rec > 0 && p >= 0 && q > 0, CBX_ERR_ARG, "n_rec, q must be positive and p >= 0");
+    CBX_REQUIRE(y && aid && fx_ptr, CBX_ERR_ARG, "null record arrays");
+    CBX_REQUIRE(fx_ptr[0] == 0, CBX_ERR_ARG, "fx_ptr[0] must be 0");
+    CBX_CUDA(cudaSetDevice(h->device));
+    cudaStream_t s = h->stream;
+    auto m = std::make_unique<Mme>();
+    m->n_rec = n_rec; m->p = p; m->q = q; m->dim = p + q;
+    const int64_t dim = p + q;
+    // W'W triplets in record order (mme_builder.cpp:107-176) and W'y (:321-387)
+    std::vector<Trip> t;
+    t.reserve((size_t)n_rec * 8);
+    std::vector<double> rhs(dim, 0.0);
+    std::vector<double> A11((size_t)p * p, 0.0);
+    double yty = 0.0;
+    for (int64_t i = 0; i < n_rec; ++i) {
+      CBX_REQUIRE(fx_ptr[i + 1] >= fx_ptr[i], CBX_ERR_ARG, "fx_ptr not monotone");
+      CBX_REQUIRE(std::isfinite(y[i]), CBX_ERR_NONFINITE, "non-finite phenotype");
+      const int64_t a0 = fx_ptr[i], a1 = fx_ptr[i + 1];
+      for (int64_t a = a0; a < a1; ++a) {
+        CBX_REQUIRE(fx_col[a] >= 0 && fx_col[a] < p, CBX_ERR_ARG, "fixed-effect column out of range");
+        for (int64_t b = a; b < a1; ++b) {
+          const double v = fx_val[a] * fx_val[b];
+          t.push_back({fx_col[a], fx_col[b], v});
+          if (fx_col[a] != fx_col[b]) t.push_back({fx_col[b], fx_col[a], v});
+        }
+        rhs[fx_col[a]] += fx_val[a] * y[i];
+      }
+      const int32_t an = aid[i];
+      if (an > 0 && an <= q) {
+        const int64_t ck = p + an - 1;
+        for (int64_t a = a0; a < a1; ++a) {
+          t.push_back({fx_col[a], ck, fx_val[a]});
+          t.push_back({ck, fx_col[a], fx_val[a]});
+        }
+        t.push_back({ck, ck, 1.0});
+        rhs[ck] += y[i];
+      }
+      yty += y[i] * y[i];
+    }
+    std::vector<int32_t> ptr, col;
+    std::vector<double> val;
+    triplets_to_csr(dim, t, ptr, col, val);
+    CBX_REQUIRE(col.size() < (size_t)INT32_MAX, CBX_ERR_UNSUPPORTED, "W'W has more than 2^31 entries");
+    std::vector<double> diag(dim, 0.0);
+    for (int64_t i = 0; i < dim; ++i)
+      for (int32_t j = ptr[i]; j < ptr[i + 1]; ++j) {
+        if (col[j] == i) diag[i] = val[j];
+        if (i < p && col[j] < p) A11[i * p + col[j]] = val[j];
+      }
+    upload_csr<double>(s, dim, ptr, col, val, m->D64);
+    upload_csr<float>(s, dim, ptr, col, val, m->D32);
+    m->diagD.resize(dim);
+    CBX_CUDA(cudaMemcpyAsync(m->diagD.p, diag.data(), dim * sizeof(double), cudaMemcpyHostToDevice, s));
+    m->rhs.resize(dim);
+    CBX_CUDA(cudaMemcpyAsync(m->rhs.p, rhs.data(), dim * sizeof(double), cudaMemcpyHostToDevice, s));
+    // block-Jacobi fixed block: (X'X + ridge I)^-1, ridge = max(1e-8 max|diag|, 1e-6) (pcg_solver.h:78-85)
+    if (p > 0) {
+      double maxd = 0.0;
+      for (int64_t i = 0; i < p; ++i) maxd = std::max(maxd, std::fabs(A11[i * p + i]));
+      const double ridge = std::max(1e-8 * maxd, 1e-6);
+      std::vector<double> M(A11);
+      for (int64_t i = 0; i < p; ++i) M[i * p + i] += ridge;
+      if (!spd_inverse(M, p)) {
+        // reference fallback: diagonal scaling of the fixed block (pcg_solver.h:108-116)
+        M.assign((size_t)p * p, 0.0);
+        for (int64_t i = 0; i < p; ++i) M[i * p + i] = std::fabs(diag[i]) > 1e-14 ? 1.0 / diag[i] : 1.0;
+      }
+      m->A11inv64.resize((size_t)p * p);
+      CBX_CUDA(cudaMemcpyAsync(m->A11inv64.p, M.data(), M.size() * sizeof(double), cudaMemcpyHostToDevice, s));
+      m->A11inv32.resize((size_t)p * p);
+      k_convert<double, float><<<grid_for(p * p, 256, 1024), 256, 0, s>>>(m->A11inv64.p, m->A11inv32.p, p * p);
+      h->launched("k_convert");
+    }
+    // records
+    m->y.resize(n_rec);
+    CBX_CUDA(cudaMemcpyAsync(m->y.p, y, n_rec * sizeof(double), cudaMemcpyHostToDevice, s));
+    m->aid.resize(n_rec);
+    CBX_CUDA(cudaMemcpyAsync(m->aid.p, aid, n_rec * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+    std::vector<int32_t> xp(n_rec + 1);
+    for (int64_t i = 0; i <= n_rec; ++i) xp[i] = (int32_t)fx_ptr[i];
+    const int64_t nx = fx_ptr[n_rec];
+    m->x_ptr.resize(n_rec + 1);
+    CBX_CUDA(cudaMemcpyAsync(m->x_ptr.p, xp.data(), (n_rec + 1) * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+    m->x_col.resize(std::max<int64_t>(nx, 1));
+    m->x_val.resize(std::max<int64_t>(nx, 1));
+    if (nx > 0) {
+      CBX_CUDA(cudaMemcpyAsync(m->x_col.p, fx_col, nx * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+      CBX_CUDA(cudaMemcpyAsync(m->x_val.p, fx_val, nx * sizeof(double), cudaMemcpyHostToDevice, s));
+    }
+    m->y_host.assign(y, y + n_rec);
+    m->yty = yty;
+    CBX_CUDA(cudaStreamSynchronize(s));
+    h->mme = std::move(m);
+  });
+}
+
+// Dense Qinv (q x q, symmetric, row- or column-major alike).  Qinv == NULL uses
+// the matrix left on the device by cbx_invert_psd_g.
+extern "C" int cbx_mme_set_qinv_dense(cbx_handle* h, const double* Qinv, int64_t q) {
+  return cbx_guard(h, [&] {
+    CBX_REQUIRE(h->mme, CBX_ERR_STATE, "call cbx_mme_create first");
+    Mme& m = *h->mme;
+    CBX_REQUIRE(q == m.q, CBX_ERR_ARG, "Qinv order does not match q");
+    CBX_CUDA(cudaSetDevice(h->device));
+    cudaStream_t s = h->stream;
+    const double* src = nullptr;
+    DevBuf<double> tmp;
+    if (Qinv) {
+      tmp.resize((size_t)q * q);
+      CBX_CUDA(cudaMemcpyAsync(tmp.p, Qinv, (size_t)q * q * sizeof(double), cudaMemcpyHostToDevice, s));
+      src = tmp.p;
+    } else {
+      CBX_REQUIRE(h->Ginv.p && h->Ginv_n == q, CBX_ERR_STATE, "no device G inverse of matching order");
+      src = h->Ginv.p;
+    }
+    m.ng = q;
+    m.ld = (q + 3) / 4 * 4;
+    m.Qd64.resize((size_t)q * m.ld);
+    m.Qd32.resize((size_t)q * m.ld);
+    k_pitch_copy<double><<<grid_for(q * m.ld, 256, 8 * h->num_sms), 256, 0, s>>>(src, q, m.ld, m.Qd64.p);
+    h->launched("k_pitch_copy");
+    k_pitch_copy<float><<<grid_for(q * m.ld, 256, 8 * h->num_sms), 256, 0, s>>>(src, q, m.ld, m.Qd32.p);
+    h->launched("k_pitch_copy");
+    std::vector<int32_t> idm(q);
+    for (int64_t i = 0; i < q; ++i) idm[i] = (int32_t)i;
+    m.gmap.resize(q);
+    m.ginv.resize(q);
+    CBX_CUDA(cudaMemcpyAsync(m.gmap.p, idm.data(), q * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+    CBX_CUDA(cudaMemcpyAsync(m.ginv.p, idm.data(), q * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+    // diag(Qinv)
+    m.diagQ.resize(q);
+    CBX_CUDA(cudaMemcpy2DAsync(m.diagQ.p, sizeof(double), src, (q + 1) * sizeof(double), sizeof(double), q,
+                               cudaMemcpyDeviceToDevice, s));
+    m.has_dense = true;
+    m.has_sparse = false;
+    CBX_CUDA(cudaStreamSynchronize(s));
+    for (auto& sp : m.solvers) sp.reset();
+  });
+}
+
+// Split Qinv = A (CSR, q x q) + S Gd S^T with Gd dense ng x ng (row-major) and
+// gmap[k] the u-index of dense row k (SplitMatrixAdapter::operator*).
+extern "C" int cbx_mme_set_qinv_split(cbx_handle* h, const int64_t* a_ptr, const int32_t* a_col,
+                                      const double* a_val, const double* Gd, int64_t ng,
+                                      const int32_t* gmap) {
+  return cbx_guard(h, [&] {
+    CBX_REQUIRE(h->mme, CBX_ERR_STATE, "call cbx_mme_create first");
+    Mme& m = *h->mme;
+    CBX_REQUIRE(a_ptr && a_ptr[0] == 0, CBX_ERR_ARG, "bad A^-1 CSR");
+    CBX_REQUIRE(ng >= 0 && ng <= m.q, CBX_ERR_ARG, "bad dense block order");
+    CBX_CUDA(cudaSetDevice(h->device));
+    cudaStream_t s = h->stream;
+    const int64_t q = m.q;
+    std::vector<int32_t> ptr(q + 1), col(a_col, a_col + a_ptr[q]);
+    std::vector<double> val(a_val, a_val + a_ptr[q]);
+    for (int64_t i = 0; i <= q; ++i) ptr[i] = (int32_t)a_ptr[i];
+    std::vector<double> diag(q, 0.0);
+    for (int64_t i = 0; i < q; ++i)
+      for (int64_t j = a_ptr[i]; j < a_ptr[i + 1]; ++j) {
+        CBX_REQUIRE(a_col[j] >= 0 && a_col[j] < q, CBX_ERR_ARG, "A^-1 column out of range");
+        if (a_col[j] == i) diag[i] += a_val[j];
+      }
+    upload_csr<double>(s, q, ptr, col, val, m.Qs64);
+    upload_csr<float>(s, q, ptr, col, val, m.Qs32);
+    m.has_sparse = true;
+    m.has_dense = ng > 0;
+    if (ng > 0) {
+      CBX_REQUIRE(Gd && gmap, CBX_ERR_ARG, "dense block or map missing");
+      std::vector<int32_t> inv(q, -1);
+      for (int64_t k = 0; k < ng; ++k) {
+        CBX_REQUIRE(gmap[k] >= 0 && gmap[k] < q, CBX_ERR_ARG, "genotyped map out of range");
+        CBX_REQUIRE(inv[gmap[k]] < 0, CBX_ERR_ARG, "genotyped map has duplicates");
+        inv[gmap[k]] = (int32_t)k;
+        diag[gmap[k]] += Gd[k * ng + k];
+      }
+      DevBuf<double> tmp;
+      tmp.resize((size_t)ng * ng);
+      CBX_CUDA(cudaMemcpyAsync(tmp.p, Gd, (size_t)ng * ng * sizeof(double), cudaMemcpyHostToDevice, s));
+      m.ng = ng;
+      m.ld = (ng + 3) / 4 * 4;
+      m.Qd64.resize((size_t)ng * m.ld);
+      m.Qd32.resize((size_t)ng * m.ld);
+      k_pitch_copy<double><<<grid_for(ng * m.ld, 256, 8 * h->num_sms), 256, 0, s>>>(tmp.p, ng, m.ld, m.Qd64.p);
+      h->launched("k_pitch_copy");
+      k_pitch_copy<float><<<grid_for(ng * m.ld, 256, 8 * h->num_sms), 256, 0, s>>>(tmp.p, ng, m.ld, m.Qd32.p);
+      h->launched("k_pitch_copy");
+      m.gmap.resize(ng);
+      m.ginv.resize(q);
+      CBX_CUDA(cudaMemcpyAsync(m.gmap.p, gmap, ng * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+      CBX_CUDA(cudaMemcpyAsync(m.ginv.p, inv.data(), q * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+      CBX_CUDA(cudaStreamSynchronize(s));
+    }
+    m.diagQ.resize(q);
+    CBX_CUDA(cudaMemcpyAsync(m.diagQ.p, diag.data(), q * sizeof(double), cudaMemcpyHostToDevice, s));
+    CBX_CUDA(cudaStreamSynchronize(s));
+    for (auto& sp : m.solvers) sp.reset();
+  });
+}
+
+extern "C" int cbx_pcg_solve(cbx_handle* h, double lambda, int32_t nrhs, const double* B, double* X,
+                             int32_t use_x0, double tol, int32_t maxit, int32_t tol_mode,
+                             int32_t precision, int32_t* iters, double* relres) {
+  return cbx_guard(h, [&] {
+    CBX_REQUIRE(h->mme, CBX_ERR_STATE, "call cbx_mme_create first");
+    CBX_REQUIRE(nrhs > 0 && B && X, CBX_ERR_ARG, "bad right-hand sides");
+    CBX_REQUIRE(maxit > 0 && tol > 0, CBX_ERR_ARG, "tol and maxit must be positive");
+    CBX_REQUIRE(precision == 0 || precision == 1, CBX_ERR_ARG, "precision must be 0 (fp64) or 1 (mixed)");
+    CBX_REQUIRE(std::isfinite(lambda), CBX_ERR_NONFINITE, "non-finite lambda");
+    CBX_CUDA(cudaSetDevice(h->device));
+    Mme& m = *h->mme;
+    cudaStream_t s = h->stream;
+    const size_t n = (size_t)m.dim * nrhs;
+    m.io_b.resize(n);
+    DevBuf<double> xb;
+    xb.resize(n);
+    CBX_CUDA(cudaMemcpyAsync(m.io_b.p, B, n * sizeof(double), cudaMemcpyHostToDevice, s));
+    if (use_x0) CBX_CUDA(cudaMemcpyAsync(xb.p, X, n * sizeof(double), cudaMemcpyHostToDevice, s));
+    PcgResult r;
+    pcg_solve(h, lambda, nrhs, m.io_b.p, xb.p, use_x0 != 0, tol, maxit, tol_mode, precision, r);
+    CBX_CUDA(cudaMemcpyAsync(X, xb.p, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    CBX_CUDA(cudaStreamSynchronize(s));
+    for (int c = 0; c < nrhs; ++c) {
+      if (iters) iters[c] = r.iters[c];
+      if (relres) relres[c] = r.relres[c];
+    }
+    for (int c = 0; c < nrhs; ++c) {
+      if (r.status[c] == sv::COL_NONFINITE) throw Error(CBX_ERR_NONFINITE, "non-finite PCG iterate");
+      if (r.status[c] == sv::COL_BREAKDOWN) throw Error(CBX_ERR_BREAKDOWN, "PCG breakdown");
+    }
+  });
+}
+
+extern "C" int cbx_qinv_apply(cbx_handle* h, int32_t nrhs, const double* X, double* Y) {
+  return cbx_guard(h, [&] {
+    CBX_REQUIRE(h->mme, CBX_ERR_STATE, "call cbx_mme_create first");
+    CBX_REQUIRE(nrhs > 0 && X && Y, CBX_ERR_ARG, "bad vectors");
+    CBX_CUDA(cudaSetDevice(h->device));
+    Mme& m = *h->mme;
+    cudaStream_t s = h->stream;
+    const size_t n = (size_t)m.q * nrhs;
+    DevBuf<double> xd, yd;
+    xd.resize(n);
+    yd.resize(n);
+    CBX_CUDA(cudaMemcpyAsync(xd.p, X, n * sizeof(double), cudaMemcpyHostToDevice, s));
+    qinv_apply(h, nrhs, xd.p, yd.p);
+    CBX_CUDA(cudaMemcpyAsync(Y, yd.p, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    CBX_CUDA(cudaStreamSynchronize(s));
+  });
+}

@@ -1,0 +1,67 @@
+// Device-resident mixed-model equations (one random component).
+//
+// LHS(lambda) = D + lambda [0 0; 0 Qinv], with
+//   D    = W'W as CSR over dim = p + q rows (W = [X Z], records on the host),
+//   Qinv = Qs + S Qd S^T: Qs an optional sparse q x q CSR (A^-1 in ssGBLUP),
+//          Qd an optional dense ng x ng block (G^-1, or G_blend^-1 - A22^-1
+//          pre-combined), S the genotyped scatter map (ng -> [0, q)).
+// FP64 copies drive refinement and the plain FP64 path; FP32 copies drive the
+// mixed-precision bulk iterations.
+#pragma once
+#include <memory>
+#include <vector>
+#include "devbuf.h"
+
+namespace cbx {
+
+template <typename T>
+struct Csr {
+  int32_t rows = 0;
+  int64_t nnz = 0;
+  DevBuf<int32_t> ptr;  // rows + 1 (int32 offsets; nnz < 2^31)
+  DevBuf<int32_t> col;
+  DevBuf<T> val;
+};
+
+// Type-erased per-RHS-count solver workspace (see mme.cu).
+struct SolverBase {
+  virtual ~SolverBase() = default;
+};
+
+struct Mme {
+  int64_t n_rec = 0, p = 0, q = 0, dim = 0;
+  // records
+  DevBuf<double> y;                // n_rec
+  DevBuf<int32_t> aid;             // n_rec, 1-based into Qinv, 0 = none
+  DevBuf<int32_t> x_ptr, x_col;    // fixed-effect design CSR (n_rec rows)
+  DevBuf<double> x_val;
+  Csr<double> D64;                 // W'W
+  Csr<float> D32;
+  DevBuf<double> rhs;              // W'y (dim)
+  DevBuf<double> diagD;            // diag(W'W) (dim)
+  // Qinv
+  bool has_dense = false, has_sparse = false;
+  int64_t ng = 0, ld = 0;          // dense block order and row pitch (multiple of 4)
+  DevBuf<double> Qd64;             // ng x ld row-major
+  DevBuf<float> Qd32;
+  DevBuf<int32_t> gmap;            // ng -> u index
+  DevBuf<int32_t> ginv;            // q -> dense index or -1
+  Csr<double> Qs64;
+  Csr<float> Qs32;
+  DevBuf<double> diagQ;            // diag(Qinv) (q)
+  // block-Jacobi fixed block: (X'X + ridge I)^-1, p x p
+  DevBuf<double> A11inv64;
+  DevBuf<float> A11inv32;
+  // host copies used by the REML driver
+  std::vector<double> y_host;
+  double yty = 0.0;
+  // warm start of the data solve (the reference keeps last_solution)
+  DevBuf<double> last_solution;
+  bool has_last = false;
+  // persistent solver workspaces, indexed by log2 of the RHS block width
+  std::unique_ptr<SolverBase> solvers[6];
+  // scratch column-major buffers of the C ABI
+  DevBuf<double> io_b, io_x;
+};
+
+}  // namespace cbx

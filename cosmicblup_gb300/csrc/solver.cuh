@@ -1,0 +1,465 @@
+// Kernels of the mixed-model operator and of the multi-right-hand-side PCG.
+//
+// Vectors hold S right-hand sides interleaved: element (row i, column c) at
+// v[i * S + c].  Every column runs its own CG recurrence (the reference's
+// PCGSolver::solve, src/core/pcg_solver.h:436-536, applied to S systems at
+// once); the matrix is read once per iteration for all columns.  All
+// reductions are deterministic: per-block partial sums are combined in a fixed
+// order by the scalar kernels.
+#pragma once
+#include <cuda_fp16.h>
+#include "mme.h"
+
+namespace cbx {
+namespace sv {
+
+constexpr int NT = 256;  // threads per block of the vector kernels
+
+// Per-column CG state (device).
+struct Col {
+  double rz, pq, rr, bnorm2, alpha, beta;
+  int active, iters, restarted, skip, status;
+  int pad;
+};
+enum ColStatus : int { COL_RUNNING = 0, COL_CONVERGED = 1, COL_MAXIT = 2, COL_BREAKDOWN = 3,
+                       COL_NONFINITE = 4 };
+
+// Read-only view of the operator in one precision.
+template <typename T>
+struct OpView {
+  int64_t p, q, dim;
+  const int32_t* Dptr; const int32_t* Dcol; const T* Dval;
+  const int32_t* Sptr; const int32_t* Scol; const T* Sval;  // null if no sparse part
+  const T* Qd; int64_t ng, ld; const int32_t* gmap; const int32_t* ginv;  // null if no dense part
+  const T* A11inv;  // p x p
+  const T* dinv;    // q (Jacobi of the random part)
+};
+
+template <typename T> struct Vec16;
+template <> struct Vec16<float> { using type = float4; static constexpr int n = 4; };
+template <> struct Vec16<double> { using type = double2; static constexpr int n = 2; };
+
+__device__ __forceinline__ float dot16(const float4& a, const float4& b) {
+  return a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w;
+}
+__device__ __forceinline__ double dot16(const double2& a, const double2& b) {
+  return a.x * b.x + a.y * b.y;
+}
+
+// Vt[c * ld + k] = X[(p + gmap[k]) * S + c] for k < ng, 0 for ng <= k < ld.
+template <typename T, int S>
+__global__ void k_gather_t(const T* __restrict__ X, T* __restrict__ Vt, int64_t p, int64_t ng,
+                           int64_t ld, const int32_t* __restrict__ gmap,
+                           const int* __restrict__ active) {
+  if (active && *active == 0) return;
+  const int64_t total = (int64_t)S * ld;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = idx / ld, k = idx - c * ld;
+    Vt[idx] = k < ng ? X[(p + gmap[k]) * S + c] : T(0);
+  }
+}
+
+// Dense block product Tout[i * S + c] = sum_k Qd[i * ld + k] * Vt[c * ld + k].
+// 8 warps per block, RPW rows per warp; lanes stream 16-byte vectors of each
+// row; the S right-hand sides of a K tile are staged in shared memory.
+template <typename T, int S, int RPW>
+__global__ void __launch_bounds__(256) k_dense(const T* __restrict__ Qd, int64_t ng, int64_t ld,
+                                               const T* __restrict__ Vt, T* __restrict__ Tout,
+                                               const int* __restrict__ active) {
+  if (active && *active == 0) return;
+  using V = typename Vec16<T>::type;
+  constexpr int VEC = Vec16<T>::n;
+  constexpr int KT = 32 * VEC * 4;
+  extern __shared__ __align__(16) uint8_t dsm[];
+  T* vt = reinterpret_cast<T*>(dsm);  // [S][KT]
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int64_t row0 = (int64_t)blockIdx.x * (8 * RPW) + warp * RPW;
+  T acc[RPW][S];
+#pragma unroll
+  for (int r = 0; r < RPW; ++r)
+#pragma unroll
+    for (int c = 0; c < S; ++c) acc[r][c] = T(0);
+  for (int64_t k0 = 0; k0 < ld; k0 += KT) {
+    __syncthreads();
+    for (int v = tid; v < S * (KT / VEC); v += 256) {
+      const int c = v / (KT / VEC), kk = (v % (KT / VEC)) * VEC;
+      V val;
+      if (k0 + kk < ld) val = *reinterpret_cast<const V*>(Vt + (int64_t)c * ld + k0 + kk);
+      else memset(&val, 0, sizeof(V));
+      *reinterpret_cast<V*>(vt + c * KT + kk) = val;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int kk = u * 32 * VEC + lane * VEC;
+      if (k0 + kk < ld) {
+        V a[RPW];
+#pragma unroll
+        for (int r = 0; r < RPW; ++r) {
+          if (row0 + r < ng) a[r] = __ldg(reinterpret_cast<const V*>(Qd + (row0 + r) * ld + k0 + kk));
+          else memset(&a[r], 0, sizeof(V));
+        }
+#pragma unroll
+        for (int c = 0; c < S; ++c) {
+          const V b = *reinterpret_cast<const V*>(vt + c * KT + kk);
+#pragma unroll
+          for (int r = 0; r < RPW; ++r) acc[r][c] += dot16(a[r], b);
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < RPW; ++r) {
+#pragma unroll
+    for (int c = 0; c < S; ++c) {
+      T v = acc[r][c];
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+      acc[r][c] = v;
+    }
+    if (lane == 0 && row0 + r < ng) {
+#pragma unroll
+      for (int c = 0; c < S; ++c) Tout[(row0 + r) * S + c] = acc[r][c];
+    }
+  }
+}
+
+// Block-level sum of one double per thread, grouped by column c = tid % S.
+// Returns the total for column (tid % S) in threads tid < S.
+template <int S>
+__device__ __forceinline__ double block_sum_cols(double v, double* red /*[NT]*/) {
+  const int tid = threadIdx.x;
+#pragma unroll
+  for (int off = 16; off >= S; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+  // now lanes < S of each warp hold that warp's per-column sums
+  const int warp = tid >> 5, lane = tid & 31;
+  if (lane < S) red[warp * S + lane] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (tid < S) {
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w * S + tid];
+  }
+  __syncthreads();
+  return t;
+}
+
+// Y = use_D * D X + lam * [0; Qs X_u + scatter(Tout)]; optional pq partials sum_i P[i]Y[i].
+// Blocks [0, nfix) take fixed-effect rows (one block per row); the others take
+// random-effect rows, one warp per row, in a grid-stride loop.
+template <typename T, int S>
+__global__ void __launch_bounds__(NT) k_spmv(OpView<T> op, const T* __restrict__ X,
+                                             const T* __restrict__ Tout, T lam, int use_D,
+                                             T* __restrict__ Y, const T* __restrict__ P,
+                                             double* __restrict__ pq_part,
+                                             const int* __restrict__ active) {
+  if (active && *active == 0) return;
+  __shared__ double red[NT];
+  __shared__ T redT[NT];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int64_t p = op.p;
+  const int nfix = (int)p;
+  double pq = 0.0;  // this thread's share for column tid % S
+  if ((int)blockIdx.x < nfix) {
+    const int64_t i = blockIdx.x;
+    constexpr int G = NT / S;
+    const int c = tid % S, g = tid / S;
+    T acc = T(0);
+    if (use_D) {
+      for (int32_t j = op.Dptr[i] + g; j < op.Dptr[i + 1]; j += G)
+        acc += op.Dval[j] * X[(int64_t)op.Dcol[j] * S + c];
+    }
+    // reduce over the G groups of this column
+    redT[tid] = acc;
+    __syncthreads();
+    if (tid < S) {
+      T s = T(0);
+      for (int gg = 0; gg < G; ++gg) s += redT[gg * S + tid];
+      Y[i * S + tid] = s;
+      if (P) pq = (double)P[i * S + tid] * (double)s;
+    }
+    __syncthreads();
+  } else {
+    constexpr int G = 32 / S;
+    const int c = lane % S, g = lane / S;
+    const int64_t nwarps = (int64_t)(gridDim.x - nfix) * (NT / 32);
+    for (int64_t i = p + (int64_t)(blockIdx.x - nfix) * (NT / 32) + warp; i < op.dim; i += nwarps) {
+      T acc = T(0);
+      if (use_D) {
+        for (int32_t j = op.Dptr[i] + g; j < op.Dptr[i + 1]; j += G)
+          acc += op.Dval[j] * X[(int64_t)op.Dcol[j] * S + c];
+      }
+      T qv = T(0);
+      const int64_t u = i - p;
+      if (op.Sptr) {
+        for (int32_t j = op.Sptr[u] + g; j < op.Sptr[u + 1]; j += G)
+          qv += op.Sval[j] * X[(p + op.Scol[j]) * S + c];
+      }
+#pragma unroll
+      for (int off = 16; off >= S; off >>= 1) {
+        acc += __shfl_xor_sync(0xffffffffu, acc, off);
+        qv += __shfl_xor_sync(0xffffffffu, qv, off);
+      }
+      if (lane < S) {
+        if (op.Qd) {
+          const int32_t k = op.ginv[u];
+          if (k >= 0) qv += Tout[(int64_t)k * S + c];
+        }
+        const T yv = acc + lam * qv;
+        Y[i * S + c] = yv;
+        if (P) pq += (double)P[i * S + c] * (double)yv;
+      }
+    }
+  }
+  if (pq_part) {
+    // threads tid < S hold pq for column tid in the fixed branch; lanes < S per warp otherwise
+    double v = pq;
+    if ((int)blockIdx.x < nfix) {
+      if (tid < S) pq_part[(int64_t)blockIdx.x * S + tid] = v;
+    } else {
+      const double t = block_sum_cols<S>(lane < S ? v : 0.0, red);
+      if (tid < S) pq_part[(int64_t)blockIdx.x * S + tid] = t;
+    }
+  }
+}
+
+// r = b - Y, z = M^-1 r on random rows, partial sums of r'r, r'z (random rows) and b'b.
+template <typename T, int S>
+__global__ void __launch_bounds__(NT) k_init_resid(OpView<T> op, const T* __restrict__ B,
+                                                   const T* __restrict__ Y, int have_Y,
+                                                   T* __restrict__ R, T* __restrict__ Z,
+                                                   double* __restrict__ part /*[grid][3][S]*/) {
+  __shared__ double red[NT];
+  double rr = 0, rz = 0, bb = 0;
+  const int64_t total = op.dim * S;
+  for (int64_t idx = blockIdx.x * (int64_t)NT + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * NT) {
+    const int64_t i = idx / S;
+    const T b = B[idx];
+    const T r = have_Y ? b - Y[idx] : b;
+    R[idx] = r;
+    rr += (double)r * r;
+    bb += (double)b * b;
+    if (i >= op.p) {
+      const T z = op.dinv[i - op.p] * r;
+      Z[idx] = z;
+      rz += (double)r * z;
+    }
+  }
+  const int c = threadIdx.x % S;
+  double t;
+  t = block_sum_cols<S>(rr, red);
+  if (threadIdx.x < S) part[((int64_t)blockIdx.x * 3 + 0) * S + c] = t;
+  t = block_sum_cols<S>(rz, red);
+  if (threadIdx.x < S) part[((int64_t)blockIdx.x * 3 + 1) * S + c] = t;
+  t = block_sum_cols<S>(bb, red);
+  if (threadIdx.x < S) part[((int64_t)blockIdx.x * 3 + 2) * S + c] = t;
+}
+
+// Fixed rows: z_f = A11inv r_f, partial r_f'z_f per row.  One block per fixed row.
+template <typename T, int S>
+__global__ void __launch_bounds__(NT) k_fixed(OpView<T> op, const T* __restrict__ R,
+                                              T* __restrict__ Z, const Col* __restrict__ col,
+                                              double* __restrict__ rz_fix /*[p][S]*/) {
+  __shared__ T redT[NT];
+  const int64_t f = blockIdx.x;
+  constexpr int G = NT / S;
+  const int tid = threadIdx.x, c = tid % S, g = tid / S;
+  T acc = T(0);
+  for (int64_t k = g; k < op.p; k += G) acc += op.A11inv[f * op.p + k] * R[k * S + c];
+  redT[tid] = acc;
+  __syncthreads();
+  if (tid < S) {
+    T s = T(0);
+    for (int gg = 0; gg < G; ++gg) s += redT[gg * S + tid];
+    const bool act = col == nullptr || col[tid].active;
+    if (act) Z[f * S + tid] = s;
+    const T zf = act ? s : Z[f * S + tid];
+    rz_fix[f * S + tid] = (double)R[f * S + tid] * (double)zf;
+  }
+}
+
+// x += alpha p, r -= alpha q (active, non-skipped columns), z = Jacobi r on random
+// rows; partial sums of r'r and r'z (random rows).
+template <typename T, int S>
+__global__ void __launch_bounds__(NT) k_update(OpView<T> op, const Col* __restrict__ col,
+                                               T* __restrict__ Xs, T* __restrict__ R,
+                                               T* __restrict__ Z, const T* __restrict__ P,
+                                               const T* __restrict__ Q,
+                                               double* __restrict__ part /*[grid][2][S]*/) {
+  __shared__ double red[NT];
+  double rr = 0, rz = 0;
+  const int c = threadIdx.x % S;
+  const bool act = col[c].active != 0;
+  const bool upd = act && !col[c].skip;
+  const T alpha = (T)col[c].alpha;
+  const int64_t total = op.dim * S;
+  for (int64_t idx = blockIdx.x * (int64_t)NT + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * NT) {
+    const int64_t i = idx / S;
+    T r = R[idx];
+    if (upd) {
+      Xs[idx] += alpha * P[idx];
+      r -= alpha * Q[idx];
+      R[idx] = r;
+    }
+    rr += (double)r * r;
+    if (i >= op.p) {
+      T z = Z[idx];
+      if (upd) {
+        z = op.dinv[i - op.p] * r;
+        Z[idx] = z;
+      }
+      rz += (double)r * z;
+    }
+  }
+  double t = block_sum_cols<S>(rr, red);
+  if (threadIdx.x < S) part[((int64_t)blockIdx.x * 2 + 0) * S + c] = t;
+  t = block_sum_cols<S>(rz, red);
+  if (threadIdx.x < S) part[((int64_t)blockIdx.x * 2 + 1) * S + c] = t;
+}
+
+// p = z + beta p (active columns).
+template <typename T, int S>
+__global__ void __launch_bounds__(NT) k_pupdate(int64_t dim, const Col* __restrict__ col,
+                                                const T* __restrict__ Z, T* __restrict__ P) {
+  const int c = threadIdx.x % S;
+  if (!col[c].active) return;
+  const T beta = (T)col[c].beta;
+  const int64_t total = dim * S;
+  for (int64_t idx = blockIdx.x * (int64_t)NT + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * NT)
+    P[idx] = Z[idx] + beta * P[idx];
+}
+
+// Scalar step after the initial residual: rz, b norm, convergence of x0.
+template <int S>
+__global__ void k_scalar_init(Col* col, int ncols, const double* part, int nblk,
+                              const double* rz_fix, int64_t p, int abs_tol, int* active_count) {
+  const int c = threadIdx.x;
+  if (c < S) {
+    double rr = 0, rz = 0, bb = 0;
+    for (int b = 0; b < nblk; ++b) {
+      rr += part[((int64_t)b * 3 + 0) * S + c];
+      rz += part[((int64_t)b * 3 + 1) * S + c];
+      bb += part[((int64_t)b * 3 + 2) * S + c];
+    }
+    for (int64_t f = 0; f < p; ++f) rz += rz_fix[f * S + c];
+    Col s{};
+    s.rz = rz;
+    s.rr = rr;
+    s.bnorm2 = bb;
+    s.beta = 0.0;
+    s.active = c < ncols ? 1 : 0;
+    s.status = c < ncols ? COL_RUNNING : COL_CONVERGED;
+    // MatrixFreePCG returns at once when ||r0|| < 1e-20 (matrix_free_pcg.h:31)
+    if (c < ncols && abs_tol && sqrt(rr) < 1e-20) { s.active = 0; s.status = COL_CONVERGED; }
+    col[c] = s;
+  }
+  __syncthreads();
+  if (c == 0) {
+    int a = 0;
+    for (int k = 0; k < S; ++k) a += col[k].active;
+    *active_count = a;
+  }
+}
+
+// alpha = rz / p'Ap, breakdown handling (pcg_solver.h:482-498).
+template <int S>
+__global__ void k_scalar_alpha(Col* col, const double* pq_part, int nblk) {
+  const int c = threadIdx.x;
+  if (c >= S) return;
+  Col s = col[c];
+  s.skip = 0;
+  if (s.active) {
+    double pq = 0;
+    for (int b = 0; b < nblk; ++b) pq += pq_part[(int64_t)b * S + c];
+    s.pq = pq;
+    if (fabs(pq) < 1e-300) {
+      if (!s.restarted) {
+        s.restarted = 1;
+        s.skip = 1;  // restart: p = z, rz unchanged; no update this iteration
+      } else {
+        s.active = 0;
+        s.status = COL_BREAKDOWN;
+      }
+    } else {
+      s.alpha = s.rz / pq;
+    }
+  }
+  col[c] = s;
+}
+
+// After the update: convergence test on the recursive residual, beta.
+template <int S>
+__global__ void k_scalar_beta(Col* col, const double* part, int nblk, const double* rz_fix,
+                              int64_t p, const double* tol_col, int abs_tol, int maxit,
+                              int* active_count) {
+  const int c = threadIdx.x;
+  if (c < S) {
+    Col s = col[c];
+    if (s.active) {
+      double rr = 0, rz = 0;
+      for (int b = 0; b < nblk; ++b) {
+        rr += part[((int64_t)b * 2 + 0) * S + c];
+        rz += part[((int64_t)b * 2 + 1) * S + c];
+      }
+      for (int64_t f = 0; f < p; ++f) rz += rz_fix[f * S + c];
+      s.rr = rr;
+      if (s.skip) {
+        s.beta = 0.0;
+        s.rz = rz;
+      } else {
+        s.iters += 1;
+        const double bn = s.bnorm2 > 0 ? sqrt(s.bnorm2) : 1.0;
+        const double res = sqrt(rr);
+        const double tol = tol_col[c];
+        const bool conv = abs_tol ? (res < tol) : (res / bn < tol);
+        if (conv) {
+          s.active = 0;
+          s.status = COL_CONVERGED;
+        } else if (!isfinite(rr) || !isfinite(rz)) {
+          s.active = 0;
+          s.status = COL_NONFINITE;
+        } else if (s.iters >= maxit) {
+          s.active = 0;
+          s.status = COL_MAXIT;
+        } else {
+          s.beta = rz / s.rz;
+          s.rz = rz;
+        }
+      }
+    }
+    col[c] = s;
+  }
+  __syncthreads();
+  if (c == 0) {
+    int a = 0;
+    for (int k = 0; k < S; ++k) a += col[k].active;
+    *active_count = a;
+  }
+}
+
+// Partial sums of squares per column (interleaved layout).
+template <int S>
+__global__ void __launch_bounds__(NT) k_colnorm2(const double* __restrict__ V, int64_t dim,
+                                                 double* __restrict__ part) {
+  __shared__ double red[NT];
+  double acc = 0;
+  const int64_t total = dim * S;
+  for (int64_t idx = blockIdx.x * (int64_t)NT + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * NT)
+    acc += V[idx] * V[idx];
+  const double t = block_sum_cols<S>(acc, red);
+  if (threadIdx.x < S) part[(int64_t)blockIdx.x * S + threadIdx.x] = t;
+}
+
+// Record loop: e = y - (X b + Z u) for column 0, partial sums of e'e.
+__global__ void k_resid_records(int64_t n_rec, int64_t p, const double* __restrict__ y,
+                                const int32_t* __restrict__ aid, int64_t q,
+                                const int32_t* __restrict__ xp, const int32_t* __restrict__ xc,
+                                const double* __restrict__ xv, const double* __restrict__ sol,
+                                double* __restrict__ e, double* __restrict__ part);
+
+}  // namespace sv
+}  // namespace cbx

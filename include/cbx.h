@@ -82,6 +82,47 @@ int cbx_grm_bed(cbx_handle* h, const uint8_t* bed, int64_t bed_bytes, int64_t n,
                 double* G, int32_t* xx_counts, float* allele_freqs,
                 double* sum2pq, int64_t* n_valid);
 
+/* ---- Mixed-model equations (one random component) ------------------------
+ * Replaces MMELHSBuilder::initialize / build_lhs / build_rhs
+ * (src/core/mme_builder.cpp:72-387, header src/core/mme_builder.h:26-71).
+ * Records follow GenRecord (src/core/design.h:20-27): y, aid = 1-based row of
+ * Qinv (0 = no random effect); the fixed-effect design follows
+ * FixedDesignG::rows (src/core/design.h:32-38) in CSR form: record i owns
+ * (fx_col[k], fx_val[k]) for fx_ptr[i] <= k < fx_ptr[i+1], columns < p.
+ * The LHS is [X'X X'Z; Z'X Z'Z + lambda Qinv]; lambda is given per solve. */
+int cbx_mme_create(cbx_handle* h, int64_t n_rec, int64_t p, int64_t q, const double* y,
+                   const int32_t* aid, const int64_t* fx_ptr, const int32_t* fx_col,
+                   const double* fx_val);
+
+/* Qinv dense, q x q (DenseMatrixAdapter, src/core/matrix_adapter.h:116-153).
+ * Qinv == NULL takes the inverse left on the device by cbx_invert_psd_g. */
+int cbx_mme_set_qinv_dense(cbx_handle* h, const double* Qinv, int64_t q);
+
+/* Qinv = A + S Gd S^T: A sparse q x q in CSR (a_ptr[q+1] int64, a_col int32,
+ * a_val), Gd dense ng x ng, gmap[k] = row of Qinv for dense row k
+ * (SplitMatrixAdapter, src/core/matrix_adapter.h:232-373, with the G^-1 and
+ * A22^-1 blocks pre-combined into Gd = G^-1 - A22^-1). */
+int cbx_mme_set_qinv_split(cbx_handle* h, const int64_t* a_ptr, const int32_t* a_col,
+                           const double* a_val, const double* Gd, int64_t ng,
+                           const int32_t* gmap);
+
+/* Solve LHS(lambda) X = B for nrhs right-hand sides (column-major dim x nrhs,
+ * dim = p + q).  Replaces PCGSolver::solve with the block-Jacobi
+ * preconditioner (src/core/pcg_solver.h:60-128, 436-536); all right-hand sides
+ * share each matrix read.  use_x0: X holds the initial guess.
+ * tol_mode 0: stop on ||r||/||b|| < tol (recursive residual, the reference);
+ * tol_mode 1: stop on ||r|| < tol (MatrixFreePCG, src/core/matrix_free_pcg.h:51).
+ * precision 0: FP64 throughout; 1: FP32 PCG bulk with FP64 iterative
+ * refinement, stopping on the TRUE FP64 residual.  iters / relres (length
+ * nrhs, may be NULL) receive CG iterations and the final relative residual. */
+int cbx_pcg_solve(cbx_handle* h, double lambda, int32_t nrhs, const double* B, double* X,
+                  int32_t use_x0, double tol, int32_t maxit, int32_t tol_mode,
+                  int32_t precision, int32_t* iters, double* relres);
+
+/* Y = Qinv X for nrhs column-major q-vectors (AbstractMatrix::operator*,
+ * src/core/matrix_adapter.h:19). */
+int cbx_qinv_apply(cbx_handle* h, int32_t nrhs, const double* X, double* Y);
+
 #ifdef __cplusplus
 }
 #endif

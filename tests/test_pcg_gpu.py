@@ -1,0 +1,150 @@
+"""GPU parity tests of the MME operator and the multi-RHS PCG against the oracle.
+
+Bar: solutions within 1e-8 relative of the oracle's FP64 PCG (the EBV parity
+target); mixed precision must reach a TRUE relative residual < 1e-10.
+"""
+import numpy as np
+import pytest
+
+from cosmicblup_gb300 import CbxError, DeviceMME
+from cosmicblup_gb300.mme import ABS, FP64, MIXED
+from cosmicblup_gb300.synth import genetic_values, simulate_bed, simulate_gblup_records
+from oracle.grm import vanraden_grm
+from oracle.mme import MME, BlockJacobi, build_fixed_design, invert_psd_matrix, matrix_free_pcg, pcg
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def gblup():
+    n, m = 300, 2000
+    bed, _ = simulate_bed(n, m, seed=1000, p_lo=0.05, miss=0.01)
+    G = vanraden_grm(bed, n, m)["G"]
+    Gi = invert_psd_matrix(G)
+    g = genetic_values(bed, n, m, seed=1002, var_a=0.4)
+    rec = simulate_gblup_records(n, 7, g, seed=1003, var_e=0.6)
+    p, rows, _ = build_fixed_design(rec["cats"])
+    return {"n": n, "G": G, "Gi": Gi, "rec": rec, "p": p, "rows": rows,
+            "mme": MME(rec["y"], rec["aid"], rows, p, n)}
+
+
+def dev_mme(handle, d):
+    dm = DeviceMME(handle, d["rec"]["y"], d["rec"]["aid"], d["rows"], d["p"], d["n"])
+    dm.set_qinv_dense(d["Gi"])
+    return dm
+
+
+def rel(a, b):
+    return np.abs(a - b).max() / np.abs(b).max()
+
+
+def test_single_rhs_fp64_matches_oracle(handle, gblup):
+    om, lam = gblup["mme"], 1.5
+    A = om.lhs(gblup["Gi"], lam)
+    b = om.rhs()
+    x_ref, it_ref, rr_ref, _ = pcg(lambda v: A @ v, b, BlockJacobi(A, om.p), 1e-10, 10000)
+    dm = dev_mme(handle, gblup)
+    x, it, rr = dm.pcg_solve(lam, b)
+    assert rel(x, x_ref) < 1e-8
+    assert rel(x, np.linalg.solve(A, b)) < 1e-8
+    assert rr[0] < 1e-10
+    assert abs(int(it[0]) - it_ref) <= 2, (it, it_ref)
+
+
+def test_multi_rhs_probes(handle, gblup):
+    om, lam = gblup["mme"], 2.0
+    A = om.lhs(gblup["Gi"], lam)
+    rng = np.random.default_rng(3)
+    k = 5
+    B = np.zeros((om.dim, k))
+    B[om.p:, :] = rng.choice([-1.0, 1.0], size=(om.q, k))
+    B[:, 2] = om.rhs()
+    dm = dev_mme(handle, gblup)
+    X, it, rr = dm.pcg_solve(lam, B)
+    Xe = np.linalg.solve(A, B)
+    for c in range(k):
+        assert rel(X[:, c], Xe[:, c]) < 1e-8, c
+        assert rr[c] < 1e-10
+    # 32 and 40 columns: one full block, and a block of 32 plus one of 8
+    B2 = np.zeros((om.dim, 40))
+    B2[om.p:, :] = rng.choice([-1.0, 1.0], size=(om.q, 40))
+    X2, it2, rr2 = dm.pcg_solve(lam, B2)
+    assert rel(X2, np.linalg.solve(A, B2)) < 1e-8
+    assert np.all(rr2 < 1e-10)
+
+
+def test_mixed_precision_true_residual(handle, gblup):
+    om, lam = gblup["mme"], 1.5
+    A = om.lhs(gblup["Gi"], lam)
+    B = np.stack([om.rhs(), np.r_[np.zeros(om.p), np.ones(om.q)]], axis=1)
+    dm = dev_mme(handle, gblup)
+    X, it, rr = dm.pcg_solve(lam, B, precision=MIXED)
+    for c in range(2):
+        true = np.linalg.norm(B[:, c] - A @ X[:, c]) / np.linalg.norm(B[:, c])
+        assert true < 1e-10 and rr[c] < 1e-10
+        assert rel(X[:, c], np.linalg.solve(A, B[:, c])) < 1e-8
+
+
+def test_warm_start_and_abs_tol(handle, gblup):
+    om, lam = gblup["mme"], 1.5
+    A = om.lhs(gblup["Gi"], lam)
+    b = om.rhs()
+    dm = dev_mme(handle, gblup)
+    x0 = np.linalg.solve(A, b) * (1 + 1e-4)
+    x, it, rr = dm.pcg_solve(lam, b, X0=x0)
+    assert rel(x, np.linalg.solve(A, b)) < 1e-8
+    xa, ita, rra = dm.pcg_solve(lam, b, tol=1e-8, tol_mode=ABS)
+    d = np.diag(A)
+    xo, ito = matrix_free_pcg(lambda v: A @ v, b, d, tol=1e-8, maxit=10000)
+    assert rra[0] < 1e-8
+    assert np.linalg.norm(b - A @ xa) < 1e-7
+
+
+def test_qinv_apply(handle, gblup):
+    dm = dev_mme(handle, gblup)
+    rng = np.random.default_rng(5)
+    X = rng.normal(size=(gblup["n"], 3))
+    Y = dm.qinv_apply(X)
+    assert rel(Y, gblup["Gi"] @ X) < 1e-12
+
+
+def test_split_qinv_equals_dense(handle, gblup):
+    """A sparse + S Gd S^T with a scattered genotyped map equals the dense sum."""
+    om, lam = gblup["mme"], 1.2
+    q = om.q
+    rng = np.random.default_rng(8)
+    # a sparse SPD tridiagonal "A^-1" and a dense block on a random subset
+    main = 2.0 + rng.random(q)
+    off = -0.4 * rng.random(q - 1)
+    Adense = np.diag(main) + np.diag(off, 1) + np.diag(off, -1)
+    ng = 120
+    gmap = np.sort(rng.choice(q, size=ng, replace=False)).astype(np.int32)
+    Wm = rng.normal(size=(ng, ng)) / np.sqrt(ng)
+    Gd = Wm @ Wm.T + 0.5 * np.eye(ng)
+    Q = Adense.copy()
+    Q[np.ix_(gmap, gmap)] += Gd
+    a_ptr = [0]
+    a_col, a_val = [], []
+    for i in range(q):
+        for j in range(max(0, i - 1), min(q, i + 2)):
+            a_col.append(j)
+            a_val.append(Adense[i, j])
+        a_ptr.append(len(a_col))
+    dm = DeviceMME(handle, gblup["rec"]["y"], gblup["rec"]["aid"], gblup["rows"], gblup["p"], q)
+    dm.set_qinv_split(np.array(a_ptr), np.array(a_col), np.array(a_val), Gd, gmap)
+    A = om.lhs(Q, lam)
+    b = om.rhs()
+    x, it, rr = dm.pcg_solve(lam, b)
+    assert rel(x, np.linalg.solve(A, b)) < 1e-8
+    X = rng.normal(size=(q, 2))
+    assert rel(dm.qinv_apply(X), Q @ X) < 1e-12
+
+
+def test_input_errors(handle, gblup):
+    y = gblup["rec"]["y"].copy()
+    y[3] = np.nan
+    with pytest.raises(CbxError, match="NONFINITE"):
+        DeviceMME(handle, y, gblup["rec"]["aid"], gblup["rows"], gblup["p"], gblup["n"])
+    dm = DeviceMME(handle, gblup["rec"]["y"], gblup["rec"]["aid"], gblup["rows"], gblup["p"], gblup["n"])
+    with pytest.raises(CbxError, match="STATE"):
+        dm.pcg_solve(1.0, np.ones(dm.dim))
