@@ -49,6 +49,12 @@ SIGNATURES = [
     ("cbx_pcg_solve", C.c_int, [C.c_void_p, C.c_double, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32,
                                 C.c_double, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]),
     ("cbx_qinv_apply", C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
+    ("cbx_invert_psd", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_double, C.c_void_p]),
+    ("cbx_reml_config_default", None, [C.c_void_p]),
+    ("cbx_reml_iterate", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_double),
+                                   C.POINTER(C.c_double), C.c_void_p]),
+    ("cbx_reml_solve", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                 C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_void_p, C.c_void_p]),
     # self-test export (not in the public header)
     ("cbx_selftest_umma", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
 ]

@@ -61,6 +61,10 @@ int cbx_destroy(cbx_handle* h) {
   {
     cbx_handle* tmp = h;
     tmp->G.release();
+    tmp->Ginv.release();
+    tmp->mme.reset();
+    tmp->dense_slot.reset();
+    tmp->libs_slot.reset();
     tmp->status.release();
     if (tmp->stream) cudaStreamDestroy(tmp->stream);
   }

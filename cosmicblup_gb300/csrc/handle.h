@@ -26,6 +26,9 @@ struct cbx_handle {
   int64_t Ginv_n = 0;
   // mixed-model equations and REML state
   std::unique_ptr<cbx::Mme> mme;
+  // library handles (cuSOLVER / cuBLAS) and dense exact AI state, owned here
+  std::shared_ptr<void> libs_slot;
+  std::shared_ptr<void> dense_slot;
 
   // count a kernel launch and check the launch error
   void launched(const char* what) {

@@ -1,0 +1,749 @@
+// AI-REML for one random component on the device, and the eigen-bending inverse.
+//
+// Replaces (reference src/core/vce.cpp unless noted):
+//  * AI_REML::solve outer loop and stop rule sum|delta| < tol (:741-837);
+//  * run_ai_iteration's EM branch with Hutchinson traces (:1490-1574),
+//    estimate_trace_Qinv_Cuu (:1266-1315) and AdaptiveTraceEstimator::estimate
+//    (src/core/adaptive_trace_estimator.cpp:11-81, one thread: batches of 16,
+//    engine std::mt19937_64(seed + samples_done), Rademacher via
+//    std::uniform_int_distribution<int>(0, 1) as in src/core/rng.h:48-53);
+//    the probes of consecutive batches are solved together as one multi-RHS
+//    block, then consumed in the reference's order with its stopping rule;
+//  * stabilize_variance (:1379-1389);
+//  * run_dense_exact_step (:2949-3195) with project_spd_2x2 (:267-283);
+//  * invert_psd_matrix (src/core/matrix_io.cpp:488-501).
+#include <algorithm>
+#include <cmath>
+#include <memory>
+#include <random>
+#include <vector>
+#include <cublas_v2.h>
+#include <cusolverDn.h>
+#include "handle.h"
+#include "pcg.h"
+#include "solver.cuh"
+
+namespace cbx {
+
+#define CBX_SOLVER(call)                                                          \
+  do {                                                                            \
+    cusolverStatus_t st_ = (call);                                                \
+    if (st_ != CUSOLVER_STATUS_SUCCESS)                                           \
+      throw Error(CBX_ERR_CUDA, std::string(#call) + " failed: " + std::to_string((int)st_)); \
+  } while (0)
+#define CBX_BLAS(call)                                                            \
+  do {                                                                            \
+    cublasStatus_t st_ = (call);                                                  \
+    if (st_ != CUBLAS_STATUS_SUCCESS)                                             \
+      throw Error(CBX_ERR_CUDA, std::string(#call) + " failed: " + std::to_string((int)st_)); \
+  } while (0)
+
+static inline unsigned gridn(int64_t n, int threads, int cap) {
+  int64_t g = (n + threads - 1) / threads;
+  return (unsigned)std::max<int64_t>(1, std::min<int64_t>(g, cap));
+}
+
+// Library handles owned by a cbx_handle (created on first use).
+struct Libs {
+  cusolverDnHandle_t sol = nullptr;
+  cublasHandle_t blas = nullptr;
+  ~Libs() {
+    if (sol) cusolverDnDestroy(sol);
+    if (blas) cublasDestroy(blas);
+  }
+};
+static Libs& libs(cbx_handle* h) {
+  if (!h->libs_slot) {
+    auto l = std::make_shared<Libs>();
+    CBX_SOLVER(cusolverDnCreate(&l->sol));
+    CBX_SOLVER(cusolverDnSetStream(l->sol, h->stream));
+    CBX_BLAS(cublasCreate(&l->blas));
+    CBX_BLAS(cublasSetStream(l->blas, h->stream));
+    h->libs_slot = l;
+  }
+  return *static_cast<Libs*>(h->libs_slot.get());
+}
+
+// ---------------------------------------------------------------------------
+// kernels of the dense paths (column-major matrices)
+__global__ void k_add_ridge_copy(const double* __restrict__ src, int64_t n, double ridge, double* __restrict__ dst) {
+  const int64_t total = n * n;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = i % n, c = i / n;
+    dst[i] = src[i] + (r == c ? ridge : 0.0);
+  }
+}
+// V[:, j] = U[:, j] / w_j
+__global__ void k_scale_cols(const double* __restrict__ U, const double* __restrict__ w, int64_t n,
+                             double* __restrict__ V) {
+  const int64_t total = n * n;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x)
+    V[i] = U[i] / w[i / n];
+}
+// C = dense(D) + lam [0 0; 0 Qd]  (dim x dim, column-major; D CSR rows = columns by symmetry)
+__global__ void k_build_lhs(int64_t dim, int64_t p, const int32_t* __restrict__ Dptr, const int32_t* __restrict__ Dcol,
+                            const double* __restrict__ Dval, const double* __restrict__ Qd, int64_t ld, double lam,
+                            double* __restrict__ C) {
+  const int64_t total = dim * dim;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = i % dim, c = i / dim;
+    C[i] = (r >= p && c >= p) ? lam * Qd[(r - p) * ld + (c - p)] : 0.0;
+  }
+}
+__global__ void k_scatter_csr(int64_t dim, const int32_t* __restrict__ Dptr, const int32_t* __restrict__ Dcol,
+                              const double* __restrict__ Dval, double* __restrict__ C) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < dim; r += (int64_t)gridDim.x * blockDim.x)
+    for (int32_t j = Dptr[r]; j < Dptr[r + 1]; ++j) C[(int64_t)Dcol[j] * dim + r] += Dval[j];
+}
+// W^T dense (dim x n_rec, column-major): column i = record i's design row
+__global__ void k_build_wt(int64_t n_rec, int64_t p, int64_t q, int64_t dim, const int32_t* __restrict__ aid,
+                           const int32_t* __restrict__ xp, const int32_t* __restrict__ xc,
+                           const double* __restrict__ xv, double* __restrict__ Wt) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_rec; i += (int64_t)gridDim.x * blockDim.x) {
+    double* col = Wt + i * dim;
+    for (int32_t j = xp[i]; j < xp[i + 1]; ++j)
+      if (xc[j] < p) col[xc[j]] += xv[j];
+    const int32_t a = aid[i];
+    if (a > 0 && a <= q) col[p + a - 1] += 1.0;
+  }
+}
+// P[i, j] = (delta_ij - (W CinvWt)[i, j]) / ve   (gather over the records' design rows)
+__global__ void k_build_P(int64_t n_rec, int64_t p, int64_t q, int64_t dim, const int32_t* __restrict__ aid,
+                          const int32_t* __restrict__ xp, const int32_t* __restrict__ xc,
+                          const double* __restrict__ xv, const double* __restrict__ CiWt, double ve,
+                          double* __restrict__ P) {
+  const int64_t total = n_rec * n_rec;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = idx % n_rec, j = idx / n_rec;
+    const double* cj = CiWt + j * dim;
+    double h = 0.0;
+    for (int32_t k = xp[i]; k < xp[i + 1]; ++k)
+      if (xc[k] < p) h += xv[k] * cj[xc[k]];
+    const int32_t a = aid[i];
+    if (a > 0 && a <= q) h += cj[p + a - 1];
+    P[idx] = ((i == j ? 1.0 : 0.0) - h) / ve;
+  }
+}
+// ZAZt[i, j] = A[aid_i - 1, aid_j - 1] (0 for records without an animal)
+__global__ void k_build_zazt(int64_t n_rec, int64_t q, const int32_t* __restrict__ aid, const double* __restrict__ A,
+                             double* __restrict__ Z) {
+  const int64_t total = n_rec * n_rec;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = idx % n_rec, j = idx / n_rec;
+    const int32_t a = aid[i], b = aid[j];
+    Z[idx] = (a > 0 && a <= q && b > 0 && b <= q) ? A[(int64_t)(b - 1) * q + (a - 1)] : 0.0;
+  }
+}
+// fill the strict upper triangle from the lower one (column-major)
+__global__ void k_symmetrize_lower(double* __restrict__ A, int64_t n) {
+  const int64_t total = n * n;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = idx % n, c = idx / n;
+    if (r < c) A[idx] = A[r * n + c];
+  }
+}
+// partial sums of: sum M_ij M_ji, sum M_ij P_ij, sum P_ij^2, tr M, tr P
+__global__ void k_ai_traces(const double* __restrict__ M, const double* __restrict__ P, int64_t n,
+                            double* __restrict__ part) {
+  __shared__ double red[256];
+  double s[5] = {0, 0, 0, 0, 0};
+  const int64_t total = n * n;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = idx % n, j = idx / n;
+    const double m = M[idx], pv = P[idx];
+    s[0] += m * M[i * n + j];
+    s[1] += m * pv;
+    s[2] += pv * pv;
+    if (i == j) { s[3] += m; s[4] += pv; }
+  }
+  for (int k = 0; k < 5; ++k) {
+    const double t = sv::block_sum_cols<1>(s[k], red);
+    if (threadIdx.x == 0) part[blockIdx.x * 5 + k] = t;
+  }
+}
+__global__ void k_log_diag_sum(const double* __restrict__ L, int64_t n, double* __restrict__ part, int* bad) {
+  __shared__ double red[256];
+  double s = 0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double d = L[i * n + i];
+    if (!(d > 0) || !isfinite(d)) atomicExch(bad, 1);
+    s += log(d);
+  }
+  const double t = sv::block_sum_cols<1>(s, red);
+  if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
+template <typename T>
+static std::vector<T> d2h(cbx_handle* h, const T* d, size_t n) {
+  std::vector<T> v(n);
+  CBX_CUDA(cudaMemcpyAsync(v.data(), d, n * sizeof(T), cudaMemcpyDeviceToHost, h->stream));
+  CBX_CUDA(cudaStreamSynchronize(h->stream));
+  return v;
+}
+
+// Cholesky of a column-major SPD matrix in place; returns false if not PD.
+static bool potrf(cbx_handle* h, double* A, int64_t n) {
+  Libs& L = libs(h);
+  int lw = 0;
+  CBX_SOLVER(cusolverDnDpotrf_bufferSize(L.sol, CUBLAS_FILL_MODE_LOWER, (int)n, A, (int)n, &lw));
+  DevBuf<double> work;
+  work.resize(std::max(lw, 1));
+  DevBuf<int> info;
+  info.resize(1);
+  CBX_SOLVER(cusolverDnDpotrf(L.sol, CUBLAS_FILL_MODE_LOWER, (int)n, A, (int)n, work.p, lw, info.p));
+  int hi = 0;
+  CBX_CUDA(cudaMemcpyAsync(&hi, info.p, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  CBX_CUDA(cudaStreamSynchronize(h->stream));
+  return hi == 0;
+}
+static void potrs(cbx_handle* h, const double* Lf, int64_t n, double* B, int64_t nrhs) {
+  Libs& L = libs(h);
+  DevBuf<int> info;
+  info.resize(1);
+  CBX_SOLVER(cusolverDnDpotrs(L.sol, CUBLAS_FILL_MODE_LOWER, (int)n, (int)nrhs, Lf, (int)n, B, (int)n, info.p));
+}
+// sum_i log L_ii of a Cholesky factor; NaN if a pivot is not positive
+static double log_diag(cbx_handle* h, const double* Lf, int64_t n) {
+  const unsigned g = gridn(n, 256, 256);
+  DevBuf<double> part;
+  part.resize(g);
+  DevBuf<int> bad;
+  bad.resize(1);
+  bad.zero(h->stream);
+  k_log_diag_sum<<<g, 256, 0, h->stream>>>(Lf, n, part.p, bad.p);
+  h->launched("k_log_diag_sum");
+  auto ph = d2h(h, part.p, g);
+  if (d2h(h, bad.p, 1)[0]) return std::nan("");
+  double s = 0;
+  for (double v : ph) s += v;
+  return s;
+}
+
+static double dot_h(const std::vector<double>& a, const std::vector<double>& b) {
+  double s = 0;
+  for (size_t i = 0; i < a.size(); ++i) s += a[i] * b[i];
+  return s;
+}
+
+// ---------------------------------------------------------------------------
+struct RemlConfigI {
+  int max_iter = 20;
+  double tol = 1e-4;
+  int mc_samples = 100;
+  int pcg_max_iter = 10000;
+  double pcg_tol = 1e-10;
+  int precision = 0;
+  int mode = 0;  // 0 auto, 1 EM + Hutchinson, 2 dense exact
+  int seed = 42;
+};
+
+struct IterInfo {
+  int kind = 0;
+  double var_u = 0, var_e = 0, logL = std::nan(""), trace = std::nan("");
+  int probes = 0;
+  int64_t pcg_iters = 0, matvecs = 0;
+  double e_sse = std::nan(""), uQu = std::nan("");
+};
+
+// variance bounds of stabilize_variance (vce.cpp:1375-1389)
+static double stabilize(double proposed, double previous, double y_var) {
+  const double floor_v = 1e-12, ceil_v = std::max(1.0, y_var * 1e6);
+  if (!std::isfinite(proposed) || proposed <= 0.0) return std::max(previous, floor_v);
+  double lo = floor_v, hi = ceil_v;
+  if (std::isfinite(previous) && previous > 0.0) {
+    lo = std::max(lo, previous * 0.1);
+    hi = std::min(hi, previous * 10.0);
+  }
+  if (lo > hi) lo = floor_v;
+  return std::min(std::max(proposed, lo), hi);
+}
+
+static double y_variance(const Mme& m) {
+  const auto& y = m.y_host;
+  const size_t n = y.size();
+  if (n > 1) {
+    double mean = 0;
+    for (double v : y) mean += v;
+    mean /= (double)n;
+    double ss = 0;
+    for (double v : y) ss += (v - mean) * (v - mean);
+    return std::max(1e-12, ss / (double)(n - 1));
+  }
+  return std::max(1e-12, m.yty);
+}
+
+// One EM iteration (vce.cpp:1490-1574).
+static void em_iteration(cbx_handle* h, const RemlConfigI& cfg, double& vu, double& ve, IterInfo& info) {
+  Mme& m = *h->mme;
+  cudaStream_t s = h->stream;
+  const int64_t p = m.p, q = m.q, dim = m.dim, n = m.n_rec;
+  const double start_vu = vu, start_ve = ve;
+  const double lam = ve / std::max(vu, 1e-9);
+  // 1. data solve, warm-started from the previous data solution
+  m.last_solution.resize(dim);
+  PcgResult r;
+  pcg_solve(h, lam, 1, m.rhs.p, m.last_solution.p, m.has_last, cfg.pcg_tol, cfg.pcg_max_iter, 0, cfg.precision, r);
+  m.has_last = true;
+  info.pcg_iters += r.iters[0];
+  info.matvecs += r.matvecs;
+  if (r.status[0] == sv::COL_NONFINITE) throw Error(CBX_ERR_NONFINITE, "non-finite data solve");
+  // 2. residual sum of squares
+  const double e_sse = record_residual(h, m.last_solution.p, nullptr);
+  // 3. u' Qinv u
+  DevBuf<double> Qu;
+  Qu.resize(q);
+  qinv_apply(h, 1, m.last_solution.p + p, Qu.p);
+  const auto u_h = d2h(h, m.last_solution.p + p, q);
+  const auto Qu_h = d2h(h, Qu.p, q);
+  const double uQu = dot_h(u_h, Qu_h);
+  // 4. Hutchinson trace of Qinv C^uu with the reference's probe schedule
+  const int n_samp = std::max(5, cfg.mc_samples / 2);
+  int min_s = std::max(30, n_samp / 3), max_s = std::max(100, n_samp);
+  if (min_s <= 0) min_s = 10;
+  if (max_s < min_s) max_s = min_s;
+  const int batch = 16;  // max(16, 4 * threads) with one thread
+  double tsum = 0, tsq = 0;
+  int done = 0;
+  DevBuf<double> B, X, QW;
+  bool stop = false;
+  while (done < max_s && !stop) {
+    // solve as many consecutive batches at once as are needed before the next check
+    std::vector<std::pair<int, int>> batches;  // (start, size)
+    int next = done;
+    do {
+      const int sz = std::min(batch, max_s - next);
+      batches.push_back({next, sz});
+      next += sz;
+    } while (next < min_s && next < max_s);
+    const int k = next - done;
+    std::vector<double> Bh((size_t)dim * k, 0.0);
+    std::vector<double> Z((size_t)q * k);
+    int col = 0;
+    for (auto& bt : batches) {
+      std::mt19937_64 gen((unsigned long)(cfg.seed + bt.first));
+      std::uniform_int_distribution<int> dist(0, 1);
+      for (int j = 0; j < bt.second; ++j, ++col)
+        for (int64_t i = 0; i < q; ++i) {
+          const double z = dist(gen) == 0 ? -1.0 : 1.0;
+          Z[(size_t)col * q + i] = z;
+          Bh[(size_t)col * dim + p + i] = z;
+        }
+    }
+    B.resize((size_t)dim * k);
+    X.resize((size_t)dim * k);
+    QW.resize((size_t)q * k);
+    CBX_CUDA(cudaMemcpyAsync(B.p, Bh.data(), Bh.size() * sizeof(double), cudaMemcpyHostToDevice, s));
+    PcgResult pr;
+    pcg_solve(h, lam, k, B.p, X.p, false, cfg.pcg_tol, cfg.pcg_max_iter, 0, cfg.precision, pr);
+    for (int c = 0; c < k; ++c) {
+      info.pcg_iters += pr.iters[c];
+      if (pr.status[c] == sv::COL_NONFINITE) throw Error(CBX_ERR_NONFINITE, "non-finite probe solve");
+    }
+    info.matvecs += pr.matvecs;
+    // Qinv C^uu z for each probe: gather the u rows (strided by dim) into q x k
+    DevBuf<double> Wu;
+    Wu.resize((size_t)q * k);
+    CBX_CUDA(cudaMemcpy2DAsync(Wu.p, q * sizeof(double), X.p + p, dim * sizeof(double), q * sizeof(double), k,
+                               cudaMemcpyDeviceToDevice, s));
+    qinv_apply(h, k, Wu.p, QW.p);
+    const auto QWh = d2h(h, QW.p, (size_t)q * k);
+    col = 0;
+    for (auto& bt : batches) {
+      double bs = 0, bq = 0;
+      for (int j = 0; j < bt.second; ++j, ++col) {
+        double v = 0;
+        for (int64_t i = 0; i < q; ++i) v += Z[(size_t)col * q + i] * QWh[(size_t)col * q + i];
+        bs += v;
+        bq += v * v;
+      }
+      tsum += bs;
+      tsq += bq;
+      done += bt.second;
+      if (done >= min_s) {
+        const double mean = tsum / done;
+        const double var = (tsq - (tsum * tsum) / done) / (done - 1.0);
+        const double se = std::sqrt(std::max(0.0, var) / done);
+        if (std::abs(mean) > 1e-12 && (se / std::abs(mean)) < 0.05) { stop = true; break; }
+      }
+    }
+  }
+  const double tr = tsum / done;
+  // 5. updates (vce.cpp:1554-1569)
+  const double y_var = y_variance(m);
+  const double vu_new = (uQu + tr * start_ve) / (double)q;
+  vu = stabilize(vu_new, start_vu, y_var);
+  const double tr_c = (double)(p + q) - lam * tr;
+  const double ve_new = (e_sse + start_ve * tr_c) / (double)n;
+  ve = stabilize(ve_new, start_ve, y_var);
+  info.kind = 0;
+  info.trace = tr;
+  info.probes = done;
+  info.e_sse = e_sse;
+  info.uQu = uQu;
+  info.var_u = vu;
+  info.var_e = ve;
+}
+
+// ---------------------------------------------------------------------------
+// dense exact AI step
+struct DenseExact {
+  bool init = false;
+  int64_t n = 0, dim = 0;
+  DevBuf<double> ZAZt, Wt;
+  double log_det_A = 0;
+};
+static DenseExact& dense_state(cbx_handle* h) {
+  if (!h->dense_slot) h->dense_slot = std::make_shared<DenseExact>();
+  return *static_cast<DenseExact*>(h->dense_slot.get());
+}
+
+static void dense_init(cbx_handle* h, DenseExact& D) {
+  Mme& m = *h->mme;
+  CBX_REQUIRE(m.has_dense && !m.has_sparse && m.ng == m.q, CBX_ERR_UNSUPPORTED,
+              "dense exact AI needs a dense Qinv");
+  cudaStream_t s = h->stream;
+  const int64_t q = m.q, n = m.n_rec, dim = m.dim;
+  // A = Qinv^-1 via Cholesky (initialize_dense, vce.cpp:2890-2897); log|A| = -log|Qinv|
+  DevBuf<double> A;
+  A.resize((size_t)q * q);
+  CBX_CUDA(cudaMemcpy2DAsync(A.p, q * sizeof(double), m.Qd64.p, m.ld * sizeof(double), q * sizeof(double), q,
+                             cudaMemcpyDeviceToDevice, s));
+  CBX_REQUIRE(potrf(h, A.p, q), CBX_ERR_FACTOR, "Qinv is not positive definite");
+  D.log_det_A = -2.0 * log_diag(h, A.p, q);
+  {
+    Libs& L = libs(h);
+    int lw = 0;
+    CBX_SOLVER(cusolverDnDpotri_bufferSize(L.sol, CUBLAS_FILL_MODE_LOWER, (int)q, A.p, (int)q, &lw));
+    DevBuf<double> work;
+    work.resize(std::max(lw, 1));
+    DevBuf<int> info;
+    info.resize(1);
+    CBX_SOLVER(cusolverDnDpotri(L.sol, CUBLAS_FILL_MODE_LOWER, (int)q, A.p, (int)q, work.p, lw, info.p));
+    k_symmetrize_lower<<<gridn(q * q, 256, 8 * h->num_sms), 256, 0, s>>>(A.p, q);
+    h->launched("k_symmetrize_lower");
+  }
+  D.ZAZt.resize((size_t)n * n);
+  k_build_zazt<<<gridn(n * n, 256, 8 * h->num_sms), 256, 0, s>>>(n, q, m.aid.p, A.p, D.ZAZt.p);
+  h->launched("k_build_zazt");
+  D.Wt.resize((size_t)dim * n);
+  D.Wt.zero(s);
+  k_build_wt<<<gridn(n, 256, 4 * h->num_sms), 256, 0, s>>>(n, m.p, q, dim, m.aid.p, m.x_ptr.p, m.x_col.p, m.x_val.p,
+                                                            D.Wt.p);
+  h->launched("k_build_wt");
+  CBX_CUDA(cudaStreamSynchronize(s));
+  D.n = n;
+  D.dim = dim;
+  D.init = true;
+}
+
+// Factor C(lambda) in C (dim x dim); returns false if not PD.
+static bool factor_lhs(cbx_handle* h, double lam, DevBuf<double>& C) {
+  Mme& m = *h->mme;
+  cudaStream_t s = h->stream;
+  const int64_t dim = m.dim;
+  C.resize((size_t)dim * dim);
+  k_build_lhs<<<gridn(dim * dim, 256, 8 * h->num_sms), 256, 0, s>>>(dim, m.p, m.D64.ptr.p, m.D64.col.p, m.D64.val.p,
+                                                                     m.Qd64.p, m.ld, lam, C.p);
+  h->launched("k_build_lhs");
+  k_scatter_csr<<<gridn(dim, 256, 4 * h->num_sms), 256, 0, s>>>(dim, m.D64.ptr.p, m.D64.col.p, m.D64.val.p, C.p);
+  h->launched("k_scatter_csr");
+  return potrf(h, C.p, dim);
+}
+
+// compute_logL of run_dense_exact_step (vce.cpp:2974-3007); -1e18 if C is not PD
+static double dense_logL(cbx_handle* h, DenseExact& D, double vu, double ve, DevBuf<double>& C, DevBuf<double>& sol,
+                         double* ld_out = nullptr) {
+  Mme& m = *h->mme;
+  const int64_t n = m.n_rec, p = m.p, q = m.q, dim = m.dim;
+  if (!factor_lhs(h, ve / vu, C)) return -1e18;
+  const double ld_C = 2.0 * log_diag(h, C.p, dim);
+  if (!std::isfinite(ld_C)) return -1e18;
+  sol.resize(dim);
+  CBX_CUDA(cudaMemcpyAsync(sol.p, m.rhs.p, dim * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+  potrs(h, C.p, dim, sol.p, 1);
+  DevBuf<double> e;
+  e.resize(n);
+  record_residual(h, sol.p, e.p);
+  const auto eh = d2h(h, e.p, n);
+  const double yPy = dot_h(m.y_host, eh) / ve;
+  if (ld_out) *ld_out = ld_C;
+  const double m2 = ld_C + (double)(n - p - q) * std::log(ve) + (double)q * std::log(vu) + yPy + D.log_det_A;
+  return -0.5 * m2;
+}
+
+static void project_spd_2x2(double A[2][2], double eps_rel = 1e-8, double eps_abs = 1e-12) {
+  const double a = A[0][0], b = 0.5 * (A[0][1] + A[1][0]), d = A[1][1];
+  // eigen-decomposition of [[a, b], [b, d]]
+  const double tr = a + d, det = a * d - b * b;
+  const double disc = std::sqrt(std::max(0.0, 0.25 * tr * tr - det));
+  double l1 = 0.5 * tr - disc, l2 = 0.5 * tr + disc;  // ascending
+  double v1x, v1y;
+  if (std::abs(b) > 0) {
+    v1x = l1 - d;
+    v1y = b;
+  } else {
+    if (a <= d) { v1x = 1; v1y = 0; } else { v1x = 0; v1y = 1; }
+    l1 = std::min(a, d);
+    l2 = std::max(a, d);
+  }
+  const double nr = std::hypot(v1x, v1y);
+  v1x /= nr;
+  v1y /= nr;
+  const double v2x = -v1y, v2y = v1x;
+  const double floor_v = std::max(eps_abs, eps_rel * std::max(l2, 0.0));
+  l1 = std::max(l1, floor_v);
+  l2 = std::max(l2, floor_v);
+  A[0][0] = l1 * v1x * v1x + l2 * v2x * v2x;
+  A[0][1] = A[1][0] = l1 * v1x * v1y + l2 * v2x * v2y;
+  A[1][1] = l1 * v1y * v1y + l2 * v2y * v2y;
+}
+
+static bool dense_exact_step(cbx_handle* h, double& vu_io, double& ve_io, IterInfo& info) {
+  Mme& m = *h->mme;
+  DenseExact& D = dense_state(h);
+  if (!D.init || D.n != m.n_rec || D.dim != m.dim) dense_init(h, D);
+  cudaStream_t s = h->stream;
+  Libs& L = libs(h);
+  const int64_t n = m.n_rec, dim = m.dim;
+  const double vu = vu_io, ve = ve_io;
+  DevBuf<double> C, sol;
+  const double cur0 = dense_logL(h, D, vu, ve, C, sol);
+  if (cur0 <= -1e18) return false;
+  double cur = cur0;
+  // C^-1 W^T, P = (I - W C^-1 W^T) / ve
+  DevBuf<double> CiWt;
+  CiWt.resize((size_t)dim * n);
+  CBX_CUDA(cudaMemcpyAsync(CiWt.p, D.Wt.p, (size_t)dim * n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  potrs(h, C.p, dim, CiWt.p, n);
+  DevBuf<double> P, Mu;
+  P.resize((size_t)n * n);
+  Mu.resize((size_t)n * n);
+  k_build_P<<<gridn(n * n, 256, 8 * h->num_sms), 256, 0, s>>>(n, m.p, m.q, dim, m.aid.p, m.x_ptr.p, m.x_col.p,
+                                                               m.x_val.p, CiWt.p, ve, P.p);
+  h->launched("k_build_P");
+  const double one = 1.0, zero = 0.0;
+  CBX_BLAS(cublasDgemm(L.blas, CUBLAS_OP_N, CUBLAS_OP_N, (int)n, (int)n, (int)n, &one, P.p, (int)n, D.ZAZt.p, (int)n,
+                       &zero, Mu.p, (int)n));
+  const unsigned g = gridn(n * n, 256, 4 * h->num_sms);
+  DevBuf<double> part;
+  part.resize((size_t)g * 5);
+  k_ai_traces<<<g, 256, 0, s>>>(Mu.p, P.p, n, part.p);
+  h->launched("k_ai_traces");
+  const auto ph = d2h(h, part.p, (size_t)g * 5);
+  double sums[5] = {0, 0, 0, 0, 0};
+  for (unsigned b = 0; b < g; ++b)
+    for (int k = 0; k < 5; ++k) sums[k] += ph[(size_t)b * 5 + k];
+  // Py = e / ve; score terms
+  DevBuf<double> e, ZPy;
+  e.resize(n);
+  ZPy.resize(n);
+  record_residual(h, sol.p, e.p);
+  std::vector<double> Py = d2h(h, e.p, n);
+  for (auto& v : Py) v /= ve;
+  DevBuf<double> dPy;
+  dPy.resize(n);
+  CBX_CUDA(cudaMemcpyAsync(dPy.p, Py.data(), n * sizeof(double), cudaMemcpyHostToDevice, s));
+  CBX_BLAS(cublasDgemv(L.blas, CUBLAS_OP_N, (int)n, (int)n, &one, D.ZAZt.p, (int)n, dPy.p, 1, &zero, ZPy.p, 1));
+  const auto ZPyh = d2h(h, ZPy.p, n);
+  const double score_u = dot_h(Py, ZPyh), score_e = dot_h(Py, Py);
+  const double grad_u = -0.5 * sums[3] + 0.5 * score_u;
+  const double grad_e = -0.5 * sums[4] + 0.5 * score_e;
+  double AI[2][2] = {{0.5 * sums[0], 0.5 * sums[1]}, {0.5 * sums[1], 0.5 * sums[2]}};
+  project_spd_2x2(AI);
+  double delta[2];
+  {
+    // LLT of the 2x2 AI (AI is SPD after the projection)
+    const double l11 = std::sqrt(AI[0][0]);
+    const double l21 = AI[1][0] / l11;
+    const double l22sq = AI[1][1] - l21 * l21;
+    if (!(l11 > 0) || !(l22sq > 0)) {
+      const double det = AI[0][0] * AI[1][1] - AI[0][1] * AI[1][0];
+      if (std::abs(det) < 1e-20) return false;
+      delta[0] = (AI[1][1] * grad_u - AI[0][1] * grad_e) / det;
+      delta[1] = (-AI[1][0] * grad_u + AI[0][0] * grad_e) / det;
+    } else {
+      const double l22 = std::sqrt(l22sq);
+      const double y0 = grad_u / l11, y1 = (grad_e - l21 * y0) / l22;
+      delta[1] = y1 / l22;
+      delta[0] = (y0 - l21 * delta[1]) / l11;
+    }
+  }
+  // step halving on logL (vce.cpp:3150-3171)
+  const int max_halving = 6;
+  for (int k = 0; k < max_halving; ++k) {
+    const double vu_n = vu + delta[0], ve_n = ve + delta[1];
+    if (vu_n > 0 && ve_n > 0) {
+      DevBuf<double> C2, s2;
+      const double nl = dense_logL(h, D, vu_n, ve_n, C2, s2);
+      if (nl > cur || k == max_halving - 1) {
+        cur = nl;
+        vu_io = vu_n;
+        ve_io = ve_n;
+        m.last_solution.resize(dim);
+        CBX_CUDA(cudaMemcpyAsync(m.last_solution.p, sol.p, dim * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        m.has_last = true;
+        info.kind = 1;
+        info.logL = cur;
+        info.var_u = vu_io;
+        info.var_e = ve_io;
+        return true;
+      }
+    }
+    delta[0] *= 0.5;
+    delta[1] *= 0.5;
+  }
+  return false;
+}
+
+static void reml_iterate(cbx_handle* h, const RemlConfigI& cfg, double& vu, double& ve, IterInfo& info) {
+  Mme& m = *h->mme;
+  const bool dense = cfg.mode == 2 || (cfg.mode == 0 && m.dim < 5000);
+  if (dense && dense_exact_step(h, vu, ve, info)) return;
+  em_iteration(h, cfg, vu, ve, info);
+}
+
+}  // namespace cbx
+
+using namespace cbx;
+
+static RemlConfigI to_cfg(const cbx_reml_config* c) {
+  RemlConfigI r;
+  if (c) {
+    r.max_iter = c->max_iter;
+    r.tol = c->tol;
+    r.mc_samples = c->mc_samples;
+    r.pcg_max_iter = c->pcg_max_iter;
+    r.pcg_tol = c->pcg_tol;
+    r.precision = c->precision;
+    r.mode = c->mode;
+    r.seed = c->seed;
+  }
+  return r;
+}
+static void to_info(const IterInfo& i, cbx_reml_iter_info* o) {
+  if (!o) return;
+  o->kind = i.kind;
+  o->var_u = i.var_u;
+  o->var_e = i.var_e;
+  o->logL = i.logL;
+  o->trace = i.trace;
+  o->probes = i.probes;
+  o->pcg_iters = i.pcg_iters;
+  o->matvecs = i.matvecs;
+  o->e_sse = i.e_sse;
+  o->uQu = i.uQu;
+}
+
+extern "C" void cbx_reml_config_default(cbx_reml_config* c) {
+  if (!c) return;
+  RemlConfigI d;
+  c->max_iter = d.max_iter;
+  c->tol = d.tol;
+  c->mc_samples = d.mc_samples;
+  c->pcg_max_iter = d.pcg_max_iter;
+  c->pcg_tol = d.pcg_tol;
+  c->precision = d.precision;
+  c->mode = d.mode;
+  c->seed = d.seed;
+}
+
+extern "C" int cbx_reml_iterate(cbx_handle* h, const cbx_reml_config* cfg, double* var_u, double* var_e,
+                                cbx_reml_iter_info* info) {
+  return cbx_guard(h, [&] {
+    CBX_REQUIRE(h->mme, CBX_ERR_STATE, "call cbx_mme_create and cbx_mme_set_qinv_* first");
+    CBX_REQUIRE(var_u && var_e && *var_u > 0 && *var_e > 0, CBX_ERR_ARG, "variances must be positive");
+    CBX_CUDA(cudaSetDevice(h->device));
+    IterInfo it;
+    reml_iterate(h, to_cfg(cfg), *var_u, *var_e, it);
+    to_info(it, info);
+  });
+}
+
+extern "C" int cbx_reml_solve(cbx_handle* h, const cbx_reml_config* cfg, double* var_u, double* var_e,
+                              int32_t* iterations, int32_t* converged, double* solution,
+                              cbx_reml_iter_info* history) {
+  return cbx_guard(h, [&] {
+    CBX_REQUIRE(h->mme, CBX_ERR_STATE, "call cbx_mme_create and cbx_mme_set_qinv_* first");
+    CBX_REQUIRE(var_u && var_e && *var_u > 0 && *var_e > 0, CBX_ERR_ARG, "variances must be positive");
+    CBX_CUDA(cudaSetDevice(h->device));
+    const RemlConfigI c = to_cfg(cfg);
+    int iters = 0, conv = 0;
+    for (int it = 0; it < c.max_iter; ++it) {
+      const double ou = *var_u, oe = *var_e;
+      IterInfo info;
+      reml_iterate(h, c, *var_u, *var_e, info);
+      if (history) to_info(info, history + it);
+      iters = it + 1;
+      const double diff = std::abs(*var_e - oe) + std::abs(*var_u - ou);
+      if (diff < c.tol) { conv = 1; break; }
+    }
+    if (iterations) *iterations = iters;
+    if (converged) *converged = conv;
+    if (solution && h->mme->has_last)
+      CBX_CUDA(cudaMemcpy(solution, h->mme->last_solution.p, h->mme->dim * sizeof(double), cudaMemcpyDeviceToHost));
+  });
+}
+
+// Eigen-bending inverse of M (n x n); M == NULL uses the device GRM of this
+// handle.  The result stays on the device (cbx_mme_set_qinv_dense(h, NULL, n))
+// and is copied to Minv when given.
+extern "C" int cbx_invert_psd(cbx_handle* h, const double* M, int64_t n, double ridge, double* Minv) {
+  return cbx_guard(h, [&] {
+    CBX_CUDA(cudaSetDevice(h->device));
+    CBX_REQUIRE(n > 0, CBX_ERR_ARG, "n must be positive");
+    cudaStream_t s = h->stream;
+    Libs& L = libs(h);
+    DevBuf<double> src;
+    const double* sp = nullptr;
+    if (M) {
+      src.resize((size_t)n * n);
+      CBX_CUDA(cudaMemcpyAsync(src.p, M, (size_t)n * n * sizeof(double), cudaMemcpyHostToDevice, s));
+      sp = src.p;
+    } else {
+      CBX_REQUIRE(h->G.p && h->G_n == n, CBX_ERR_STATE, "no device GRM of this order (cbx_grm_bed)");
+      sp = h->G.p;
+    }
+    DevBuf<double> U, w;
+    U.resize((size_t)n * n);
+    w.resize(n);
+    k_add_ridge_copy<<<gridn(n * n, 256, 8 * h->num_sms), 256, 0, s>>>(sp, n, ridge > 0 ? ridge : 0.0, U.p);
+    h->launched("k_add_ridge_copy");
+    src.release();
+    int lw = 0;
+    CBX_SOLVER(cusolverDnDsyevd_bufferSize(L.sol, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, (int)n, U.p,
+                                           (int)n, w.p, &lw));
+    {
+      DevBuf<double> work;
+      work.resize(std::max(lw, 1));
+      DevBuf<int> info;
+      info.resize(1);
+      CBX_SOLVER(cusolverDnDsyevd(L.sol, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, (int)n, U.p, (int)n, w.p,
+                                  work.p, lw, info.p));
+      int hi = 0;
+      CBX_CUDA(cudaMemcpyAsync(&hi, info.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+      CBX_CUDA(cudaStreamSynchronize(s));
+      CBX_REQUIRE(hi == 0, CBX_ERR_FACTOR, "symmetric eigensolver failed, info " + std::to_string(hi));
+    }
+    std::vector<double> wh = d2h(h, w.p, n);
+    double maxeig = wh[0];
+    for (double v : wh) maxeig = std::max(maxeig, v);
+    const double eps = std::max(1e-12 * maxeig, 1e-6);
+    for (auto& v : wh) if (v < eps) v = eps;
+    CBX_CUDA(cudaMemcpyAsync(w.p, wh.data(), n * sizeof(double), cudaMemcpyHostToDevice, s));
+    DevBuf<double> V;
+    V.resize((size_t)n * n);
+    k_scale_cols<<<gridn(n * n, 256, 8 * h->num_sms), 256, 0, s>>>(U.p, w.p, n, V.p);
+    h->launched("k_scale_cols");
+    h->Ginv.resize((size_t)n * n);
+    const double one = 1.0, zero = 0.0;
+    CBX_BLAS(cublasDgemm(L.blas, CUBLAS_OP_N, CUBLAS_OP_T, (int)n, (int)n, (int)n, &one, V.p, (int)n, U.p, (int)n,
+                         &zero, h->Ginv.p, (int)n));
+    h->Ginv_n = n;
+    if (Minv) CBX_CUDA(cudaMemcpyAsync(Minv, h->Ginv.p, (size_t)n * n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    CBX_CUDA(cudaStreamSynchronize(s));
+  });
+}

@@ -123,6 +123,57 @@ int cbx_pcg_solve(cbx_handle* h, double lambda, int32_t nrhs, const double* B, d
  * src/core/matrix_adapter.h:19). */
 int cbx_qinv_apply(cbx_handle* h, int32_t nrhs, const double* X, double* Y);
 
+/* ---- G inverse with eigen-bending -----------------------------------------
+ * Replaces invert_psd_matrix (src/core/matrix_io.cpp:488-501): eigenvalues
+ * below max(1e-12 lambda_max, 1e-6) are raised to that bound, then
+ * U diag(1/lambda) U^T, in FP64.  M == NULL inverts the GRM left on the device
+ * by cbx_grm_bed.  The inverse stays on the device (use it with
+ * cbx_mme_set_qinv_dense(h, NULL, n)); Minv (host, n x n) may be NULL. */
+int cbx_invert_psd(cbx_handle* h, const double* M, int64_t n, double ridge, double* Minv);
+
+/* ---- AI-REML, one random component ---------------------------------------
+ * Mirrors VCEConfig (src/core/vce.h:140-165) with the defaults of Config
+ * (src/config/config.h:41-57): ai_maxit 20, vce_tol 1e-4, vce_mc_samples 100,
+ * pcg_maxit 10000, pcg_tol 1e-10. */
+typedef struct cbx_reml_config {
+  int32_t max_iter;      /* REML iterations */
+  double tol;            /* stop when |d var_u| + |d var_e| < tol */
+  int32_t mc_samples;    /* Hutchinson samples parameter (min 30 / max 100 at 100) */
+  int32_t pcg_max_iter;  /* per PCG solve */
+  double pcg_tol;        /* relative residual of every PCG solve */
+  int32_t precision;     /* 0: FP64 PCG, 1: FP32 PCG + FP64 refinement */
+  int32_t mode;          /* 0: dense exact AI when dim < 5000, else EM + Hutchinson
+                            (run_ai_iteration's choice); 1: EM; 2: dense exact */
+  int32_t seed;          /* probe seed (AdaptiveTraceEstimator default 42) */
+} cbx_reml_config;
+
+/* Diagnostics of one REML iteration. */
+typedef struct cbx_reml_iter_info {
+  int32_t kind;          /* 0: EM + Hutchinson, 1: dense exact AI */
+  double var_u, var_e;   /* variances after the iteration */
+  double logL;           /* REML log-likelihood (dense exact step), NaN otherwise */
+  double trace;          /* Hutchinson estimate of tr(Qinv C^uu) (EM), NaN otherwise */
+  int32_t probes;        /* probe vectors used */
+  int64_t pcg_iters;     /* CG iterations over all solves of the iteration */
+  int64_t matvecs;       /* operator applications (one matrix read each) */
+  double e_sse, uQu;     /* e'e and u'Qinv u of the data solve (EM) */
+} cbx_reml_iter_info;
+
+void cbx_reml_config_default(cbx_reml_config* cfg);
+
+/* One AI-REML iteration on the MME of this handle: run_ai_iteration
+ * (src/core/vce.cpp:1334-1660) restricted to its single-component branches:
+ * run_dense_exact_step (:2949-3195) or the EM update with Hutchinson traces
+ * (:1490-1574).  var_u / var_e are updated in place; info may be NULL. */
+int cbx_reml_iterate(cbx_handle* h, const cbx_reml_config* cfg, double* var_u, double* var_e,
+                     cbx_reml_iter_info* info);
+
+/* Full AI_REML::solve loop (src/core/vce.cpp:741-837).  history (length
+ * max_iter) and solution (length dim: the last data solve) may be NULL. */
+int cbx_reml_solve(cbx_handle* h, const cbx_reml_config* cfg, double* var_u, double* var_e,
+                   int32_t* iterations, int32_t* converged, double* solution,
+                   cbx_reml_iter_info* history);
+
 #ifdef __cplusplus
 }
 #endif
