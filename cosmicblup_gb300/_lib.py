@@ -55,6 +55,9 @@ SIGNATURES = [
                                    C.POINTER(C.c_double), C.c_void_p]),
     ("cbx_reml_solve", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                  C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_void_p, C.c_void_p]),
+    ("cbx_profile_enable", C.c_int, [C.c_void_p, C.c_int32]),
+    ("cbx_profile_read", C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int64), C.POINTER(C.c_double),
+                                   C.POINTER(C.c_double)]),
     # self-test export (not in the public header)
     ("cbx_selftest_umma", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
 ]
@@ -110,6 +113,14 @@ class Handle:
     def check(self, rc: int) -> None:
         if rc != CBX_OK:
             raise CbxError(rc, lib().cbx_last_error(self._h).decode())
+
+    def profile(self, on: bool) -> None:
+        self.check(lib().cbx_profile_enable(self.raw, 1 if on else 0))
+
+    def profile_read(self, bucket: int) -> tuple[int, float, float]:
+        n, ms, b = C.c_int64(0), C.c_double(0), C.c_double(0)
+        self.check(lib().cbx_profile_read(self.raw, bucket, C.byref(n), C.byref(ms), C.byref(b)))
+        return n.value, ms.value, b.value
 
     def launches(self) -> int:
         return int(lib().cbx_launch_count(self.raw))

@@ -30,6 +30,16 @@ struct cbx_handle {
   std::shared_ptr<void> libs_slot;
   std::shared_ptr<void> dense_slot;
 
+  // optional per-launch timing of the dense block product (bench roofline):
+  // bucket 0 = FP32 launches, bucket 1 = FP64 launches
+  bool prof_on = false;
+  struct ProfRec {
+    cudaEvent_t a, b;
+    int bucket;
+    double bytes;
+  };
+  std::vector<ProfRec> prof;
+
   // count a kernel launch and check the launch error
   void launched(const char* what) {
     ++launches;

@@ -195,9 +195,22 @@ void matvec(cbx_handle* h, const sv::OpView<T>& op, Workspace<T, S>& w, const T*
     constexpr int KT = 32 * sv::Vec16<T>::n * 4;
     const int smem = S * KT * (int)sizeof(T);
     CBX_CUDA(cudaFuncSetAttribute(sv::k_dense<T, S, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    cbx_handle::ProfRec pr{};
+    if (h->prof_on) {
+      CBX_CUDA(cudaEventCreate(&pr.a));
+      CBX_CUDA(cudaEventCreate(&pr.b));
+      CBX_CUDA(cudaEventRecord(pr.a, s));
+    }
     sv::k_dense<T, S, R><<<(unsigned)((op.ng + 8 * R - 1) / (8 * R)), 256, smem, s>>>(op.Qd, op.ng, op.ld, w.Vt.p,
                                                                                      w.Tout.p, active);
     h->launched("k_dense");
+    if (h->prof_on) {
+      CBX_CUDA(cudaEventRecord(pr.b, s));
+      pr.bucket = sizeof(T) == 4 ? 0 : 1;
+      // algorithmic bytes: the dense block once, the S gathered vectors, the S outputs
+      pr.bytes = (double)sizeof(T) * ((double)op.ng * op.ld + (double)S * op.ld + (double)op.ng * S);
+      h->prof.push_back(pr);
+    }
   }
   sv::k_spmv<T, S><<<w.nblk_spmv, sv::NT, 0, s>>>(op, X, w.Tout.p, (T)lam, use_D, Y, P, pq_part, active);
   h->launched("k_spmv");
@@ -830,6 +843,38 @@ extern "C" int cbx_pcg_solve(cbx_handle* h, double lambda, int32_t nrhs, const d
       if (r.status[c] == sv::COL_NONFINITE) throw Error(CBX_ERR_NONFINITE, "non-finite PCG iterate");
       if (r.status[c] == sv::COL_BREAKDOWN) throw Error(CBX_ERR_BREAKDOWN, "PCG breakdown");
     }
+  });
+}
+
+// Kernel timing of the dense block product (see include/cbx.h).
+extern "C" int cbx_profile_enable(cbx_handle* h, int32_t on) {
+  return cbx_guard(h, [&] {
+    CBX_CUDA(cudaSetDevice(h->device));
+    CBX_CUDA(cudaStreamSynchronize(h->stream));
+    for (auto& r : h->prof) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
+    h->prof.clear();
+    h->prof_on = on != 0;
+  });
+}
+
+extern "C" int cbx_profile_read(cbx_handle* h, int32_t bucket, int64_t* launches, double* total_ms,
+                                double* total_bytes) {
+  return cbx_guard(h, [&] {
+    CBX_CUDA(cudaSetDevice(h->device));
+    CBX_CUDA(cudaStreamSynchronize(h->stream));
+    int64_t n = 0;
+    double ms = 0, bytes = 0;
+    for (auto& r : h->prof) {
+      if (r.bucket != bucket) continue;
+      float t = 0;
+      CBX_CUDA(cudaEventElapsedTime(&t, r.a, r.b));
+      ms += t;
+      bytes += r.bytes;
+      ++n;
+    }
+    if (launches) *launches = n;
+    if (total_ms) *total_ms = ms;
+    if (total_bytes) *total_bytes = bytes;
   });
 }
 

@@ -123,6 +123,16 @@ int cbx_pcg_solve(cbx_handle* h, double lambda, int32_t nrhs, const double* B, d
  * src/core/matrix_adapter.h:19). */
 int cbx_qinv_apply(cbx_handle* h, int32_t nrhs, const double* X, double* Y);
 
+/* ---- Kernel timing (no reference counterpart: benchmark instrumentation) ---
+ * When enabled, every launch of the dense block product (the G^-1 / H^-1 part
+ * of the MME operator) is bracketed by CUDA events on the handle's stream.
+ * cbx_profile_read sums, for bucket 0 (FP32 launches) or 1 (FP64 launches),
+ * the launch count, their device time and their algorithmic bytes (the dense
+ * block once plus the gathered vectors and outputs).  Enabling clears the log. */
+int cbx_profile_enable(cbx_handle* h, int32_t on);
+int cbx_profile_read(cbx_handle* h, int32_t bucket, int64_t* launches, double* total_ms,
+                     double* total_bytes);
+
 /* ---- G inverse with eigen-bending -----------------------------------------
  * Replaces invert_psd_matrix (src/core/matrix_io.cpp:488-501): eigenvalues
  * below max(1e-12 lambda_max, 1e-6) are raised to that bound, then
