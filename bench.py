@@ -1,0 +1,392 @@
+#!/usr/bin/env python3
+"""Benchmark of the GBLUP hot path on GB300.
+
+Workload (default ``--config c2``): GBLUP with n = 20,000 genotyped animals,
+m = 50,000 SNPs (allele frequencies U(0.01, 0.5), HWE genotypes, 2 % missing),
+h2 = 0.3, fixed effects mean + 200-level contemporary group, one record per
+animal.  Seeded synthetic data of those shapes (no public dataset exists).
+
+Setup (untimed, phases reported): BED -> GRM on the tensor cores -> eigen-bent
+G^-1 (FP64) -> mixed-model equations on the device.
+
+Step: one AI-REML iteration, which at this size is the EM update with
+Hutchinson traces (one data solve plus >= 32 Rademacher probe solves, the probe
+blocks solved as multi-RHS PCG), every solve to relative residual 1e-10.
+``value`` uses the mixed-precision solver (FP32 PCG bulk, FP64 refinement on
+the true residual) with all inputs resident in HBM; the plain FP64 path is
+timed on the same state for the mixed-vs-FP64 ratio.  ``e2e`` runs the public C
+ABI per step from host buffers (records uploaded, solution downloaded).
+
+``--impl reference`` times the CPU restatement of the path (FP64 PCG, numpy
+with all host threads) on a bounded sample of iterations of the same operator
+and scales it by the PCG work of one REML iteration.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = ("REML iter/s & PCG solves/s at relres 1e-10, mixed vs FP64, 1 GB300; "
+          "GRM int8 TOPS")
+UNIT = "REML iter/s"
+
+CONFIGS = {
+    "c2": dict(name="gblup_n20000_m50000_cg200", n=20000, m=50000, p_lo=0.01, miss=0.02,
+               var_a=0.3, var_e=0.7, levels=200, seed=2000),
+    "c1": dict(name="gblup_n2000_m10000_sex2", n=2000, m=10000, p_lo=0.05, miss=0.01,
+               var_a=0.4, var_e=0.6, levels=2, seed=1000),
+}
+WORK_FILE = os.path.join(ROOT, "profiles", "reml_iteration_work.md")
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return d["hbm_gbs"], d["bf16_tflops"], "measured"
+    except Exception:
+        return 6800.0, 1900.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thr = threading.Thread(target=self._read, daemon=True)
+            self.thr.start()
+        except FileNotFoundError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows for k in range(4) if r[5 + k] == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.rows)}
+
+
+def build_records(cfg, bed):
+    """Phenotypes and the fixed-effect design (mu + contemporary group)."""
+    from cosmicblup_gb300.synth import genetic_values, simulate_gblup_records
+    from oracle.mme import build_fixed_design  # design restatement = data preparation only
+    g = genetic_values(bed, cfg["n"], cfg["m"], seed=cfg["seed"] + 2, var_a=cfg["var_a"])
+    rec = simulate_gblup_records(cfg["n"], cfg["levels"], g, seed=cfg["seed"] + 3, var_e=cfg["var_e"])
+    p, rows, _ = build_fixed_design(rec["cats"])
+    return rec, p, rows
+
+
+def cpu_pcg_iteration_cost(WtW, Qd, p, lam, iters: int, seed: int = 0) -> float:
+    """Seconds per FP64 PCG iteration of the oracle on the operator W'W + lam [0; Qd].
+
+    Runs a fixed number of iterations (tol = 0) with the block-Jacobi
+    preconditioner; numpy/BLAS uses every host thread."""
+    from oracle.mme import pcg
+    dim = WtW.shape[0]
+    d = WtW.diagonal().copy()
+    d[p:] += lam * np.diag(Qd)
+    A11 = WtW[:p, :p].toarray()
+    A11[np.diag_indices(p)] += max(1e-8 * np.abs(np.diag(A11)).max(), 1e-6)
+    dinv = 1.0 / d[p:]
+
+    def matvec(v):
+        y = WtW @ v
+        y[p:] += lam * (Qd @ v[p:])
+        return y
+
+    def prec(v):
+        r = np.empty_like(v)
+        r[:p] = np.linalg.solve(A11, v[:p])
+        r[p:] = dinv * v[p:]
+        return r
+
+    rng = np.random.default_rng(seed)
+    b = np.zeros(dim)
+    b[p:] = rng.choice([-1.0, 1.0], size=dim - p)
+    t0 = time.perf_counter()
+    pcg(matvec, b, prec, tol=0.0, maxit=iters)
+    dt = time.perf_counter() - t0
+    return dt / (iters + 2)  # iterations + the initial and final residual matvecs
+
+
+def read_work_file():
+    try:
+        txt = open(WORK_FILE).read()
+        m = re.search(r"fp64_pcg_iterations_per_reml_iteration:\s*([0-9.]+)", txt)
+        return float(m.group(1)) if m else None
+    except OSError:
+        return None
+
+
+def read_traffic():
+    try:
+        txt = open(os.path.join(ROOT, "profiles", "k_dense_fp32_c2.md")).read()
+        m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", txt)
+        return float(m.group(1)) if m else None
+    except OSError:
+        return None
+
+
+# ---------------------------------------------------------------------------
+def run_reference(args, cfg):
+    """CPU restatement of the path on a bounded sample (rank 0 only)."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import scipy.sparse as sp  # noqa: F401
+    from cosmicblup_gb300.synth import simulate_gblup_records
+    from oracle.mme import build_fixed_design, sparse_data_part
+    n = cfg["n"]
+    work = read_work_file()
+    if work is None:
+        print(json.dumps({"impl": "reference", "unavailable":
+                          f"{WORK_FILE} (PCG work of one REML iteration) is missing"}))
+        return
+    rng = np.random.default_rng(7)
+    rec = simulate_gblup_records(n, cfg["levels"], rng.normal(0, 0.5, n), seed=cfg["seed"] + 3,
+                                 var_e=cfg["var_e"])
+    p, rows, _ = build_fixed_design(rec["cats"])
+    WtW, _ = sparse_data_part(rec["aid"], rows, p, n)
+    # the per-iteration cost of a dense-block operator does not depend on its
+    # values: a well-conditioned symmetric stand-in of the G^-1 block's size
+    Qd = rng.standard_normal((n, n)) * (1.0 / n)
+    Qd = 0.5 * (Qd + Qd.T)
+    Qd[np.diag_indices(n)] += 2.0
+    lam = cfg["var_e"] / cfg["var_a"]
+    per_step_iters = 10
+    for _ in range(args.warmup):
+        cpu_pcg_iteration_cost(WtW, Qd, p, lam, per_step_iters)
+    costs = [cpu_pcg_iteration_cost(WtW, Qd, p, lam, per_step_iters, seed=s) for s in range(args.steps)]
+    c = float(np.mean(costs))
+    value = 1.0 / (c * work)
+    cores = os.cpu_count()
+    sample = (f"oracle FP64 PCG ({per_step_iters} iterations per step, numpy/BLAS on {cores} threads) on "
+              f"the {n + p}-row operator; scaled by {work:.0f} PCG iterations per REML iteration")
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": c * per_step_iters * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": {"workload": cfg["name"], "precision": "fp64 (CPU restatement)"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+# ---------------------------------------------------------------------------
+def run_gpu(args, cfg):
+    import ctypes as C
+    from cosmicblup_gb300 import AIREML, DeviceMME, Handle, RemlConfig, invert_psd
+    from cosmicblup_gb300._lib import lib, ptr
+    from cosmicblup_gb300.mme import FP64, MIXED, rows_to_csr
+    from cosmicblup_gb300.synth import simulate_bed
+    from cosmicblup_gb300.vce import MODE_EM
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist  # scalars only: replicas share nothing
+        dist.init_process_group("gloo")
+    hbm_peak, bf16_peak, peak_src = peaks()
+    n, m = cfg["n"], cfg["m"]
+    phases = {}
+    h = Handle(local)
+
+    t0 = time.perf_counter()
+    bed, _ = simulate_bed(n, m, seed=cfg["seed"], p_lo=cfg["p_lo"], miss=cfg["miss"])
+    rec, p, rows = build_records(cfg, bed)
+    phases["synthetic_data_s"] = time.perf_counter() - t0
+
+    # GRM on the tensor cores
+    h.profile(True)
+    s2pq, nval = C.c_double(0), C.c_int64(0)
+    bedarr = np.frombuffer(bed, dtype=np.uint8)
+    t0 = time.perf_counter()
+    h.check(lib().cbx_grm_bed(h.raw, ptr(bedarr), bedarr.size, n, m, C.c_float(0.01), 1, 2048, None, None,
+                              None, C.byref(s2pq), C.byref(nval)))
+    phases["grm_call_s"] = time.perf_counter() - t0
+    gl, gms, gops = h.profile_read(2)
+    grm = {"n": n, "m_valid": nval.value, "kernel_ms": gms,
+           "tops_int8_equivalent": gops / (gms * 1e-3) / 1e12 if gms > 0 else None,
+           "note": "2 n^2 m_valid integer ops; exact f16 digit GEMMs on tcgen05 (no int8 MMA on sm_103a)"}
+
+    # eigen-bent G^-1 (FP64, cuSOLVER syevd + GEMM); host copy for the CPU baseline
+    t0 = time.perf_counter()
+    Ginv_host = invert_psd(h, None, n, download=(rank == 0 and not args.no_cpu_baseline))
+    phases["g_inverse_s"] = time.perf_counter() - t0
+
+    dm = DeviceMME(h, rec["y"], rec["aid"], rows, p, n)
+    dm.set_qinv_dense(None)
+    fp, fc, fv = rows_to_csr(rows)
+    h2d_bytes = rec["y"].nbytes + rec["aid"].nbytes + fp.nbytes + fc.nbytes + fv.nbytes
+    d2h_bytes = 8 * (p + n) + 16
+
+    # ---- mixed-precision REML iterations (the headline) ----
+    r = AIREML(dm, 0.5, 0.5, RemlConfig.default(mode=MODE_EM, precision=MIXED))
+    t0 = time.perf_counter()
+    for _ in range(args.warmup):
+        r.run_iteration()
+    phases["warmup_s"] = time.perf_counter() - t0
+    state = (r.var_u, r.var_e)
+    h.profile(True)
+    clocks = ClockSampler(local)
+    clocks.start()
+    l0 = h.launches()
+    if dist:
+        dist.barrier()
+    h.timer_start()
+    infos = [r.run_iteration() for _ in range(args.steps)]
+    ms = h.timer_stop()
+    launches = h.launches() - l0
+    clk = clocks.stop()
+    dl, dms, dbytes = h.profile_read(0)
+    solves = sum(1 + i["probes"] for i in infos)
+    if dist:
+        import torch
+        t = torch.tensor([ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * args.steps / (ms * 1e-3)
+
+    # ---- plain FP64 path on the same state ----
+    fp64 = None
+    if args.fp64_steps > 0:
+        r64 = AIREML(dm, *state, RemlConfig.default(mode=MODE_EM, precision=FP64))
+        h.profile(True)
+        h.timer_start()
+        i64 = [r64.run_iteration() for _ in range(args.fp64_steps)]
+        ms64 = h.timer_stop()
+        dl64, dms64, db64 = h.profile_read(1)
+        fp64 = {"reml_iter_per_s": args.fp64_steps / (ms64 * 1e-3),
+                "pcg_solves_per_s": sum(1 + i["probes"] for i in i64) / (ms64 * 1e-3),
+                "ms_per_step": ms64 / args.fp64_steps,
+                "pcg_iterations_per_step": sum(i["pcg_iters"] for i in i64) / args.fp64_steps,
+                "solves_per_step": sum(1 + i["probes"] for i in i64) / args.fp64_steps,
+                "matvecs_per_step": sum(i["matvecs"] for i in i64) / args.fp64_steps,
+                "k_dense_fp64_GBps": db64 / (dms64 * 1e-3) / 1e9 if dms64 > 0 else None}
+
+    # ---- end to end through the C ABI from host buffers ----
+    e2e_steps = max(1, min(args.steps, 3))
+    h.timer_start()
+    for _ in range(e2e_steps):
+        dm2 = DeviceMME(h, rec["y"], rec["aid"], (fp, fc, fv), p, n)
+        dm2.set_qinv_dense(None)
+        r2 = AIREML(dm2, *state, RemlConfig.default(mode=MODE_EM, precision=MIXED, max_iter=1))
+        r2.solve()
+    ms_e2e = h.timer_stop()
+    e2e = {"value": world * e2e_steps / (ms_e2e * 1e-3), "unit": UNIT,
+           "h2d_bytes_per_step": int(h2d_bytes), "d2h_bytes_per_step": int(d2h_bytes)}
+
+    # ---- CPU baseline: the oracle's FP64 PCG on this operator, bounded sample ----
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline and fp64 is not None:
+        from oracle.mme import sparse_data_part
+        WtW, _ = sparse_data_part(rec["aid"], rows, p, n)
+        lam = state[1] / state[0]
+        iters = 10 if n >= 10000 else 50
+        c = cpu_pcg_iteration_cost(WtW, Ginv_host, p, lam, iters)
+        # one RHS at a time on the CPU: every CG iteration of every solve plus
+        # the initial residual of each solve is one operator application
+        work = fp64["pcg_iterations_per_step"] + fp64["solves_per_step"]
+        cpu = {"value": 1.0 / (c * work), "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+               "sample": f"oracle FP64 PCG, {iters} iterations on this operator (numpy/BLAS, all threads); "
+                         f"scaled by {work:.0f} single-RHS operator applications per REML iteration "
+                         f"(the FP64 path's count)"}
+
+    if rank != 0:
+        return
+    ach = dbytes / (dms * 1e-3) / 1e9 if dms > 0 else None
+    traffic = read_traffic()
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+        "data": "synthetic (seeded generator with the workload's shapes)",
+        "config": {"workload": cfg["name"], "n_animals": n, "n_snps": m, "fixed_levels": cfg["levels"],
+                   "step": "one EM+Hutchinson AI-REML iteration (data solve + probe solves, relres 1e-10)",
+                   "precision": "mixed: FP32 PCG bulk + FP64 refinement on the true residual",
+                   "l2": "inputs larger than L2 (1.6 GB FP32 G^-1 block read per PCG iteration)",
+                   "parallelism": f"replicas x{world}"},
+        "pcg_solves_per_s": world * solves / (ms * 1e-3),
+        "pcg_iterations_per_step": sum(i["pcg_iters"] for i in infos) / args.steps,
+        "probes_per_step": sum(i["probes"] for i in infos) / args.steps,
+        "fp64": fp64,
+        "mixed_vs_fp64": (value / world) / fp64["reml_iter_per_s"] if fp64 else None,
+        "grm": grm,
+        "setup": phases,
+        "clocks": clk,
+        "e2e": e2e,
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "kernel": "k_dense<float> (G^-1 block x probe block)",
+                     "achieved": ach, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": (ach / hbm_peak) if ach else None, "traffic": traffic,
+                     "peak_source": peak_src, "launches": dl, "avg_launch_ms": dms / dl if dl else None},
+        "cpu_baseline": cpu,
+        "variances": {"var_u": r.var_u, "var_e": r.var_e},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="cbx", choices=["cbx", "reference"])
+    ap.add_argument("--config", default="c2", choices=sorted(CONFIGS))
+    ap.add_argument("--fp64-steps", type=int, default=1)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    cfg = CONFIGS[args.config]
+    if args.impl == "reference":
+        run_reference(args, cfg)
+    else:
+        run_gpu(args, cfg)
+
+
+if __name__ == "__main__":
+    main()

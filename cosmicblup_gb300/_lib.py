@@ -58,6 +58,8 @@ SIGNATURES = [
     ("cbx_profile_enable", C.c_int, [C.c_void_p, C.c_int32]),
     ("cbx_profile_read", C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int64), C.POINTER(C.c_double),
                                    C.POINTER(C.c_double)]),
+    ("cbx_timer_start", C.c_int, [C.c_void_p]),
+    ("cbx_timer_stop", C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     # self-test export (not in the public header)
     ("cbx_selftest_umma", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
 ]
@@ -121,6 +123,14 @@ class Handle:
         n, ms, b = C.c_int64(0), C.c_double(0), C.c_double(0)
         self.check(lib().cbx_profile_read(self.raw, bucket, C.byref(n), C.byref(ms), C.byref(b)))
         return n.value, ms.value, b.value
+
+    def timer_start(self) -> None:
+        self.check(lib().cbx_timer_start(self.raw))
+
+    def timer_stop(self) -> float:
+        ms = C.c_double(0)
+        self.check(lib().cbx_timer_stop(self.raw, C.byref(ms)))
+        return ms.value
 
     def launches(self) -> int:
         return int(lib().cbx_launch_count(self.raw))

@@ -66,6 +66,9 @@ int cbx_destroy(cbx_handle* h) {
     tmp->dense_slot.reset();
     tmp->libs_slot.reset();
     tmp->status.release();
+    for (auto& r : tmp->prof) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
+    if (tmp->timer_a) cudaEventDestroy(tmp->timer_a);
+    if (tmp->timer_b) cudaEventDestroy(tmp->timer_b);
     if (tmp->stream) cudaStreamDestroy(tmp->stream);
   }
   delete h;
@@ -82,6 +85,28 @@ int cbx_sync(cbx_handle* h) {
   return cbx_guard(h, [&] {
     CBX_CUDA(cudaSetDevice(h->device));
     CBX_CUDA(cudaStreamSynchronize(h->stream));
+  });
+}
+
+int cbx_timer_start(cbx_handle* h) {
+  return cbx_guard(h, [&] {
+    CBX_CUDA(cudaSetDevice(h->device));
+    if (!h->timer_a) CBX_CUDA(cudaEventCreate(&h->timer_a));
+    if (!h->timer_b) CBX_CUDA(cudaEventCreate(&h->timer_b));
+    CBX_CUDA(cudaStreamSynchronize(h->stream));
+    CBX_CUDA(cudaEventRecord(h->timer_a, h->stream));
+  });
+}
+
+int cbx_timer_stop(cbx_handle* h, double* ms) {
+  return cbx_guard(h, [&] {
+    CBX_REQUIRE(h->timer_a && h->timer_b, CBX_ERR_STATE, "cbx_timer_start not called");
+    CBX_CUDA(cudaSetDevice(h->device));
+    CBX_CUDA(cudaEventRecord(h->timer_b, h->stream));
+    CBX_CUDA(cudaEventSynchronize(h->timer_b));
+    float t = 0;
+    CBX_CUDA(cudaEventElapsedTime(&t, h->timer_a, h->timer_b));
+    if (ms) *ms = t;
   });
 }
 

@@ -635,8 +635,21 @@ extern "C" int cbx_grm_bed(cbx_handle* h, const uint8_t* bed, int64_t bed_bytes,
     CBX_CUDA(cudaFuncSetAttribute(grm::k_grm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   grm::SMEM_BYTES));
     const int grid = std::min<int>(h->num_sms, args.ntiles);
+    cbx_handle::ProfRec pr{};
+    if (h->prof_on) {
+      CBX_CUDA(cudaEventCreate(&pr.a));
+      CBX_CUDA(cudaEventCreate(&pr.b));
+      CBX_CUDA(cudaEventRecord(pr.a, s));
+    }
     grm::k_grm_tc<<<grid, grm::THREADS, grm::SMEM_BYTES, s>>>(args);
     h->launched("k_grm_tc");
+    if (h->prof_on) {
+      CBX_CUDA(cudaEventRecord(pr.b, s));
+      pr.bucket = 2;
+      // algorithmic integer work 2 n^2 K (the full square of X X^T)
+      pr.bytes = 2.0 * (double)n * (double)n * (double)K;
+      h->prof.push_back(pr);
+    }
     h->check_status("cbx_grm_bed");
     if (G) CBX_CUDA(cudaMemcpyAsync(G, h->G.p, n * n * sizeof(double), cudaMemcpyDeviceToHost, s));
     if (xx_counts)

@@ -19,7 +19,7 @@ struct cbx_handle {
   cbx::DevBuf<int> status;  // device-side error word(s)
 
   // Genomic relationship matrix kept on the device after cbx_grm_bed, and its
-  // eigen-bent inverse after cbx_invert_psd_g.
+  // eigen-bent inverse after cbx_invert_psd.
   cbx::DevBuf<double> G;
   int64_t G_n = 0;
   cbx::DevBuf<double> Ginv;
@@ -39,6 +39,7 @@ struct cbx_handle {
     double bytes;
   };
   std::vector<ProfRec> prof;
+  cudaEvent_t timer_a = nullptr, timer_b = nullptr;
 
   // count a kernel launch and check the launch error
   void launched(const char* what) {

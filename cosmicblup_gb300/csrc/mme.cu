@@ -711,7 +711,7 @@ extern "C" int cbx_mme_create(cbx_handle* h, int64_t n_rec, int64_t p, int64_t q
 }
 
 // Dense Qinv (q x q, symmetric, row- or column-major alike).  Qinv == NULL uses
-// the matrix left on the device by cbx_invert_psd_g.
+// the matrix left on the device by cbx_invert_psd.
 extern "C" int cbx_mme_set_qinv_dense(cbx_handle* h, const double* Qinv, int64_t q) {
   return cbx_guard(h, [&] {
     CBX_REQUIRE(h->mme, CBX_ERR_STATE, "call cbx_mme_create first");

@@ -33,43 +33,77 @@ def encode_bed(geno_snp_major: np.ndarray) -> bytes:
     return BED_MAGIC + packed.astype(np.uint8).tobytes()
 
 
-def simulate_bed(n: int, m: int, seed: int, p_lo: float = 0.05, miss: float = 0.01,
-                 chunk: int = 4096) -> tuple[bytes, np.ndarray]:
-    """Return (bed_bytes, p) for n samples and m SNPs, generated in SNP chunks."""
+def _bed_chunk(n: int, p: np.ndarray, miss: float, seed) -> bytes:
+    """SNP-major BED payload for the SNPs with frequencies p (one uint16 draw per call)."""
     rng = np.random.default_rng(seed)
-    p = rng.uniform(p_lo, 0.5, size=m)
-    parts = [BED_MAGIC]
-    for s in range(0, m, chunk):
-        e = min(s + chunk, m)
-        g = rng.binomial(2, p[s:e, None], size=(e - s, n)).astype(np.int8)
-        if miss > 0:
-            g[rng.random((e - s, n)) < miss] = -1
-        parts.append(encode_bed(g)[3:])
-    return b"".join(parts), p
+    k = p.shape[0]
+    scale = 65536.0
+    tm = np.uint32(round(miss * scale))
+    q2 = (1.0 - miss) * scale
+    t2 = (tm + np.round(q2 * p * p)).astype(np.uint32)[:, None]                 # two copies
+    t1 = (t2[:, 0] + np.round(q2 * 2 * p * (1 - p))).astype(np.uint32)[:, None]  # one copy
+    bps = (n + 3) // 4
+    u = rng.integers(0, 65536, size=(k, bps * 4), dtype=np.uint16).astype(np.uint32)
+    # code: 01 missing, 00 two copies, 10 one copy, 11 none
+    code = ((u < tm).astype(np.uint8) + 2 * ((u >= t2) & (u < t1)).astype(np.uint8)
+            + 3 * (u >= t1).astype(np.uint8))
+    code[:, n:] = 0  # PLINK pads unused slots with 00
+    c = code.reshape(k, bps, 4)
+    packed = c[:, :, 0] | (c[:, :, 1] << 2) | (c[:, :, 2] << 4) | (c[:, :, 3] << 6)
+    return packed.astype(np.uint8).tobytes()
+
+
+def simulate_bed(n: int, m: int, seed: int, p_lo: float = 0.05, miss: float = 0.01,
+                 chunk: int = 1024, threads: int | None = None) -> tuple[bytes, np.ndarray]:
+    """Return (bed_bytes, p) for n samples and m SNPs.
+
+    Chunks of SNPs are generated in parallel threads from independent child
+    seeds of ``seed``, so the result depends only on (n, m, seed, p_lo, miss, chunk).
+    """
+    import concurrent.futures as cf
+    import os
+    ss = np.random.SeedSequence(seed)
+    p_seed, *chunk_seeds = ss.spawn(1 + (m + chunk - 1) // chunk)
+    p = np.random.default_rng(p_seed).uniform(p_lo, 0.5, size=m)
+    starts = list(range(0, m, chunk))
+    threads = threads or min(16, os.cpu_count() or 1)
+    with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+        parts = list(ex.map(lambda a: _bed_chunk(n, p[a[1]:a[1] + chunk], miss, a[0]),
+                            zip(chunk_seeds, starts)))
+    return BED_MAGIC + b"".join(parts), p
+
+
+def _g_chunk(payload, n, bps, s, e, w):
+    lut = np.array([2.0, np.nan, 1.0, 0.0])
+    blk = payload[s * bps:e * bps].reshape(e - s, bps)
+    codes = np.stack([(blk >> (2 * k)) & 3 for k in range(4)], axis=2).reshape(e - s, bps * 4)[:, :n]
+    x = lut[codes]
+    obs = ~np.isnan(x)
+    cnt = np.maximum(obs.sum(axis=1), 1)
+    mu = np.where(obs, x, 0).sum(axis=1) / cnt
+    pf = mu / 2
+    z = np.where(obs, x - mu[:, None], 0.0)
+    return w @ z, float((2 * pf * (1 - pf)).sum())
 
 
 def genetic_values(bed: bytes, n: int, m: int, seed: int, var_a: float,
-                   chunk: int = 2048) -> np.ndarray:
+                   chunk: int = 1024, threads: int | None = None) -> np.ndarray:
     """g = Z w / sqrt(sum 2pq) with w ~ N(0, var_a); Z centred at the observed 2p."""
+    import concurrent.futures as cf
+    import os
     rng = np.random.default_rng(seed)
+    w = rng.normal(0.0, np.sqrt(var_a), size=m)
     bps = (n + 3) // 4
     payload = np.frombuffer(bed, dtype=np.uint8, offset=3)
-    lut = np.array([2.0, np.nan, 1.0, 0.0])
+    threads = threads or min(16, os.cpu_count() or 1)
+    with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+        res = list(ex.map(lambda s: _g_chunk(payload, n, bps, s, min(s + chunk, m), w[s:min(s + chunk, m)]),
+                          range(0, m, chunk)))
     g = np.zeros(n)
     s2pq = 0.0
-    for s in range(0, m, chunk):
-        e = min(s + chunk, m)
-        blk = payload[s * bps:e * bps].reshape(e - s, bps)
-        codes = np.stack([(blk >> (2 * k)) & 3 for k in range(4)], axis=2).reshape(e - s, bps * 4)[:, :n]
-        x = lut[codes]
-        obs = ~np.isnan(x)
-        cnt = np.maximum(obs.sum(axis=1), 1)
-        mu = np.where(obs, x, 0).sum(axis=1) / cnt
-        pf = mu / 2
-        s2pq += float((2 * pf * (1 - pf)).sum())
-        z = np.where(obs, x - mu[:, None], 0.0)
-        w = rng.normal(0.0, np.sqrt(var_a), size=e - s)
-        g += w @ z
+    for gv, sp in res:
+        g += gv
+        s2pq += sp
     return g / np.sqrt(max(s2pq, 1e-12))
 
 

@@ -76,7 +76,7 @@ int cbx_bed_snp_counts(cbx_handle* h, const uint8_t* bed, int64_t bed_bytes,
  *                 the exact integer cross-products formed on the tensor cores
  *   allele_freqs: m floats, (float)freq or -1 for filtered SNPs
  *   sum2pq, n_valid: scalars
- * G is also kept on the device inside the handle (see cbx_invert_psd_g). */
+ * G is also kept on the device inside the handle (see cbx_invert_psd). */
 int cbx_grm_bed(cbx_handle* h, const uint8_t* bed, int64_t bed_bytes, int64_t n,
                 int64_t m, float min_maf, int algorithm, int64_t block_size,
                 double* G, int32_t* xx_counts, float* allele_freqs,
@@ -95,7 +95,7 @@ int cbx_mme_create(cbx_handle* h, int64_t n_rec, int64_t p, int64_t q, const dou
                    const double* fx_val);
 
 /* Qinv dense, q x q (DenseMatrixAdapter, src/core/matrix_adapter.h:116-153).
- * Qinv == NULL takes the inverse left on the device by cbx_invert_psd_g. */
+ * Qinv == NULL takes the inverse left on the device by cbx_invert_psd. */
 int cbx_mme_set_qinv_dense(cbx_handle* h, const double* Qinv, int64_t q);
 
 /* Qinv = A + S Gd S^T: A sparse q x q in CSR (a_ptr[q+1] int64, a_col int32,
@@ -128,10 +128,15 @@ int cbx_qinv_apply(cbx_handle* h, int32_t nrhs, const double* X, double* Y);
  * of the MME operator) is bracketed by CUDA events on the handle's stream.
  * cbx_profile_read sums, for bucket 0 (FP32 launches) or 1 (FP64 launches),
  * the launch count, their device time and their algorithmic bytes (the dense
- * block once plus the gathered vectors and outputs).  Enabling clears the log. */
+ * block once plus the gathered vectors and outputs).  Bucket 2 holds the GRM
+ * kernel of cbx_grm_bed, its "bytes" being the algorithmic integer operations
+ * 2 n^2 m_valid.  Enabling clears the log.  cbx_timer_start / cbx_timer_stop
+ * bracket any sequence of calls with CUDA events on the handle's stream. */
 int cbx_profile_enable(cbx_handle* h, int32_t on);
 int cbx_profile_read(cbx_handle* h, int32_t bucket, int64_t* launches, double* total_ms,
                      double* total_bytes);
+int cbx_timer_start(cbx_handle* h);
+int cbx_timer_stop(cbx_handle* h, double* ms);
 
 /* ---- G inverse with eigen-bending -----------------------------------------
  * Replaces invert_psd_matrix (src/core/matrix_io.cpp:488-501): eigenvalues

@@ -193,3 +193,22 @@ def matrix_free_pcg(matvec, b, diag, tol=1e-10, maxit=1000, x0=None):
         p = z + (rz_new / rz) * p
         rz = rz_new
     return x, maxit
+
+
+def sparse_data_part(aid, rows, p, q):
+    """W'W as a scipy CSR matrix (dim x dim) and W as CSR (n x dim), for large cases."""
+    import scipy.sparse as sp
+    n = len(rows)
+    r_idx, c_idx, vals = [], [], []
+    for i, nz in enumerate(rows):
+        for c, v in nz:
+            r_idx.append(i)
+            c_idx.append(c)
+            vals.append(v)
+    aid = np.asarray(aid)
+    ok = (aid > 0) & (aid <= q)
+    r_idx.extend(np.nonzero(ok)[0].tolist())
+    c_idx.extend((p + aid[ok] - 1).tolist())
+    vals.extend([1.0] * int(ok.sum()))
+    W = sp.csr_matrix((vals, (r_idx, c_idx)), shape=(n, p + q))
+    return (W.T @ W).tocsr(), W
