@@ -44,6 +44,9 @@ UNIT = "REML iter/s"
 CONFIGS = {
     "c2": dict(name="gblup_n20000_m50000_cg200", n=20000, m=50000, p_lo=0.01, miss=0.02,
                var_a=0.3, var_e=0.7, levels=200, seed=2000),
+    # profiling case: same generator, G^-1 block (268 MB FP32) still larger than L2
+    "c2s": dict(name="gblup_n8192_m16384_cg200", n=8192, m=16384, p_lo=0.01, miss=0.02,
+                var_a=0.3, var_e=0.7, levels=200, seed=2100),
     "c1": dict(name="gblup_n2000_m10000_sex2", n=2000, m=10000, p_lo=0.05, miss=0.01,
                var_a=0.4, var_e=0.6, levels=2, seed=1000),
 }
