@@ -60,6 +60,11 @@ SIGNATURES = [
                                    C.POINTER(C.c_double)]),
     ("cbx_timer_start", C.c_int, [C.c_void_p]),
     ("cbx_timer_stop", C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
+    ("cbx_ainv_henderson", C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.POINTER(C.c_int64),
+                                     C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("cbx_ssgblup_qinv", C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p,
+                                   C.c_void_p, C.c_double, C.c_int32, C.c_double, C.c_double, C.c_double,
+                                   C.c_void_p, C.c_void_p]),
     # self-test export (not in the public header)
     ("cbx_selftest_umma", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
 ]

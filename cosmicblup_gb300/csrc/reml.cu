@@ -688,6 +688,65 @@ extern "C" int cbx_reml_solve(cbx_handle* h, const cbx_reml_config* cfg, double*
   });
 }
 
+namespace cbx {
+
+// Eigen-bending inverse of a device matrix into out_dev (both n x n, column-major).
+void invert_psd_device(cbx_handle* h, const double* M_dev, int64_t n, double ridge, double* out_dev) {
+  cudaStream_t s = h->stream;
+  Libs& L = libs(h);
+  DevBuf<double> U, w;
+  U.resize((size_t)n * n);
+  w.resize(n);
+  k_add_ridge_copy<<<gridn(n * n, 256, 8 * h->num_sms), 256, 0, s>>>(M_dev, n, ridge > 0 ? ridge : 0.0, U.p);
+  h->launched("k_add_ridge_copy");
+  int lw = 0;
+  CBX_SOLVER(cusolverDnDsyevd_bufferSize(L.sol, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, (int)n, U.p,
+                                         (int)n, w.p, &lw));
+  {
+    DevBuf<double> work;
+    work.resize(std::max(lw, 1));
+    DevBuf<int> info;
+    info.resize(1);
+    CBX_SOLVER(cusolverDnDsyevd(L.sol, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, (int)n, U.p, (int)n, w.p,
+                                work.p, lw, info.p));
+    int hi = 0;
+    CBX_CUDA(cudaMemcpyAsync(&hi, info.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CBX_CUDA(cudaStreamSynchronize(s));
+    CBX_REQUIRE(hi == 0, CBX_ERR_FACTOR, "symmetric eigensolver failed, info " + std::to_string(hi));
+  }
+  std::vector<double> wh = d2h(h, w.p, n);
+  double maxeig = wh[0];
+  for (double v : wh) maxeig = std::max(maxeig, v);
+  const double eps = std::max(1e-12 * maxeig, 1e-6);
+  for (auto& v : wh) if (v < eps) v = eps;
+  CBX_CUDA(cudaMemcpyAsync(w.p, wh.data(), n * sizeof(double), cudaMemcpyHostToDevice, s));
+  DevBuf<double> V;
+  V.resize((size_t)n * n);
+  k_scale_cols<<<gridn(n * n, 256, 8 * h->num_sms), 256, 0, s>>>(U.p, w.p, n, V.p);
+  h->launched("k_scale_cols");
+  const double one = 1.0, zero = 0.0;
+  CBX_BLAS(cublasDgemm(L.blas, CUBLAS_OP_N, CUBLAS_OP_T, (int)n, (int)n, (int)n, &one, V.p, (int)n, U.p, (int)n,
+                       &zero, out_dev, (int)n));
+}
+
+// In-place inverse of an SPD device matrix by Cholesky; false if not PD.
+bool chol_inverse_device(cbx_handle* h, double* A, int64_t n) {
+  if (!potrf(h, A, n)) return false;
+  Libs& L = libs(h);
+  int lw = 0;
+  CBX_SOLVER(cusolverDnDpotri_bufferSize(L.sol, CUBLAS_FILL_MODE_LOWER, (int)n, A, (int)n, &lw));
+  DevBuf<double> work;
+  work.resize(std::max(lw, 1));
+  DevBuf<int> info;
+  info.resize(1);
+  CBX_SOLVER(cusolverDnDpotri(L.sol, CUBLAS_FILL_MODE_LOWER, (int)n, A, (int)n, work.p, lw, info.p));
+  k_symmetrize_lower<<<gridn(n * n, 256, 8 * h->num_sms), 256, 0, h->stream>>>(A, n);
+  h->launched("k_symmetrize_lower");
+  return true;
+}
+
+}  // namespace cbx
+
 // Eigen-bending inverse of M (n x n); M == NULL uses the device GRM of this
 // handle.  The result stays on the device (cbx_mme_set_qinv_dense(h, NULL, n))
 // and is copied to Minv when given.
@@ -696,7 +755,6 @@ extern "C" int cbx_invert_psd(cbx_handle* h, const double* M, int64_t n, double 
     CBX_CUDA(cudaSetDevice(h->device));
     CBX_REQUIRE(n > 0, CBX_ERR_ARG, "n must be positive");
     cudaStream_t s = h->stream;
-    Libs& L = libs(h);
     DevBuf<double> src;
     const double* sp = nullptr;
     if (M) {
@@ -707,41 +765,8 @@ extern "C" int cbx_invert_psd(cbx_handle* h, const double* M, int64_t n, double 
       CBX_REQUIRE(h->G.p && h->G_n == n, CBX_ERR_STATE, "no device GRM of this order (cbx_grm_bed)");
       sp = h->G.p;
     }
-    DevBuf<double> U, w;
-    U.resize((size_t)n * n);
-    w.resize(n);
-    k_add_ridge_copy<<<gridn(n * n, 256, 8 * h->num_sms), 256, 0, s>>>(sp, n, ridge > 0 ? ridge : 0.0, U.p);
-    h->launched("k_add_ridge_copy");
-    src.release();
-    int lw = 0;
-    CBX_SOLVER(cusolverDnDsyevd_bufferSize(L.sol, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, (int)n, U.p,
-                                           (int)n, w.p, &lw));
-    {
-      DevBuf<double> work;
-      work.resize(std::max(lw, 1));
-      DevBuf<int> info;
-      info.resize(1);
-      CBX_SOLVER(cusolverDnDsyevd(L.sol, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, (int)n, U.p, (int)n, w.p,
-                                  work.p, lw, info.p));
-      int hi = 0;
-      CBX_CUDA(cudaMemcpyAsync(&hi, info.p, sizeof(int), cudaMemcpyDeviceToHost, s));
-      CBX_CUDA(cudaStreamSynchronize(s));
-      CBX_REQUIRE(hi == 0, CBX_ERR_FACTOR, "symmetric eigensolver failed, info " + std::to_string(hi));
-    }
-    std::vector<double> wh = d2h(h, w.p, n);
-    double maxeig = wh[0];
-    for (double v : wh) maxeig = std::max(maxeig, v);
-    const double eps = std::max(1e-12 * maxeig, 1e-6);
-    for (auto& v : wh) if (v < eps) v = eps;
-    CBX_CUDA(cudaMemcpyAsync(w.p, wh.data(), n * sizeof(double), cudaMemcpyHostToDevice, s));
-    DevBuf<double> V;
-    V.resize((size_t)n * n);
-    k_scale_cols<<<gridn(n * n, 256, 8 * h->num_sms), 256, 0, s>>>(U.p, w.p, n, V.p);
-    h->launched("k_scale_cols");
     h->Ginv.resize((size_t)n * n);
-    const double one = 1.0, zero = 0.0;
-    CBX_BLAS(cublasDgemm(L.blas, CUBLAS_OP_N, CUBLAS_OP_T, (int)n, (int)n, (int)n, &one, V.p, (int)n, U.p, (int)n,
-                         &zero, h->Ginv.p, (int)n));
+    invert_psd_device(h, sp, n, ridge, h->Ginv.p);
     h->Ginv_n = n;
     if (Minv) CBX_CUDA(cudaMemcpyAsync(Minv, h->Ginv.p, (size_t)n * n * sizeof(double), cudaMemcpyDeviceToHost, s));
     CBX_CUDA(cudaStreamSynchronize(s));
