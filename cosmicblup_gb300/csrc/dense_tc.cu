@@ -1,0 +1,339 @@
+// Dense block product on the tensor cores for the FP32 PCG bulk:
+//   Tpart[ks][i][c] = sum_{k in split ks} Qd[i][k] * Vt[c][k]      (S = 16 or 32 columns)
+// with 3xTF32 splitting (hi*hi + hi*lo + lo*hi, FP32 accumulation in TMEM),
+// which keeps FP32-level accuracy on the tf32 tensor path.
+//
+// This replaces, for probe blocks, the CUDA-core product of DenseMatrixAdapter /
+// SplitMatrixAdapter (reference src/core/matrix_adapter.h:125-127, 252-278)
+// applied to every probe of AdaptiveTraceEstimator.  One persistent CTA per SM
+// walks (128-row tile, K split) work units:
+//   warp 0  TMA producer (SWIZZLE_128B tiles of Qd and Vt),
+//   warp 1  TMEM owner and MMA issuer (kind::tf32, M = 128, N = S),
+//   warps 2-5 split each staged tile into tf32 hi / lo parts in shared memory,
+//   warps 6-9 epilogue (TMEM -> partial sums in global memory).
+// The K splits are summed in a fixed order by the consumer (k_spmv), so the
+// result is deterministic.
+#include <cuda.h>
+#include <algorithm>
+#include <vector>
+#include "handle.h"
+#include "dense_tc.h"
+
+namespace cbx {
+namespace dtc {
+
+constexpr int KB = 32;                 // FP32 elements per 128-byte row of a tile
+constexpr int NSTAGE = 4;
+constexpr int A_BYTES = 128 * KB * 4;  // 16 KB
+constexpr int THREADS = 320;
+
+template <int S>
+struct Layout {
+  static constexpr int B_BYTES = S * KB * 4;
+  static constexpr int STAGE = 2 * A_BYTES + 2 * 4096;  // A, A_lo, B, B_lo (B padded to 4 KB)
+  static constexpr int OFF_BAR = NSTAGE * STAGE;
+  static constexpr int SMEM = OFF_BAR + 256 + 1024;     // + alignment slack
+};
+
+struct Bars {
+  uint64_t full[NSTAGE], conv[NSTAGE], empty[NSTAGE];
+  uint64_t acc_full[2], acc_empty[2], drain;
+  uint32_t tmem;
+  int abort;
+};
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_addr(bar))
+      : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void umma_tf32(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(d),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc)
+      : "memory");
+}
+// K-major SWIZZLE_128B descriptor: 8-row groups 1024 bytes apart.
+__device__ __forceinline__ uint64_t sdesc_sw128(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+  d |= (uint64_t)1 << 16;              // leading byte offset (unused for swizzled K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;    // stride byte offset
+  d |= (uint64_t)1 << 46;              // descriptor version
+  d |= (uint64_t)2 << 61;              // SWIZZLE_128B
+  return d;
+}
+__host__ __device__ constexpr uint32_t idesc_tf32(uint32_t M, uint32_t N) {
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((N >> 3) << 17) | ((M >> 4) << 24);
+}
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr)
+      : "memory");
+}
+
+// hi = a with the 13 low mantissa bits cleared (exact tf32), lo = a - hi (exact in FP32)
+__device__ __forceinline__ void split4(float4& v, float4& lo) {
+  float* p = reinterpret_cast<float*>(&v);
+  float* q = reinterpret_cast<float*>(&lo);
+#pragma unroll
+  for (int e = 0; e < 4; ++e) {
+    const float hi = __uint_as_float(__float_as_uint(p[e]) & 0xFFFFE000u);
+    q[e] = p[e] - hi;
+    p[e] = hi;
+  }
+}
+
+template <int S>
+__global__ void __launch_bounds__(THREADS, 1)
+    k_dense_tf32(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int ng,
+                 int ksteps, int ksplit, int kps, int nunits, float* __restrict__ Tpart, const int* active,
+                 int* status) {
+  if (active && *active == 0) return;
+  using LY = Layout<S>;
+  extern __shared__ uint8_t dsm_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(dsm_raw) + 1023) & ~uintptr_t(1023));
+  Bars* bars = reinterpret_cast<Bars*>(smem + LY::OFF_BAR);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (tid == 0) {
+    for (int i = 0; i < NSTAGE; ++i) {
+      mbar_init(&bars->full[i], 1);
+      mbar_init(&bars->conv[i], 128);
+      mbar_init(&bars->empty[i], 1);
+    }
+    for (int i = 0; i < 2; ++i) {
+      mbar_init(&bars->acc_full[i], 1);
+      mbar_init(&bars->acc_empty[i], 4);
+    }
+    mbar_init(&bars->drain, 1);
+    bars->abort = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    tmem_alloc(&bars->tmem, 64);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = bars->tmem;
+  volatile int* abort_flag = &bars->abort;
+  auto fail = [&]() {
+    bars->abort = 1;
+    atomicExch(status, DEV_TIMEOUT);
+  };
+
+  if (warp == 0) {
+    if (lane == 0) {
+      uint32_t g = 0;
+      bool ok = true;
+      for (int u = blockIdx.x; u < nunits && ok; u += gridDim.x) {
+        const int mt = u / ksplit, ks = u % ksplit;
+        const int k0 = ks * kps, k1 = min(ksteps, k0 + kps);
+        for (int k = k0; k < k1; ++k, ++g) {
+          const uint32_t s = g % NSTAGE;
+          if (!mbar_wait(&bars->empty[s], ((g / NSTAGE) & 1) ^ 1, abort_flag)) { ok = false; break; }
+          uint8_t* st = smem + s * LY::STAGE;
+          mbar_expect_tx(&bars->full[s], A_BYTES + LY::B_BYTES);
+          tma_load_2d(smem_addr(st), &tmA, k * KB, mt * 128, &bars->full[s]);
+          tma_load_2d(smem_addr(st + 2 * A_BYTES), &tmB, k * KB, 0, &bars->full[s]);
+        }
+      }
+      if (!ok) fail();
+    }
+    __syncwarp();
+  } else if (warp == 1) {
+    if (lane == 0) {
+      constexpr uint32_t ID = idesc_tf32(128, S);
+      uint32_t g = 0, c = 0;
+      bool ok = true;
+      for (int u = blockIdx.x; u < nunits && ok; u += gridDim.x, ++c) {
+        const int ks = u % ksplit;
+        const int k0 = ks * kps, k1 = min(ksteps, k0 + kps);
+        const uint32_t b = c & 1;
+        if (!mbar_wait(&bars->acc_empty[b], ((c >> 1) & 1) ^ 1, abort_flag)) { ok = false; break; }
+        tc_fence_after();
+        const uint32_t d = tmem + b * 32;
+        for (int k = k0; k < k1; ++k, ++g) {
+          const uint32_t s = g % NSTAGE;
+          if (!mbar_wait(&bars->conv[s], (g / NSTAGE) & 1, abort_flag)) { ok = false; break; }
+          tc_fence_after();
+          const uint32_t st = smem_addr(smem + s * LY::STAGE);
+          const uint64_t dA = sdesc_sw128(st), dAl = sdesc_sw128(st + A_BYTES);
+          const uint64_t dB = sdesc_sw128(st + 2 * A_BYTES), dBl = sdesc_sw128(st + 2 * A_BYTES + 4096);
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {  // four K slices of 8 tf32 (32 bytes) per 128-byte row
+            const uint32_t first = (k == k0 && j == 0) ? 0u : 1u;
+            umma_tf32(d, dA + 2 * j, dB + 2 * j, ID, first);
+            umma_tf32(d, dA + 2 * j, dBl + 2 * j, ID, 1u);
+            umma_tf32(d, dAl + 2 * j, dB + 2 * j, ID, 1u);
+          }
+          umma_commit(&bars->empty[s]);
+        }
+        if (!ok) break;
+        umma_commit(&bars->acc_full[b]);
+      }
+      if (!ok) fail();
+      umma_commit(&bars->drain);
+      const uint64_t t0 = global_ns();
+      while (!mbar_try(&bars->drain, 0) && global_ns() - t0 < kWaitLimitNs) {}
+    }
+    __syncwarp();
+  } else if (warp < 6) {
+    // converters: split the staged tiles into tf32 hi (in place) and lo
+    const int t = tid - 64;
+    uint32_t g = 0;
+    bool ok = true;
+    for (int u = blockIdx.x; u < nunits && ok; u += gridDim.x) {
+      const int ks = u % ksplit;
+      const int k0 = ks * kps, k1 = min(ksteps, k0 + kps);
+      for (int k = k0; k < k1; ++k, ++g) {
+        const uint32_t s = g % NSTAGE;
+        if (!mbar_wait(&bars->full[s], (g / NSTAGE) & 1, abort_flag)) { ok = false; break; }
+        uint8_t* st = smem + s * LY::STAGE;
+        float4* A = reinterpret_cast<float4*>(st);
+        float4* Al = reinterpret_cast<float4*>(st + A_BYTES);
+#pragma unroll 4
+        for (int i = t; i < A_BYTES / 16; i += 128) {
+          float4 v = A[i], lo;
+          split4(v, lo);
+          A[i] = v;
+          Al[i] = lo;
+        }
+        float4* B = reinterpret_cast<float4*>(st + 2 * A_BYTES);
+        float4* Bl = reinterpret_cast<float4*>(st + 2 * A_BYTES + 4096);
+        for (int i = t; i < LY::B_BYTES / 16; i += 128) {
+          float4 v = B[i], lo;
+          split4(v, lo);
+          B[i] = v;
+          Bl[i] = lo;
+        }
+        fence_async_smem();
+        mbar_arrive(&bars->conv[s]);
+      }
+    }
+    if (!ok) fail();
+  } else {
+    // epilogue: TMEM lane quadrant (warp % 4), one output row per thread
+    const int q = warp & 3;
+    uint32_t c = 0;
+    bool ok = true;
+    for (int u = blockIdx.x; u < nunits && ok; u += gridDim.x, ++c) {
+      const int mt = u / ksplit, ks = u % ksplit;
+      const uint32_t b = c & 1;
+      if (!mbar_wait(&bars->acc_full[b], (c >> 1) & 1, abort_flag)) { ok = false; break; }
+      tc_fence_after();
+      uint32_t r[32];
+      tmem_ld32(tmem + (uint32_t(q * 32) << 16) + b * 32, r);
+      tmem_ld_wait();
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&bars->acc_empty[b]);
+      const int row = mt * 128 + q * 32 + lane;
+      if (row < ng) {
+        float4* dst = reinterpret_cast<float4*>(Tpart + ((int64_t)ks * ng + row) * S);
+#pragma unroll
+        for (int j = 0; j < S / 4; ++j)
+          dst[j] = make_float4(__uint_as_float(r[4 * j]), __uint_as_float(r[4 * j + 1]),
+                               __uint_as_float(r[4 * j + 2]), __uint_as_float(r[4 * j + 3]));
+      }
+    }
+    if (!ok) fail();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 1) tmem_dealloc(tmem, 64);
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    CBX_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q));
+    CBX_REQUIRE(p && q == cudaDriverEntryPointSuccess, CBX_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+    fn = reinterpret_cast<EncodeTiledFn>(p);
+  }
+  return fn;
+}
+
+static CUtensorMap make_map(const float* base, int64_t cols, int64_t rows, int box_rows) {
+  CUtensorMap m;
+  const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+  const cuuint64_t strides[1] = {(cuuint64_t)cols * 4};
+  const cuuint32_t box[2] = {(cuuint32_t)KB, (cuuint32_t)box_rows};
+  const cuuint32_t es[2] = {1, 1};
+  CUresult r = encode_fn()(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides, box, es,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  CBX_REQUIRE(r == CUDA_SUCCESS, CBX_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+  return m;
+}
+
+}  // namespace dtc
+
+int dense_tc_ksplit(int64_t ng, int64_t ld, int num_sms) {
+  const int mtiles = (int)((ng + 127) / 128);
+  const int ksteps = (int)((ld + dtc::KB - 1) / dtc::KB);
+  int best = 1;
+  double best_eff = -1;
+  for (int ks = 1; ks <= 8 && ks <= ksteps; ++ks) {
+    // every split must own at least one K step: use the effective split count
+    const int kps = (ksteps + ks - 1) / ks;
+    const int eff_ks = (ksteps + kps - 1) / kps;
+    const int units = mtiles * eff_ks;
+    const int waves = (units + num_sms - 1) / num_sms;
+    const double eff = (double)units / ((double)waves * num_sms);
+    if (eff > best_eff + 0.02) {
+      best_eff = eff;
+      best = eff_ks;
+    }
+  }
+  return best;
+}
+
+void dense_tc(cbx_handle* h, const float* Qd, int64_t ng, int64_t ld, const float* Vt, int S, int ksplit, float* Tpart,
+              const int* active) {
+  CBX_REQUIRE(S == 16 || S == 32, CBX_ERR_ARG, "dense_tc supports 16 or 32 columns");
+  CBX_REQUIRE(ld % 4 == 0, CBX_ERR_ARG, "row pitch must be a multiple of 4");
+  const CUtensorMap ma = dtc::make_map(Qd, ld, ng, 128);
+  const CUtensorMap mb = dtc::make_map(Vt, ld, S, S);
+  const int ksteps = (int)((ld + dtc::KB - 1) / dtc::KB);
+  const int kps = (ksteps + ksplit - 1) / ksplit;
+  CBX_REQUIRE((int64_t)(ksplit - 1) * kps < ksteps, CBX_ERR_ARG, "K split leaves an empty split");
+  const int mtiles = (int)((ng + 127) / 128);
+  const int nunits = mtiles * ksplit;
+  const int grid = std::min(nunits, h->num_sms);
+  if (S == 32) {
+    constexpr int SM = dtc::Layout<32>::SMEM;
+    CBX_CUDA(cudaFuncSetAttribute(dtc::k_dense_tf32<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, SM));
+    dtc::k_dense_tf32<32><<<grid, dtc::THREADS, SM, h->stream>>>(ma, mb, (int)ng, ksteps, ksplit, kps, nunits, Tpart,
+                                                                 active, h->status.p);
+  } else {
+    constexpr int SM = dtc::Layout<16>::SMEM;
+    CBX_CUDA(cudaFuncSetAttribute(dtc::k_dense_tf32<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, SM));
+    dtc::k_dense_tf32<16><<<grid, dtc::THREADS, SM, h->stream>>>(ma, mb, (int)ng, ksteps, ksplit, kps, nunits, Tpart,
+                                                                 active, h->status.p);
+  }
+  h->launched("k_dense_tf32");
+}
+
+}  // namespace cbx

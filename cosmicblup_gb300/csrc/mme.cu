@@ -16,6 +16,8 @@
 #include "handle.h"
 #include "pcg.h"
 #include "solver.cuh"
+#include "dense_tc.h"
+#include <cstdlib>
 
 namespace cbx {
 namespace sv {
@@ -170,7 +172,7 @@ struct Workspace {
     if (dim == m.dim && (!m.has_dense || Vt.n == (size_t)S * m.ld)) return;
     const int64_t n = m.dim * S;
     R.resize(n); Z.resize(n); P.resize(n); Q.resize(n); X.resize(n);
-    if (m.has_dense) { Vt.resize((size_t)S * m.ld); Tout.resize((size_t)m.ng * S); }
+    if (m.has_dense) { Vt.resize((size_t)S * m.ld); Tout.resize((size_t)m.ng * S * 8); }
     nblk_vec = (int)grid_for(n, sv::NT, 2 * num_sms);
     nblk_spmv = (int)m.p + (int)grid_for(m.dim - m.p, 8, 8 * num_sms);
     part.resize((size_t)nblk_vec * 3 * S);
@@ -183,11 +185,42 @@ struct Workspace {
   }
 };
 
+// FP32 probe blocks of 16 or 32 columns use the tcgen05 3xTF32 product unless
+// the environment sets CBX_DENSE_TC=0.
+static bool use_dense_tc() {
+  static int v = -1;
+  if (v < 0) {
+    const char* e = std::getenv("CBX_DENSE_TC");
+    v = (e && e[0] == '0') ? 0 : 1;
+  }
+  return v == 1;
+}
+
 template <typename T, int S>
 void matvec(cbx_handle* h, const sv::OpView<T>& op, Workspace<T, S>& w, const T* X, T* Y, double lam, int use_D,
             const T* P, double* pq_part, const int* active) {
   cudaStream_t s = h->stream;
-  if (op.Qd) {
+  int tsplit = 1;
+  if (op.Qd && sizeof(T) == 4 && (S == 16 || S == 32) && use_dense_tc()) {
+    sv::k_gather_t<T, S><<<grid_for(S * op.ld, 256, 4 * h->num_sms), 256, 0, s>>>(X, w.Vt.p, op.p, op.ng, op.ld,
+                                                                               op.gmap, active);
+    h->launched("k_gather_t");
+    tsplit = dense_tc_ksplit(op.ng, op.ld, h->num_sms);
+    cbx_handle::ProfRec pr{};
+    if (h->prof_on) {
+      CBX_CUDA(cudaEventCreate(&pr.a));
+      CBX_CUDA(cudaEventCreate(&pr.b));
+      CBX_CUDA(cudaEventRecord(pr.a, s));
+    }
+    dense_tc(h, reinterpret_cast<const float*>(op.Qd), op.ng, op.ld, reinterpret_cast<const float*>(w.Vt.p), S,
+             tsplit, reinterpret_cast<float*>(w.Tout.p), active);
+    if (h->prof_on) {
+      CBX_CUDA(cudaEventRecord(pr.b, s));
+      pr.bucket = 0;
+      pr.bytes = 4.0 * ((double)op.ng * op.ld + (double)S * op.ld + (double)op.ng * S * tsplit);
+      h->prof.push_back(pr);
+    }
+  } else if (op.Qd) {
     sv::k_gather_t<T, S><<<grid_for(S * op.ld, 256, 4 * h->num_sms), 256, 0, s>>>(X, w.Vt.p, op.p, op.ng, op.ld,
                                                                                op.gmap, active);
     h->launched("k_gather_t");
@@ -212,7 +245,7 @@ void matvec(cbx_handle* h, const sv::OpView<T>& op, Workspace<T, S>& w, const T*
       h->prof.push_back(pr);
     }
   }
-  sv::k_spmv<T, S><<<w.nblk_spmv, sv::NT, 0, s>>>(op, X, w.Tout.p, (T)lam, use_D, Y, P, pq_part, active);
+  sv::k_spmv<T, S><<<w.nblk_spmv, sv::NT, 0, s>>>(op, X, w.Tout.p, tsplit, (T)lam, use_D, Y, P, pq_part, active);
   h->launched("k_spmv");
 }
 
@@ -367,8 +400,15 @@ struct Solver : public SolverBase {
     const int64_t n = m.dim * S;
     if (!use_x0) CBX_CUDA(cudaMemsetAsync(Xi.p, 0, n * sizeof(double), s));
     std::vector<double> bn = norms(h, m, Bi.p);
+    std::vector<double> rn;
+    if (use_x0) {
+      rn = residual(h, m, op64, lam, res.matvecs);
+    } else {
+      // x0 = 0: the residual is b itself, no FP64 operator application needed
+      CBX_CUDA(cudaMemcpyAsync(R64.p, Bi.p, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+      rn = bn;
+    }
     for (auto& b : bn) if (!(b > 0)) b = 1.0;
-    std::vector<double> rn = residual(h, m, op64, lam, res.matvecs);
     std::vector<int> done(ncols, 0);
     for (int c = 0; c < ncols; ++c)
       if ((abs_tol ? rn[c] : rn[c] / bn[c]) < tol) done[c] = 1;

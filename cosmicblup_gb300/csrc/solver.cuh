@@ -149,7 +149,7 @@ __device__ __forceinline__ double block_sum_cols(double v, double* red /*[NT]*/)
 // random-effect rows, one warp per row, in a grid-stride loop.
 template <typename T, int S>
 __global__ void __launch_bounds__(NT) k_spmv(OpView<T> op, const T* __restrict__ X,
-                                             const T* __restrict__ Tout, T lam, int use_D,
+                                             const T* __restrict__ Tout, int tsplit, T lam, int use_D,
                                              T* __restrict__ Y, const T* __restrict__ P,
                                              double* __restrict__ pq_part,
                                              const int* __restrict__ active) {
@@ -203,7 +203,10 @@ __global__ void __launch_bounds__(NT) k_spmv(OpView<T> op, const T* __restrict__
       if (lane < S) {
         if (op.Qd) {
           const int32_t k = op.ginv[u];
-          if (k >= 0) qv += Tout[(int64_t)k * S + c];
+          if (k >= 0) {
+            // K-split partial sums of the dense block product, in a fixed order
+            for (int t = 0; t < tsplit; ++t) qv += Tout[((int64_t)t * op.ng + k) * S + c];
+          }
         }
         const T yv = acc + lam * qv;
         Y[i * S + c] = yv;

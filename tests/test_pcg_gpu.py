@@ -156,3 +156,20 @@ def test_input_errors(handle, gblup):
     dm = DeviceMME(handle, gblup["rec"]["y"], gblup["rec"]["aid"], gblup["rows"], gblup["p"], gblup["n"])
     with pytest.raises(CbxError, match="STATE"):
         dm.pcg_solve(1.0, np.ones(dm.dim))
+
+
+@pytest.mark.parametrize("k", [16, 32])
+def test_mixed_probe_block_tensor_cores(handle, gblup, k):
+    """Blocks of 16 / 32 probes use the tcgen05 3xTF32 block product in the FP32 bulk."""
+    om, lam = gblup["mme"], 2.0
+    A = om.lhs(gblup["Gi"], lam)
+    rng = np.random.default_rng(40 + k)
+    B = np.zeros((om.dim, k))
+    B[om.p:, :] = rng.choice([-1.0, 1.0], size=(om.q, k))
+    dm = dev_mme(handle, gblup)
+    X, it, rr = dm.pcg_solve(lam, B, precision=MIXED)
+    Xe = np.linalg.solve(A, B)
+    for c in range(k):
+        true = np.linalg.norm(B[:, c] - A @ X[:, c]) / np.linalg.norm(B[:, c])
+        assert true < 1e-10 and rr[c] < 1e-10, (c, true)
+        assert rel(X[:, c], Xe[:, c]) < 1e-8, c
