@@ -65,6 +65,10 @@ SIGNATURES = [
     ("cbx_ssgblup_qinv", C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p,
                                    C.c_void_p, C.c_double, C.c_int32, C.c_double, C.c_double, C.c_double,
                                    C.c_void_p, C.c_void_p]),
+    ("cbx_reml_gradient", C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_int32, C.c_int32, C.c_int32,
+                                    C.c_int32, C.c_double, C.c_int32, C.c_void_p, C.POINTER(C.c_double),
+                                    C.POINTER(C.c_int64)]),
+    ("cbx_reml_logl_dense", C.c_int, [C.c_void_p, C.c_double, C.c_double, C.POINTER(C.c_double)]),
     # self-test export (not in the public header)
     ("cbx_selftest_umma", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
 ]

@@ -164,6 +164,7 @@ template <typename T, int S>
 struct Workspace {
   DevBuf<T> R, Z, P, Q, Vt, Tout, X;
   DevBuf<double> part, pq_part, rz_fix, tol;
+  DevBuf<T> seg_part;
   DevBuf<sv::Col> col;
   DevBuf<int> active;
   int nblk_vec = 0, nblk_spmv = 0;
@@ -181,6 +182,7 @@ struct Workspace {
     tol.resize(S);
     col.resize(S);
     active.resize(1);
+    seg_part.resize((size_t)std::max<int32_t>(m.nseg, 1) * S);
     dim = m.dim;
   }
 };
@@ -245,7 +247,13 @@ void matvec(cbx_handle* h, const sv::OpView<T>& op, Workspace<T, S>& w, const T*
       h->prof.push_back(pr);
     }
   }
-  sv::k_spmv<T, S><<<w.nblk_spmv, sv::NT, 0, s>>>(op, X, w.Tout.p, tsplit, (T)lam, use_D, Y, P, pq_part, active);
+  if (use_D && h->mme->nseg > 0) {
+    const Mme& mm = *h->mme;
+    sv::k_fix_seg<T, S><<<mm.nseg, sv::NT, 0, s>>>(op, mm.seg_row.p, mm.seg_lo.p, mm.seg_hi.p, X, w.seg_part.p, active);
+    h->launched("k_fix_seg");
+  }
+  sv::k_spmv<T, S><<<w.nblk_spmv, sv::NT, 0, s>>>(op, X, w.Tout.p, tsplit, h->mme->fix_seg_ptr.p, w.seg_part.p,
+                                                  (T)lam, use_D, Y, P, pq_part, active);
   h->launched("k_spmv");
 }
 
@@ -272,7 +280,7 @@ void run_pcg(cbx_handle* h, Mme& m, const sv::OpView<T>& op, Workspace<T, S>& w,
   std::vector<double> tolv(S, 1.0);
   for (int c = 0; c < ncols; ++c) tolv[c] = tol_col[c];
   CBX_CUDA(cudaMemcpyAsync(w.tol.p, tolv.data(), S * sizeof(double), cudaMemcpyHostToDevice, s));
-  sv::k_scalar_init<S><<<1, 32, 0, s>>>(w.col.p, ncols, w.part.p, w.nblk_vec, w.rz_fix.p, m.p, abs_tol, w.active.p);
+  sv::k_scalar_init<S><<<1, sv::NT, 0, s>>>(w.col.p, ncols, w.part.p, w.nblk_vec, w.rz_fix.p, m.p, abs_tol, w.active.p);
   h->launched("k_scalar_init");
   CBX_CUDA(cudaMemcpyAsync(w.P.p, w.Z.p, n * sizeof(T), cudaMemcpyDeviceToDevice, s));
   int host_active = 1;
@@ -280,7 +288,7 @@ void run_pcg(cbx_handle* h, Mme& m, const sv::OpView<T>& op, Workspace<T, S>& w,
   for (int it = 0; it < maxit && host_active; it += CHECK) {
     for (int j = 0; j < CHECK; ++j) {
       matvec<T, S>(h, op, w, w.P.p, w.Q.p, lam, 1, w.P.p, w.pq_part.p, w.active.p);
-      sv::k_scalar_alpha<S><<<1, 32, 0, s>>>(w.col.p, w.pq_part.p, w.nblk_spmv);
+      sv::k_scalar_alpha<S><<<1, sv::NT, 0, s>>>(w.col.p, w.pq_part.p, w.nblk_spmv);
       h->launched("k_scalar_alpha");
       sv::k_update<T, S><<<w.nblk_vec, sv::NT, 0, s>>>(op, w.col.p, X, w.R.p, w.Z.p, w.P.p, w.Q.p, w.part.p);
       h->launched("k_update");
@@ -288,7 +296,7 @@ void run_pcg(cbx_handle* h, Mme& m, const sv::OpView<T>& op, Workspace<T, S>& w,
         sv::k_fixed<T, S><<<(unsigned)m.p, sv::NT, 0, s>>>(op, w.R.p, w.Z.p, w.col.p, w.rz_fix.p);
         h->launched("k_fixed");
       }
-      sv::k_scalar_beta<S><<<1, 32, 0, s>>>(w.col.p, w.part.p, w.nblk_vec, w.rz_fix.p, m.p, w.tol.p, abs_tol,
+      sv::k_scalar_beta<S><<<1, sv::NT, 0, s>>>(w.col.p, w.part.p, w.nblk_vec, w.rz_fix.p, m.p, w.tol.p, abs_tol,
                                             maxit, w.active.p);
       h->launched("k_scalar_beta");
       sv::k_pupdate<T, S><<<w.nblk_vec, sv::NT, 0, s>>>(m.dim, w.col.p, w.Z.p, w.P.p);
@@ -703,6 +711,28 @@ extern "C" int cbx_mme_create(cbx_handle* h, int64_t n_rec, int64_t p, int64_t q
         if (col[j] == i) diag[i] = val[j];
         if (i < p && col[j] < p) A11[i * p + col[j]] = val[j];
       }
+    {
+      // segments of the fixed-effect rows (sv::FIX_SEG entries at most)
+      std::vector<int32_t> srow, slo, shi, sptr(p + 1, 0);
+      for (int64_t f = 0; f < p; ++f) {
+        for (int32_t j = ptr[f]; j < ptr[f + 1]; j += sv::FIX_SEG) {
+          srow.push_back((int32_t)f);
+          slo.push_back(j);
+          shi.push_back(std::min<int32_t>(ptr[f + 1], j + sv::FIX_SEG));
+        }
+        sptr[f + 1] = (int32_t)srow.size();
+      }
+      m->nseg = (int32_t)srow.size();
+      m->fix_seg_ptr.resize(p + 1);
+      CBX_CUDA(cudaMemcpyAsync(m->fix_seg_ptr.p, sptr.data(), (p + 1) * 4, cudaMemcpyHostToDevice, s));
+      if (m->nseg > 0) {
+        m->seg_row.resize(m->nseg); m->seg_lo.resize(m->nseg); m->seg_hi.resize(m->nseg);
+        CBX_CUDA(cudaMemcpyAsync(m->seg_row.p, srow.data(), m->nseg * 4, cudaMemcpyHostToDevice, s));
+        CBX_CUDA(cudaMemcpyAsync(m->seg_lo.p, slo.data(), m->nseg * 4, cudaMemcpyHostToDevice, s));
+        CBX_CUDA(cudaMemcpyAsync(m->seg_hi.p, shi.data(), m->nseg * 4, cudaMemcpyHostToDevice, s));
+      }
+      CBX_CUDA(cudaStreamSynchronize(s));
+    }
     upload_csr<double>(s, dim, ptr, col, val, m->D64);
     upload_csr<float>(s, dim, ptr, col, val, m->D32);
     m->diagD.resize(dim);

@@ -38,6 +38,9 @@ struct Mme {
   Csr<double> D64;                 // W'W
   Csr<float> D32;
   DevBuf<double> rhs;              // W'y (dim)
+  // fixed-effect rows of W'W cut into segments of at most FIX_SEG entries
+  int32_t nseg = 0;
+  DevBuf<int32_t> seg_row, seg_lo, seg_hi, fix_seg_ptr;  // fix_seg_ptr: p + 1
   DevBuf<double> diagD;            // diag(W'W) (dim)
   // Qinv
   bool has_dense = false, has_sparse = false;

@@ -389,6 +389,83 @@ static void em_iteration(cbx_handle* h, const RemlConfigI& cfg, double& vu, doub
 }
 
 // ---------------------------------------------------------------------------
+// REML score with respect to (var_u, var_e) -- the data-driven AI-REML score of
+// run_aireml_step (vce.cpp:2648-2675), which is the exact REML derivative:
+//   d logL / d var_u = (u'Qinv u + var_e tr - q var_u) / (2 var_u^2)
+//   d logL / d var_e = (e'e - var_e (n - p - q + lambda tr)) / (2 var_e^2)
+// with tr = tr(Qinv C^uu) estimated from `nprobe` Rademacher probes (the
+// reference's probe stream, batches of 16 seeded seed + done) solved as
+// multi-RHS blocks, or exactly from the q unit vectors (exact != 0).
+static void reml_gradient(cbx_handle* h, double vu, double ve, int nprobe, int seed, int exact, int precision,
+                          double pcg_tol, int pcg_maxit, double* grad, double* trace_out, int64_t* iters_out) {
+  Mme& m = *h->mme;
+  cudaStream_t s = h->stream;
+  const int64_t p = m.p, q = m.q, dim = m.dim, n = m.n_rec;
+  const double lam = ve / std::max(vu, 1e-9);
+  int64_t iters = 0;
+  DevBuf<double> sol;
+  sol.resize(dim);
+  PcgResult r;
+  pcg_solve(h, lam, 1, m.rhs.p, sol.p, false, pcg_tol, pcg_maxit, 0, precision, r);
+  iters += r.iters[0];
+  const double e_sse = record_residual(h, sol.p, nullptr);
+  DevBuf<double> Qu;
+  Qu.resize(q);
+  qinv_apply(h, 1, sol.p + p, Qu.p);
+  const double uQu = dot_h(d2h(h, sol.p + p, q), d2h(h, Qu.p, q));
+  const int64_t total = exact ? q : nprobe;
+  CBX_REQUIRE(total > 0, CBX_ERR_ARG, "nprobe must be positive");
+  double tsum = 0.0;
+  const int64_t blk = 32;
+  // probe generator state: the reference's batches of 16 from mt19937_64(seed + done)
+  std::mt19937_64 gen;
+  std::uniform_int_distribution<int> dist(0, 1);
+  for (int64_t c0 = 0; c0 < total; c0 += blk) {
+    const int k = (int)std::min<int64_t>(blk, total - c0);
+    std::vector<double> Bh((size_t)dim * k, 0.0), Z((size_t)q * k, 0.0);
+    for (int j = 0; j < k; ++j) {
+      const int64_t idx = c0 + j;
+      if (exact) {
+        Z[(size_t)j * q + idx] = 1.0;
+        Bh[(size_t)j * dim + p + idx] = 1.0;
+      } else {
+        if (idx % 16 == 0) gen.seed((unsigned long)(seed + idx));
+        for (int64_t i = 0; i < q; ++i) {
+          const double z = dist(gen) == 0 ? -1.0 : 1.0;
+          Z[(size_t)j * q + i] = z;
+          Bh[(size_t)j * dim + p + i] = z;
+        }
+      }
+    }
+    DevBuf<double> B, X, Wu, QW;
+    B.resize((size_t)dim * k);
+    X.resize((size_t)dim * k);
+    Wu.resize((size_t)q * k);
+    QW.resize((size_t)q * k);
+    CBX_CUDA(cudaMemcpyAsync(B.p, Bh.data(), Bh.size() * sizeof(double), cudaMemcpyHostToDevice, s));
+    PcgResult pr;
+    pcg_solve(h, lam, k, B.p, X.p, false, pcg_tol, pcg_maxit, 0, precision, pr);
+    for (int c = 0; c < k; ++c) iters += pr.iters[c];
+    CBX_CUDA(cudaMemcpy2DAsync(Wu.p, q * sizeof(double), X.p + p, dim * sizeof(double), q * sizeof(double), k,
+                               cudaMemcpyDeviceToDevice, s));
+    qinv_apply(h, k, Wu.p, QW.p);
+    const auto QWh = d2h(h, QW.p, (size_t)q * k);
+    for (int j = 0; j < k; ++j) {
+      double v = 0;
+      for (int64_t i = 0; i < q; ++i) v += Z[(size_t)j * q + i] * QWh[(size_t)j * q + i];
+      tsum += v;
+    }
+  }
+  const double tr = exact ? tsum : tsum / (double)total;
+  double lambda_tr = lam * tr;
+  if (lambda_tr > q - 1e-6) lambda_tr = q - 1e-6;  // as the reference (vce.cpp:2662)
+  grad[0] = 0.5 * (uQu + tr * ve - (double)q * vu) / (vu * vu);
+  grad[1] = 0.5 * (e_sse - ve * ((double)(n - p - q) + lambda_tr)) / (ve * ve);
+  if (trace_out) *trace_out = tr;
+  if (iters_out) *iters_out = iters;
+}
+
+// ---------------------------------------------------------------------------
 // dense exact AI step
 struct DenseExact {
   bool init = false;
@@ -746,6 +823,30 @@ bool chol_inverse_device(cbx_handle* h, double* A, int64_t n) {
 }
 
 }  // namespace cbx
+
+extern "C" int cbx_reml_gradient(cbx_handle* h, double var_u, double var_e, int32_t nprobe, int32_t seed,
+                                 int32_t exact_trace, int32_t precision, double pcg_tol, int32_t pcg_maxit,
+                                 double* grad, double* trace, int64_t* pcg_iters) {
+  return cbx_guard(h, [&] {
+    CBX_REQUIRE(h->mme, CBX_ERR_STATE, "call cbx_mme_create and cbx_mme_set_qinv_* first");
+    CBX_REQUIRE(var_u > 0 && var_e > 0 && grad, CBX_ERR_ARG, "variances must be positive");
+    CBX_CUDA(cudaSetDevice(h->device));
+    cbx::reml_gradient(h, var_u, var_e, nprobe, seed, exact_trace, precision, pcg_tol, pcg_maxit, grad, trace,
+                       pcg_iters);
+  });
+}
+
+// REML log-likelihood by dense factorization (small problems; dense Qinv).
+extern "C" int cbx_reml_logl_dense(cbx_handle* h, double var_u, double var_e, double* logL) {
+  return cbx_guard(h, [&] {
+    CBX_REQUIRE(h->mme && logL, CBX_ERR_STATE, "call cbx_mme_create and cbx_mme_set_qinv_dense first");
+    CBX_CUDA(cudaSetDevice(h->device));
+    cbx::DenseExact& D = cbx::dense_state(h);
+    if (!D.init || D.n != h->mme->n_rec || D.dim != h->mme->dim) cbx::dense_init(h, D);
+    cbx::DevBuf<double> C, sol;
+    *logL = cbx::dense_logL(h, D, var_u, var_e, C, sol);
+  });
+}
 
 // Eigen-bending inverse of M (n x n); M == NULL uses the device GRM of this
 // handle.  The result stays on the device (cbx_mme_set_qinv_dense(h, NULL, n))

@@ -144,12 +144,42 @@ __device__ __forceinline__ double block_sum_cols(double v, double* red /*[NT]*/)
   return t;
 }
 
+// Fixed-effect rows of W'W can hold one entry per record (the mean holds all of
+// them).  They are cut into segments of at most FIX_SEG entries; k_fix_seg
+// computes one partial sum per (segment, column) and k_spmv adds a row's
+// segment partials in order.
+constexpr int FIX_SEG = 1024;
+
+template <typename T, int S>
+__global__ void __launch_bounds__(NT) k_fix_seg(OpView<T> op, const int32_t* __restrict__ seg_row,
+                                                const int32_t* __restrict__ seg_lo, const int32_t* __restrict__ seg_hi,
+                                                const T* __restrict__ X, T* __restrict__ seg_part,
+                                                const int* __restrict__ active) {
+  if (active && *active == 0) return;
+  __shared__ T redT[NT];
+  const int sg = blockIdx.x;
+  constexpr int G = NT / S;
+  const int tid = threadIdx.x, c = tid % S, g = tid / S;
+  T acc = T(0);
+  for (int32_t j = seg_lo[sg] + g; j < seg_hi[sg]; j += G) acc += op.Dval[j] * X[(int64_t)op.Dcol[j] * S + c];
+  redT[tid] = acc;
+  __syncthreads();
+  if (tid < S) {
+    T s = T(0);
+    for (int gg = 0; gg < G; ++gg) s += redT[gg * S + tid];
+    seg_part[(int64_t)sg * S + tid] = s;
+  }
+  (void)seg_row;
+}
+
 // Y = use_D * D X + lam * [0; Qs X_u + scatter(Tout)]; optional pq partials sum_i P[i]Y[i].
 // Blocks [0, nfix) take fixed-effect rows (one block per row); the others take
 // random-effect rows, one warp per row, in a grid-stride loop.
 template <typename T, int S>
 __global__ void __launch_bounds__(NT) k_spmv(OpView<T> op, const T* __restrict__ X,
-                                             const T* __restrict__ Tout, int tsplit, T lam, int use_D,
+                                             const T* __restrict__ Tout, int tsplit,
+                                             const int32_t* __restrict__ fix_seg_ptr,
+                                             const T* __restrict__ seg_part, T lam, int use_D,
                                              T* __restrict__ Y, const T* __restrict__ P,
                                              double* __restrict__ pq_part,
                                              const int* __restrict__ active) {
@@ -162,23 +192,13 @@ __global__ void __launch_bounds__(NT) k_spmv(OpView<T> op, const T* __restrict__
   double pq = 0.0;  // this thread's share for column tid % S
   if ((int)blockIdx.x < nfix) {
     const int64_t i = blockIdx.x;
-    constexpr int G = NT / S;
-    const int c = tid % S, g = tid / S;
-    T acc = T(0);
-    if (use_D) {
-      for (int32_t j = op.Dptr[i] + g; j < op.Dptr[i + 1]; j += G)
-        acc += op.Dval[j] * X[(int64_t)op.Dcol[j] * S + c];
-    }
-    // reduce over the G groups of this column
-    redT[tid] = acc;
-    __syncthreads();
     if (tid < S) {
       T s = T(0);
-      for (int gg = 0; gg < G; ++gg) s += redT[gg * S + tid];
+      if (use_D)
+        for (int32_t k = fix_seg_ptr[i]; k < fix_seg_ptr[i + 1]; ++k) s += seg_part[(int64_t)k * S + tid];
       Y[i * S + tid] = s;
       if (P) pq = (double)P[i * S + tid] * (double)s;
     }
-    __syncthreads();
   } else {
     constexpr int G = 32 / S;
     const int c = lane % S, g = lane / S;
@@ -335,19 +355,42 @@ __global__ void __launch_bounds__(NT) k_pupdate(int64_t dim, const Col* __restri
     P[idx] = Z[idx] + beta * P[idx];
 }
 
+// Sum of part[b * stride + c] over b < nblk for every column c < S, by all
+// threads of the block in a fixed order (deterministic); result in red[c].
+template <int S>
+__device__ __forceinline__ void col_sums(const double* __restrict__ part, int nblk, int64_t stride,
+                                         double* red /*[blockDim]*/) {
+  const int t = threadIdx.x;
+  const int G = blockDim.x / S;
+  const int c = t % S, g = t / S;
+  double v = 0.0;
+  if (g < G)
+    for (int b = g; b < nblk; b += G) v += part[(int64_t)b * stride + c];
+  red[t] = v;
+  __syncthreads();
+  if (t < S) {
+    double a = 0.0;
+    for (int k = 0; k < G; ++k) a += red[k * S + t];
+    red[t] = a;  // safe: red[t] for t < S is only read by thread t itself above
+  }
+  __syncthreads();
+}
+
 // Scalar step after the initial residual: rz, b norm, convergence of x0.
 template <int S>
 __global__ void k_scalar_init(Col* col, int ncols, const double* part, int nblk,
                               const double* rz_fix, int64_t p, int abs_tol, int* active_count) {
+  __shared__ double red[NT];
+  __shared__ double sums[3][S];
+  for (int j = 0; j < 3; ++j) {
+    col_sums<S>(part + (int64_t)j * S, nblk, 3 * S, red);
+    if (threadIdx.x < S) sums[j][threadIdx.x] = red[threadIdx.x];
+    __syncthreads();
+  }
+  col_sums<S>(rz_fix, (int)p, S, red);
   const int c = threadIdx.x;
   if (c < S) {
-    double rr = 0, rz = 0, bb = 0;
-    for (int b = 0; b < nblk; ++b) {
-      rr += part[((int64_t)b * 3 + 0) * S + c];
-      rz += part[((int64_t)b * 3 + 1) * S + c];
-      bb += part[((int64_t)b * 3 + 2) * S + c];
-    }
-    for (int64_t f = 0; f < p; ++f) rz += rz_fix[f * S + c];
+    const double rr = sums[0][c], rz = sums[1][c] + (p > 0 ? red[c] : 0.0), bb = sums[2][c];
     Col s{};
     s.rz = rz;
     s.rr = rr;
@@ -370,13 +413,14 @@ __global__ void k_scalar_init(Col* col, int ncols, const double* part, int nblk,
 // alpha = rz / p'Ap, breakdown handling (pcg_solver.h:482-498).
 template <int S>
 __global__ void k_scalar_alpha(Col* col, const double* pq_part, int nblk) {
+  __shared__ double red[NT];
+  col_sums<S>(pq_part, nblk, S, red);
   const int c = threadIdx.x;
   if (c >= S) return;
   Col s = col[c];
   s.skip = 0;
   if (s.active) {
-    double pq = 0;
-    for (int b = 0; b < nblk; ++b) pq += pq_part[(int64_t)b * S + c];
+    const double pq = red[c];
     s.pq = pq;
     if (fabs(pq) < 1e-300) {
       if (!s.restarted) {
@@ -398,16 +442,20 @@ template <int S>
 __global__ void k_scalar_beta(Col* col, const double* part, int nblk, const double* rz_fix,
                               int64_t p, const double* tol_col, int abs_tol, int maxit,
                               int* active_count) {
+  __shared__ double red[NT];
+  __shared__ double sums[3][S];
+  for (int j = 0; j < 2; ++j) {
+    col_sums<S>(part + (int64_t)j * S, nblk, 2 * S, red);
+    if (threadIdx.x < S) sums[j][threadIdx.x] = red[threadIdx.x];
+    __syncthreads();
+  }
+  col_sums<S>(rz_fix, (int)p, S, red);
   const int c = threadIdx.x;
   if (c < S) {
     Col s = col[c];
     if (s.active) {
-      double rr = 0, rz = 0;
-      for (int b = 0; b < nblk; ++b) {
-        rr += part[((int64_t)b * 2 + 0) * S + c];
-        rz += part[((int64_t)b * 2 + 1) * S + c];
-      }
-      for (int64_t f = 0; f < p; ++f) rz += rz_fix[f * S + c];
+      const double rr = sums[0][c];
+      const double rz = sums[1][c] + (p > 0 ? red[c] : 0.0);
       s.rr = rr;
       if (s.skip) {
         s.beta = 0.0;

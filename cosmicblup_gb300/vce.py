@@ -102,3 +102,22 @@ def invert_psd(handle: Handle, M=None, n: int | None = None, ridge: float = 0.0,
     out = np.empty((n, n), dtype=np.float64) if download else None
     handle.check(lib().cbx_invert_psd(handle.raw, ptr(M), int(n), float(ridge), ptr(out)))
     return out
+
+
+def reml_gradient(mme: DeviceMME, var_u: float, var_e: float, nprobe: int = 256, seed: int = 42,
+                  exact: bool = False, precision: int = 0, pcg_tol: float = 1e-10,
+                  pcg_maxit: int = 10000) -> dict:
+    """d logL / d(var_u, var_e) (the reference's AI-REML score) -- cbx_reml_gradient."""
+    g = np.zeros(2)
+    tr = C.c_double(0)
+    it = C.c_int64(0)
+    mme.h.check(lib().cbx_reml_gradient(mme.h.raw, float(var_u), float(var_e), int(nprobe), int(seed),
+                                        1 if exact else 0, int(precision), float(pcg_tol), int(pcg_maxit),
+                                        ptr(g), C.byref(tr), C.byref(it)))
+    return {"grad": g, "trace": tr.value, "pcg_iters": it.value}
+
+
+def reml_logl_dense(mme: DeviceMME, var_u: float, var_e: float) -> float:
+    out = C.c_double(0)
+    mme.h.check(lib().cbx_reml_logl_dense(mme.h.raw, float(var_u), float(var_e), C.byref(out)))
+    return out.value

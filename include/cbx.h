@@ -189,6 +189,23 @@ int cbx_reml_solve(cbx_handle* h, const cbx_reml_config* cfg, double* var_u, dou
                    int32_t* iterations, int32_t* converged, double* solution,
                    cbx_reml_iter_info* history);
 
+/* ---- REML gradient (backward entry) --------------------------------------
+ * d logL / d (var_u, var_e) in grad[2], as the data-driven AI-REML score of
+ * run_aireml_step (src/core/vce.cpp:2648-2675):
+ *   grad_u = (u'Qinv u + var_e tr - q var_u) / (2 var_u^2)
+ *   grad_e = (e'e - var_e (n - p - q + lambda tr)) / (2 var_e^2)
+ * tr = tr(Qinv C^uu) is estimated from nprobe Rademacher probes (the
+ * reference's stream: batches of 16 from mt19937_64(seed + done)) solved as
+ * multi-RHS blocks together with the data solve, or computed exactly from the
+ * q unit vectors when exact_trace != 0.  precision as cbx_pcg_solve.
+ * trace / pcg_iters may be NULL. */
+int cbx_reml_gradient(cbx_handle* h, double var_u, double var_e, int32_t nprobe, int32_t seed,
+                      int32_t exact_trace, int32_t precision, double pcg_tol, int32_t pcg_maxit,
+                      double* grad, double* trace, int64_t* pcg_iters);
+/* REML log-likelihood of run_dense_exact_step's compute_logL (src/core/vce.cpp:
+ * 2974-3007) by dense Cholesky of the LHS: small problems with a dense Qinv. */
+int cbx_reml_logl_dense(cbx_handle* h, double var_u, double var_e, double* logL);
+
 #ifdef __cplusplus
 }
 #endif
