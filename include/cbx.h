@@ -206,6 +206,19 @@ int cbx_reml_gradient(cbx_handle* h, double var_u, double var_e, int32_t nprobe,
  * 2974-3007) by dense Cholesky of the LHS: small problems with a dense Qinv. */
 int cbx_reml_logl_dense(cbx_handle* h, double var_u, double var_e, double* logL);
 
+/* ---- Dense Qinv product without device allocation -------------------------
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory while they run (code under CUDA stream capture, where cudaMalloc is
+ * not allowed; hosts that own the device memory pool; latency-critical loops):
+ * Y = Qd X for the dense Qinv of the handle's MME (cbx_mme_set_qinv_dense), X
+ * and Y column-major q x nrhs DEVICE arrays.  Every intermediate lives in one
+ * static 32 MiB device array (resident on each GPU that loads the library):
+ * q is limited to about 65,000 (CBX_ERR_ARG beyond).  The first call on a
+ * device resolves that array's address and should come before any stream
+ * capture; calls that overlap on the GPU share the array and race.  Runs on the
+ * handle's stream; the result equals cbx_qinv_apply's. */
+int cbx_dense_apply_noalloc(cbx_handle* h, int32_t nrhs, const double* X_dev, double* Y_dev);
+
 #ifdef __cplusplus
 }
 #endif
