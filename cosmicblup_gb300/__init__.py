@@ -7,9 +7,10 @@ reference interfaces used by tests and benchmarks.
 from ._lib import CbxError, Handle, lib  # noqa: F401
 from .grm import GrmBuilder, GrmOptions, PlinkReader, bed_snp_counts  # noqa: F401
 from .mme import DeviceMME  # noqa: F401
-from .vce import AIREML, RemlConfig, invert_psd  # noqa: F401
+from .vce import AIREML, RemlConfig, final_solve, invert_psd, reml_gradient, reml_logl_dense  # noqa: F401
 from .ped import ainv_henderson, ssgblup_qinv  # noqa: F401
 
 __all__ = ["CbxError", "Handle", "lib", "GrmBuilder", "GrmOptions", "PlinkReader",
-           "bed_snp_counts", "DeviceMME", "AIREML", "RemlConfig", "invert_psd",
+           "bed_snp_counts", "DeviceMME", "AIREML", "RemlConfig", "final_solve", "invert_psd",
+           "reml_gradient", "reml_logl_dense",
            "ainv_henderson", "ssgblup_qinv"]

@@ -65,6 +65,8 @@ SIGNATURES = [
     ("cbx_ssgblup_qinv", C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p,
                                    C.c_void_p, C.c_double, C.c_int32, C.c_double, C.c_double, C.c_double,
                                    C.c_void_p, C.c_void_p]),
+    ("cbx_final_solve", C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_int32, C.c_double, C.c_int32,
+                                  C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("cbx_reml_gradient", C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_int32, C.c_int32, C.c_int32,
                                     C.c_int32, C.c_double, C.c_int32, C.c_void_p, C.POINTER(C.c_double),
                                     C.POINTER(C.c_int64)]),

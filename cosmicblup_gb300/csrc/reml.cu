@@ -19,50 +19,12 @@
 #include <vector>
 #include <cublas_v2.h>
 #include <cusolverDn.h>
+#include "dense.h"
 #include "handle.h"
 #include "pcg.h"
 #include "solver.cuh"
 
 namespace cbx {
-
-#define CBX_SOLVER(call)                                                          \
-  do {                                                                            \
-    cusolverStatus_t st_ = (call);                                                \
-    if (st_ != CUSOLVER_STATUS_SUCCESS)                                           \
-      throw Error(CBX_ERR_CUDA, std::string(#call) + " failed: " + std::to_string((int)st_)); \
-  } while (0)
-#define CBX_BLAS(call)                                                            \
-  do {                                                                            \
-    cublasStatus_t st_ = (call);                                                  \
-    if (st_ != CUBLAS_STATUS_SUCCESS)                                             \
-      throw Error(CBX_ERR_CUDA, std::string(#call) + " failed: " + std::to_string((int)st_)); \
-  } while (0)
-
-static inline unsigned gridn(int64_t n, int threads, int cap) {
-  int64_t g = (n + threads - 1) / threads;
-  return (unsigned)std::max<int64_t>(1, std::min<int64_t>(g, cap));
-}
-
-// Library handles owned by a cbx_handle (created on first use).
-struct Libs {
-  cusolverDnHandle_t sol = nullptr;
-  cublasHandle_t blas = nullptr;
-  ~Libs() {
-    if (sol) cusolverDnDestroy(sol);
-    if (blas) cublasDestroy(blas);
-  }
-};
-static Libs& libs(cbx_handle* h) {
-  if (!h->libs_slot) {
-    auto l = std::make_shared<Libs>();
-    CBX_SOLVER(cusolverDnCreate(&l->sol));
-    CBX_SOLVER(cusolverDnSetStream(l->sol, h->stream));
-    CBX_BLAS(cublasCreate(&l->blas));
-    CBX_BLAS(cublasSetStream(l->blas, h->stream));
-    h->libs_slot = l;
-  }
-  return *static_cast<Libs*>(h->libs_slot.get());
-}
 
 // ---------------------------------------------------------------------------
 // kernels of the dense paths (column-major matrices)
@@ -177,35 +139,6 @@ __global__ void k_log_diag_sum(const double* __restrict__ L, int64_t n, double* 
   if (threadIdx.x == 0) part[blockIdx.x] = t;
 }
 
-template <typename T>
-static std::vector<T> d2h(cbx_handle* h, const T* d, size_t n) {
-  std::vector<T> v(n);
-  CBX_CUDA(cudaMemcpyAsync(v.data(), d, n * sizeof(T), cudaMemcpyDeviceToHost, h->stream));
-  CBX_CUDA(cudaStreamSynchronize(h->stream));
-  return v;
-}
-
-// Cholesky of a column-major SPD matrix in place; returns false if not PD.
-static bool potrf(cbx_handle* h, double* A, int64_t n) {
-  Libs& L = libs(h);
-  int lw = 0;
-  CBX_SOLVER(cusolverDnDpotrf_bufferSize(L.sol, CUBLAS_FILL_MODE_LOWER, (int)n, A, (int)n, &lw));
-  DevBuf<double> work;
-  work.resize(std::max(lw, 1));
-  DevBuf<int> info;
-  info.resize(1);
-  CBX_SOLVER(cusolverDnDpotrf(L.sol, CUBLAS_FILL_MODE_LOWER, (int)n, A, (int)n, work.p, lw, info.p));
-  int hi = 0;
-  CBX_CUDA(cudaMemcpyAsync(&hi, info.p, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
-  CBX_CUDA(cudaStreamSynchronize(h->stream));
-  return hi == 0;
-}
-static void potrs(cbx_handle* h, const double* Lf, int64_t n, double* B, int64_t nrhs) {
-  Libs& L = libs(h);
-  DevBuf<int> info;
-  info.resize(1);
-  CBX_SOLVER(cusolverDnDpotrs(L.sol, CUBLAS_FILL_MODE_LOWER, (int)n, (int)nrhs, Lf, (int)n, B, (int)n, info.p));
-}
 // sum_i log L_ii of a Cholesky factor; NaN if a pivot is not positive
 static double log_diag(cbx_handle* h, const double* Lf, int64_t n) {
   const unsigned g = gridn(n, 256, 256);
@@ -845,6 +778,78 @@ extern "C" int cbx_reml_logl_dense(cbx_handle* h, double var_u, double var_e, do
     if (!D.init || D.n != h->mme->n_rec || D.dim != h->mme->dim) cbx::dense_init(h, D);
     cbx::DevBuf<double> C, sol;
     *logL = cbx::dense_logL(h, D, var_u, var_e, C, sol);
+  });
+}
+
+// Final MME solve and fixed-effect standard errors (GSSolve::solve,
+// src/solve/mixed_model_solver.cpp:37-420): lambda = var_e / var_u (0 when
+// var_u <= 1e-9); sol = C^-1 W'y; beta_se_i = sqrt(max(0, var_e (C^-1)_ii)),
+// Cinv_beta = (C^-1)[0:p, 0:p] from p unit right-hand sides.
+// solver 0: dense Cholesky when the Qinv is dense and dim < 10000 (the
+// reference's direct LDLT), else as 1; 1: PCG with relative tolerance;
+// 2: PCG with absolute tolerance warm-started from the last REML data solve
+// (the matrix-free path of GSSolve, mixed_model_solver.cpp:239-256).
+extern "C" int cbx_final_solve(cbx_handle* h, double var_u, double var_e, int32_t solver, double tol,
+                               int32_t maxit, int32_t precision, int32_t calc_se, double* sol, double* beta_se,
+                               double* Cinv_beta) {
+  return cbx_guard(h, [&] {
+    CBX_REQUIRE(h->mme, CBX_ERR_STATE, "call cbx_mme_create and cbx_mme_set_qinv_* first");
+    CBX_REQUIRE(sol && var_e > 0, CBX_ERR_ARG, "bad arguments");
+    CBX_CUDA(cudaSetDevice(h->device));
+    cbx::Mme& m = *h->mme;
+    cudaStream_t s = h->stream;
+    const int64_t p = m.p, dim = m.dim;
+    const double lam = var_u > 1e-9 ? var_e / var_u : 0.0;
+    const bool dense = solver == 0 && m.has_dense && !m.has_sparse && dim < 10000;
+    cbx::DevBuf<double> x;
+    x.resize(dim);
+    std::vector<double> Ci((size_t)p * p, 0.0);
+    if (dense) {
+      cbx::DevBuf<double> C;
+      CBX_REQUIRE(cbx::factor_lhs(h, lam, C), CBX_ERR_FACTOR, "Direct Solver Decomposition Failed");
+      CBX_CUDA(cudaMemcpyAsync(x.p, m.rhs.p, dim * sizeof(double), cudaMemcpyDeviceToDevice, s));
+      cbx::potrs(h, C.p, dim, x.p, 1);
+      if (calc_se && p > 0) {
+        std::vector<double> E((size_t)dim * p, 0.0);
+        for (int64_t i = 0; i < p; ++i) E[(size_t)i * dim + i] = 1.0;
+        cbx::DevBuf<double> Ed;
+        Ed.resize(E.size());
+        CBX_CUDA(cudaMemcpyAsync(Ed.p, E.data(), E.size() * sizeof(double), cudaMemcpyHostToDevice, s));
+        cbx::potrs(h, C.p, dim, Ed.p, p);
+        std::vector<double> Eh = cbx::d2h(h, Ed.p, E.size());
+        for (int64_t i = 0; i < p; ++i)
+          for (int64_t j = 0; j < p; ++j) Ci[(size_t)i * p + j] = Eh[(size_t)i * dim + j];
+      }
+    } else {
+      const bool abs_mode = solver == 2;
+      const bool warm = abs_mode && m.has_last;
+      if (warm) CBX_CUDA(cudaMemcpyAsync(x.p, m.last_solution.p, dim * sizeof(double), cudaMemcpyDeviceToDevice, s));
+      cbx::PcgResult r;
+      cbx::pcg_solve(h, lam, 1, m.rhs.p, x.p, warm, tol, maxit, abs_mode ? 1 : 0, precision, r);
+      if (r.status[0] == cbx::sv::COL_NONFINITE) throw cbx::Error(CBX_ERR_NONFINITE, "non-finite final solve");
+      if (calc_se && p > 0) {
+        std::vector<double> E((size_t)dim * p, 0.0);
+        for (int64_t i = 0; i < p; ++i) E[(size_t)i * dim + i] = 1.0;
+        cbx::DevBuf<double> Ed, Xd;
+        Ed.resize(E.size());
+        Xd.resize(E.size());
+        CBX_CUDA(cudaMemcpyAsync(Ed.p, E.data(), E.size() * sizeof(double), cudaMemcpyHostToDevice, s));
+        cbx::PcgResult re;
+        cbx::pcg_solve(h, lam, (int)p, Ed.p, Xd.p, false, tol, maxit, abs_mode ? 1 : 0, precision, re);
+        std::vector<double> Xh = cbx::d2h(h, Xd.p, E.size());
+        for (int64_t i = 0; i < p; ++i)
+          for (int64_t j = 0; j < p; ++j) Ci[(size_t)i * p + j] = Xh[(size_t)i * dim + j];
+      }
+    }
+    CBX_CUDA(cudaMemcpyAsync(sol, x.p, dim * sizeof(double), cudaMemcpyDeviceToHost, s));
+    CBX_CUDA(cudaStreamSynchronize(s));
+    if (calc_se) {
+      for (int64_t i = 0; i < p; ++i) {
+        if (beta_se) beta_se[i] = std::sqrt(std::max(0.0, var_e * Ci[(size_t)i * p + i]));
+        if (Cinv_beta)
+          for (int64_t j = 0; j < p; ++j) Cinv_beta[(size_t)i * p + j] = Ci[(size_t)i * p + j];
+      }
+    }
   });
 }
 

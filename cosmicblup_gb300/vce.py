@@ -121,3 +121,14 @@ def reml_logl_dense(mme: DeviceMME, var_u: float, var_e: float) -> float:
     out = C.c_double(0)
     mme.h.check(lib().cbx_reml_logl_dense(mme.h.raw, float(var_u), float(var_e), C.byref(out)))
     return out.value
+
+
+def final_solve(mme: DeviceMME, var_u: float, var_e: float, solver: int = 0, tol: float = 1e-10,
+                maxit: int = 10000, precision: int = 0, calc_se: bool = True) -> dict:
+    """GSSolve::solve: BLUE / BLUP solution and fixed-effect SEs (cbx_final_solve)."""
+    sol = np.zeros(mme.dim)
+    se = np.zeros(mme.p)
+    ci = np.zeros((mme.p, mme.p))
+    mme.h.check(lib().cbx_final_solve(mme.h.raw, float(var_u), float(var_e), int(solver), float(tol), int(maxit),
+                                      int(precision), 1 if calc_se else 0, ptr(sol), ptr(se), ptr(ci)))
+    return {"beta": sol[:mme.p], "u": sol[mme.p:], "sol": sol, "beta_se": se, "Cinv_beta": ci}

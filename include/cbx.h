@@ -146,6 +146,28 @@ int cbx_timer_stop(cbx_handle* h, double* ms);
  * cbx_mme_set_qinv_dense(h, NULL, n)); Minv (host, n x n) may be NULL. */
 int cbx_invert_psd(cbx_handle* h, const double* M, int64_t n, double ridge, double* Minv);
 
+/* ---- Pedigree: Henderson A^-1 and the ssGBLUP H^-1 blocks ----------------
+ * cbx_ainv_henderson replaces genmatrix::ml + the Henderson A^-1 assembly
+ * (src/core/a_matrix.cpp:127-186, 392-439): dam / sire are 0-based parent
+ * indices (-1 or out of range = unknown).  Call with ptr == NULL to get *nnz,
+ * then with ptr (n + 1), col / val (nnz) to receive the upper+lower CSR of A^-1.
+ * F (inbreeding) and dii_out (Mendelian sampling variances) may be NULL. */
+int cbx_ainv_henderson(cbx_handle* h, int64_t n, const int64_t* dam, const int64_t* sire,
+                       int64_t* nnz, int64_t* ptr, int32_t* col, double* val, double* F,
+                       double* dii_out);
+
+/* cbx_ssgblup_qinv replaces MatrixBuilder's H^-1 path (src/io/
+ * relationship_builder.cpp:495-584): A22 = rows/columns gmap of A (by the
+ * T D T' recursion over generations on the device; parents must precede
+ * progeny), optional tuneG (tune_g != 0), Gb = (1 - alpha) G* + alpha A22,
+ * Gd = tau Gb^-1 (eigen-bending) - omega A22^-1, and installs
+ * Qinv = A^-1 + S Gd S' on the MME (q = n) as cbx_mme_set_qinv_split would.
+ * G == NULL uses the device GRM of this handle (order ng).  A22_out / Gd_out
+ * (ng x ng) may be NULL. */
+int cbx_ssgblup_qinv(cbx_handle* h, int64_t n, const int64_t* dam, const int64_t* sire, int64_t ng,
+                     const int32_t* gmap, const double* G, double alpha, int32_t tune_g, double tau,
+                     double omega, double ridge, double* A22_out, double* Gd_out);
+
 /* ---- AI-REML, one random component ---------------------------------------
  * Mirrors VCEConfig (src/core/vce.h:140-165) with the defaults of Config
  * (src/config/config.h:41-57): ai_maxit 20, vce_tol 1e-4, vce_mc_samples 100,
@@ -188,6 +210,19 @@ int cbx_reml_iterate(cbx_handle* h, const cbx_reml_config* cfg, double* var_u, d
 int cbx_reml_solve(cbx_handle* h, const cbx_reml_config* cfg, double* var_u, double* var_e,
                    int32_t* iterations, int32_t* converged, double* solution,
                    cbx_reml_iter_info* history);
+
+/* ---- Final MME solve and fixed-effect standard errors ---------------------
+ * Replaces GSSolve::solve (src/solve/mixed_model_solver.cpp:37-420) for one
+ * random component: lambda = var_e / var_u (0 if var_u <= 1e-9), sol (dim) =
+ * C^-1 W'y; with calc_se, beta_se[i] = sqrt(max(0, var_e (C^-1)_ii)) and
+ * Cinv_beta (p x p) from p unit right-hand sides solved as one block.
+ * solver 0: dense Cholesky when Qinv is dense and dim < 10000 (the reference's
+ * direct path), otherwise as 1; 1: PCG, relative tolerance; 2: PCG, absolute
+ * tolerance, warm-started from the last REML data solve (the matrix-free path,
+ * :239-256).  beta_se / Cinv_beta may be NULL. */
+int cbx_final_solve(cbx_handle* h, double var_u, double var_e, int32_t solver, double tol,
+                    int32_t maxit, int32_t precision, int32_t calc_se, double* sol, double* beta_se,
+                    double* Cinv_beta);
 
 /* ---- REML gradient (backward entry) --------------------------------------
  * d logL / d (var_u, var_e) in grad[2], as the data-driven AI-REML score of
