@@ -166,7 +166,7 @@ def read_work_file():
 
 def read_traffic():
     try:
-        txt = open(os.path.join(ROOT, "profiles", "k_dense_fp32_c2.md")).read()
+        txt = open(os.path.join(ROOT, "profiles", "k_dense_tf32_n8192.md")).read()
         m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", txt)
         return float(m.group(1)) if m else None
     except OSError:
