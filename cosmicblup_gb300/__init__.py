@@ -9,8 +9,9 @@ from .grm import GrmBuilder, GrmOptions, PlinkReader, bed_snp_counts  # noqa: F4
 from .mme import DeviceMME  # noqa: F401
 from .vce import AIREML, RemlConfig, final_solve, invert_psd, reml_gradient, reml_logl_dense  # noqa: F401
 from .ped import ainv_henderson, ssgblup_qinv  # noqa: F401
+from .mt import MvEigenVce, MvOptions, solve_multi_trait  # noqa: F401
 
 __all__ = ["CbxError", "Handle", "lib", "GrmBuilder", "GrmOptions", "PlinkReader",
            "bed_snp_counts", "DeviceMME", "AIREML", "RemlConfig", "final_solve", "invert_psd",
            "reml_gradient", "reml_logl_dense",
-           "ainv_henderson", "ssgblup_qinv"]
+           "ainv_henderson", "ssgblup_qinv", "MvEigenVce", "MvOptions", "solve_multi_trait"]

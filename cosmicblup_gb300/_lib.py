@@ -71,6 +71,11 @@ SIGNATURES = [
                                     C.c_int32, C.c_double, C.c_int32, C.c_void_p, C.POINTER(C.c_double),
                                     C.POINTER(C.c_int64)]),
     ("cbx_reml_logl_dense", C.c_int, [C.c_void_p, C.c_double, C.c_double, C.POINTER(C.c_double)]),
+    ("cbx_mt_vce", C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
+                             C.c_int32, C.c_double, C.c_void_p, C.c_void_p, C.POINTER(C.c_int32),
+                             C.POINTER(C.c_int32)]),
+    ("cbx_mt_solve", C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
+                               C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("cbx_dense_apply_noalloc", C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
     # self-test export (not in the public header)
     ("cbx_selftest_umma", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),

@@ -140,3 +140,27 @@ def simulate_pedigree(n_gen: int, per_gen: int, n_sires: int, n_dams: int, seed:
         sire[lo:lo + per_gen] = s
         dam[lo:lo + per_gen] = d
     return sire, dam
+
+
+def simulate_mt_records(bed: bytes, n: int, m: int, seed: int, Vg: np.ndarray, Ve: np.ndarray,
+                        n_levels: int = 2) -> dict:
+    """Multi-trait records y_i = mu + level effect + g_i + e_i (one row per animal).
+
+    g = [g_1 .. g_t] L_g' with g_k independent genetic values of variance 1
+    (Cov(vec g) = Vg (x) G), e_i ~ N(0, Ve); a 2-level class (sex) plus the mean
+    as fixed effects.  Returns Y (n x t) and the dense design X (n x (1 + levels - 1)).
+    """
+    Vg, Ve = np.asarray(Vg, dtype=np.float64), np.asarray(Ve, dtype=np.float64)
+    t = Vg.shape[0]
+    rng = np.random.default_rng(seed)
+    g0 = np.stack([genetic_values(bed, n, m, seed=seed * 1000 + k + 1, var_a=1.0) for k in range(t)], axis=1)
+    g = g0 @ np.linalg.cholesky(Vg).T
+    e = rng.standard_normal((n, t)) @ np.linalg.cholesky(Ve).T
+    lvl = rng.integers(0, n_levels, size=n)
+    eff = rng.normal(0.0, 1.0, size=(n_levels, t))
+    Y = 10.0 + eff[lvl] + g + e
+    X = np.zeros((n, n_levels))
+    X[:, 0] = 1.0
+    for k in range(1, n_levels):
+        X[lvl == k, k] = 1.0
+    return {"Y": Y, "X": X, "level": lvl}

@@ -224,6 +224,31 @@ int cbx_final_solve(cbx_handle* h, double var_u, double var_e, int32_t solver, d
                     int32_t maxit, int32_t precision, int32_t calc_se, double* sol, double* beta_se,
                     double* Cinv_beta);
 
+/* ---- Multi-trait GBLUP ----------------------------------------------------
+ * cbx_mt_vce replaces MvEigenVce (src/core/eigen_vce.cpp:106-266) as GSVce
+ * runs it (src/variance/variance_estimator.cpp:86-325, projection on):
+ * Y (n x t, column-major, complete cases), X (n x p, column-major dense
+ * fixed-effect design), G (n x n) or NULL for G = (G^-1)^-1 from the device
+ * G^-1 of this handle (cbx_invert_psd).  Projection onto null(X'), eigen-
+ * decomposition of the projected G, then EM on Vg / Ve (t x t, row-major)
+ * from Cov(Y)/2 until both relative Frobenius changes are below tol (the
+ * reference uses max_iter = max(500, 25 vce_max_iter), tol = vce_tol).
+ * 1 <= t <= 8, n <= 46,000.  CBX_ERR_FACTOR if some V_i is not positive
+ * definite (the reference throws). */
+int cbx_mt_vce(cbx_handle* h, int64_t n, int32_t t, int64_t p, const double* Y, const double* X,
+               const double* G, int32_t max_iter, double tol, double* Vg, double* Ve,
+               int32_t* iterations, int32_t* converged);
+
+/* cbx_mt_solve replaces GSSolve::solveMultiTrait (src/solve/
+ * mixed_model_solver.cpp:425-524): the explicit Kronecker MME
+ * [Ve^-1 (x) X'X, Ve^-1 (x) X'; Ve^-1 (x) X, Ve^-1 (x) I + Vg^-1 (x) G^-1]
+ * with right-hand side [Ve^-1 (x) X' ; Ve^-1 (x) I] vec(Y), built on the device
+ * and solved by dense Cholesky.  Ginv (n x n) or NULL for the device G^-1.
+ * beta (p t) and u (n t) come back trait-major (index trait * p + effect,
+ * trait * n + animal).  (n + p) t <= 46,000. */
+int cbx_mt_solve(cbx_handle* h, int64_t n, int32_t t, int64_t p, const double* Y, const double* X,
+                 const double* Ginv, const double* Vg, const double* Ve, double* beta, double* u);
+
 /* ---- REML gradient (backward entry) --------------------------------------
  * d logL / d (var_u, var_e) in grad[2], as the data-driven AI-REML score of
  * run_aireml_step (src/core/vce.cpp:2648-2675):
