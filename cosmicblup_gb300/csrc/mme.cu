@@ -64,6 +64,22 @@ __global__ void k_pitch_copy(const double* __restrict__ src, int64_t n, int64_t 
   }
 }
 
+// dst[i * ld + k] = fl32(src - fl32(src)) (k < n), 0 in the padding: the low
+// FP32 part of the float-float copy of the block
+__global__ void k_pitch_lo(const double* __restrict__ src, int64_t n, int64_t ld, float* __restrict__ dst) {
+  const int64_t total = n * ld;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = idx / ld, k = idx - i * ld;
+    if (k < n) {
+      const double v = src[i * n + k];
+      dst[idx] = __double2float_rn(v - (double)__double2float_rn(v));
+    } else {
+      dst[idx] = 0.0f;
+    }
+  }
+}
+
 // column-major (dim x ncols) -> interleaved (dim x S), zero in unused columns
 __global__ void k_to_inter(const double* __restrict__ cm, int64_t dim, int ncols, int S,
                            double* __restrict__ it) {
@@ -104,15 +120,22 @@ __global__ void k_scale_down(const double* __restrict__ r64, const double* __res
     r32[idx] = sc[c] > 0 ? (float)(r64[idx] / sc[c]) : 0.0f;
   }
 }
-// x64 += s_c * d32
-__global__ void k_accumulate(double* __restrict__ x64, const float* __restrict__ d32,
-                             const double* __restrict__ sc, int64_t dim, int S) {
+// Dc = s_c * d32 (0 for columns with s_c = 0); x64 += Dc
+__global__ void k_correction(double* __restrict__ x64, const float* __restrict__ d32,
+                             const double* __restrict__ sc, int64_t dim, int S, double* __restrict__ dc) {
   const int64_t total = dim * S;
   for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
        idx += (int64_t)gridDim.x * blockDim.x) {
     const int c = (int)(idx % S);
-    if (sc[c] > 0) x64[idx] += sc[c] * (double)d32[idx];
+    const double d = sc[c] > 0 ? sc[c] * (double)d32[idx] : 0.0;
+    dc[idx] = d;
+    x64[idx] += d;
   }
+}
+// R -= Y
+__global__ void k_sub_inplace(double* __restrict__ R, const double* __restrict__ Y, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    R[i] -= Y[i];
 }
 // R = B - Y
 __global__ void k_sub(const double* __restrict__ B, const double* __restrict__ Y, int64_t n,
@@ -197,13 +220,58 @@ static bool use_dense_tc() {
   }
   return v == 1;
 }
+// recursive refinement residuals r -= A d with the float-float block product
+// in the mixed solver (CBX_RESID_FF=0 recomputes every r = b - A x in FP64)
+static bool use_resid_ff() {
+  static int v = -1;
+  if (v < 0) {
+    const char* e = std::getenv("CBX_RESID_FF");
+    v = (e && e[0] == '0') ? 0 : 1;
+  }
+  return v == 1;
+}
+
+template <int S>
+constexpr int rpw_ff() {
+  return S >= 32 ? 2 : (S >= 8 ? 4 : 8);
+}
 
 template <typename T, int S>
 void matvec(cbx_handle* h, const sv::OpView<T>& op, Workspace<T, S>& w, const T* X, T* Y, double lam, int use_D,
-            const T* P, double* pq_part, const int* active) {
+            const T* P, double* pq_part, const int* active, bool ff = false) {
   cudaStream_t s = h->stream;
   int tsplit = 1;
-  if (op.Qd && sizeof(T) == 4 && (S == 16 || S == 32) && use_dense_tc()) {
+  if constexpr (sizeof(T) == 8) {
+    ff = ff && op.Qd && h->mme->Qlo32.p && h->mme->Qd32.p;
+  } else {
+    ff = false;
+  }
+  if (ff) {
+    if constexpr (sizeof(T) == 8) {
+      const Mme& mm = *h->mme;
+      sv::k_gather_t<T, S><<<grid_for(S * op.ld, 256, 4 * h->num_sms), 256, 0, s>>>(X, w.Vt.p, op.p, op.ng, op.ld,
+                                                                                 op.gmap, active);
+      h->launched("k_gather_t");
+      constexpr int R = rpw_ff<S>();
+      const int smem = S * 256 * (int)sizeof(float2);
+      CBX_CUDA(cudaFuncSetAttribute(sv::k_dense_ff<S, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+      cbx_handle::ProfRec pr{};
+      if (h->prof_on) {
+        CBX_CUDA(cudaEventCreate(&pr.a));
+        CBX_CUDA(cudaEventCreate(&pr.b));
+        CBX_CUDA(cudaEventRecord(pr.a, s));
+      }
+      sv::k_dense_ff<S, R><<<(unsigned)((op.ng + 8 * R - 1) / (8 * R)), 256, smem, s>>>(
+          mm.Qd32.p, mm.Qlo32.p, op.ng, op.ld, w.Vt.p, w.Tout.p, active);
+      h->launched("k_dense_ff");
+      if (h->prof_on) {
+        CBX_CUDA(cudaEventRecord(pr.b, s));
+        pr.bucket = 1;
+        pr.bytes = 8.0 * ((double)op.ng * op.ld + (double)S * op.ld + (double)op.ng * S);
+        h->prof.push_back(pr);
+      }
+    }
+  } else if (op.Qd && sizeof(T) == 4 && (S == 16 || S == 32) && use_dense_tc()) {
     sv::k_gather_t<T, S><<<grid_for(S * op.ld, 256, 4 * h->num_sms), 256, 0, s>>>(X, w.Vt.p, op.p, op.ng, op.ld,
                                                                                op.gmap, active);
     h->launched("k_gather_t");
@@ -315,7 +383,7 @@ template <int S>
 struct Solver : public SolverBase {
   Workspace<double, S> w64;
   Workspace<float, S> w32;
-  DevBuf<double> dinv64, Bi, Xi, R64, Y64, part, scale;
+  DevBuf<double> dinv64, Bi, Xi, R64, Y64, part, scale, Dc64;
   DevBuf<float> dinv32, R32, D32;
   double dinv_lam = std::nan("");
 
@@ -339,6 +407,7 @@ struct Solver : public SolverBase {
       w32.alloc(m, h->num_sms);
       R32.resize(n);
       D32.resize(n);
+      Dc64.resize(n);
     }
   }
 
@@ -437,10 +506,31 @@ struct Solver : public SolverBase {
       std::vector<sv::Col> cols;
       run_pcg<float, S>(h, m, op32, w32, lam, R32.p, D32.p, ncols, itol.data(), 0, inner_max, false, cols,
                         res.matvecs);
-      k_accumulate<<<grid_for(n, 256, 4 * h->num_sms), 256, 0, s>>>(Xi.p, D32.p, scale.p, m.dim, S);
-      h->launched("k_accumulate");
+      k_correction<<<grid_for(n, 256, 4 * h->num_sms), 256, 0, s>>>(Xi.p, D32.p, scale.p, m.dim, S, Dc64.p);
+      h->launched("k_correction");
       res.refinements += 1;
-      std::vector<double> rn_new = residual(h, m, op64, lam, res.matvecs);
+      // Residual of the new iterate.  A correction that is small next to the
+      // solution (||d|| <= 2^-8 ||x|| in every column) updates it as r -= A d
+      // with the float-float block product: that product's error is bounded
+      // by ~2^-46 |A| |d| <= 2^-54 |A| |x|, below the rounding of an FP64
+      // b - A x.  Otherwise (the first correction from x0 = 0, where d = x)
+      // r = b - A x is recomputed in FP64.
+      bool recursive = use_resid_ff() && m.Qlo32.p;
+      if (recursive) {
+        const std::vector<double> dn = norms(h, m, Dc64.p), xn = norms(h, m, Xi.p);
+        for (int c = 0; c < ncols; ++c)
+          if (sc[c] > 0 && !(dn[c] <= std::ldexp(xn[c], -8))) recursive = false;
+      }
+      std::vector<double> rn_new;
+      if (recursive) {
+        matvec<double, S>(h, op64, w64, Dc64.p, Y64.p, lam, 1, nullptr, nullptr, nullptr, true);
+        ++res.matvecs;
+        k_sub_inplace<<<grid_for(n, 256, 4 * h->num_sms), 256, 0, s>>>(R64.p, Y64.p, n);
+        h->launched("k_sub_inplace");
+        rn_new = norms(h, m, R64.p);
+      } else {
+        rn_new = residual(h, m, op64, lam, res.matvecs);
+      }
       for (int c = 0; c < ncols; ++c) {
         if (sc[c] <= 0) continue;
         res.iters[c] += cols[c].iters;
@@ -807,6 +897,9 @@ extern "C" int cbx_mme_set_qinv_dense(cbx_handle* h, const double* Qinv, int64_t
     h->launched("k_pitch_copy");
     k_pitch_copy<float><<<grid_for(q * m.ld, 256, 8 * h->num_sms), 256, 0, s>>>(src, q, m.ld, m.Qd32.p);
     h->launched("k_pitch_copy");
+    m.Qlo32.resize((size_t)q * m.ld);
+    k_pitch_lo<<<grid_for(q * m.ld, 256, 8 * h->num_sms), 256, 0, s>>>(src, q, m.ld, m.Qlo32.p);
+    h->launched("k_pitch_lo");
     std::vector<int32_t> idm(q);
     for (int64_t i = 0; i < q; ++i) idm[i] = (int32_t)i;
     m.gmap.resize(q);
@@ -870,6 +963,9 @@ extern "C" int cbx_mme_set_qinv_split(cbx_handle* h, const int64_t* a_ptr, const
       h->launched("k_pitch_copy");
       k_pitch_copy<float><<<grid_for(ng * m.ld, 256, 8 * h->num_sms), 256, 0, s>>>(tmp.p, ng, m.ld, m.Qd32.p);
       h->launched("k_pitch_copy");
+      m.Qlo32.resize((size_t)ng * m.ld);
+      k_pitch_lo<<<grid_for(ng * m.ld, 256, 8 * h->num_sms), 256, 0, s>>>(tmp.p, ng, m.ld, m.Qlo32.p);
+      h->launched("k_pitch_lo");
       m.gmap.resize(ng);
       m.ginv.resize(q);
       CBX_CUDA(cudaMemcpyAsync(m.gmap.p, gmap, ng * sizeof(int32_t), cudaMemcpyHostToDevice, s));

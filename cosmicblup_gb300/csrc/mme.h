@@ -47,6 +47,7 @@ struct Mme {
   int64_t ng = 0, ld = 0;          // dense block order and row pitch (multiple of 4)
   DevBuf<double> Qd64;             // ng x ld row-major
   DevBuf<float> Qd32;
+  DevBuf<float> Qlo32;             // fl32(Qd64 - Qd32): with Qd32 the float-float block
   DevBuf<int32_t> gmap;            // ng -> u index
   DevBuf<int32_t> ginv;            // q -> dense index or -1
   Csr<double> Qs64;

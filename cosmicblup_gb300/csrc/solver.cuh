@@ -125,6 +125,129 @@ __global__ void __launch_bounds__(256) k_dense(const T* __restrict__ Qd, int64_t
   }
 }
 
+// ---------------------------------------------------------------------------
+// Float-float ("double-single") block product for the refinement residual.
+//
+// GB300 runs FP64 at 1.25 TFLOP/s, so an FP64 product with 32 right-hand
+// sides is FP64-bound (2 ng^2 S flops).  The residual needs ~46-bit accuracy,
+// not FP64 units: with Qd = Qh + Ql (Qh = fl32(Qd), Ql = fl32(Qd - Qh)) and
+// x = xh + xl likewise, each term is
+//   Qh xh  exactly, as p + e with p = fl(Qh xh), e = fma(Qh, xh, -p),
+//   + Qh xl + Ql xh (FP32, relative 2^-24 of terms that are 2^-24 small),
+// accumulated in an unevaluated (hi, lo) pair by Knuth's two-sum.  Every
+// dropped or rounded part is below 2^-46 of |Qd| |x| per term; the pair is
+// renormalised after each K tile so lo stays below ulp(hi).  All arithmetic is
+// FP32 (the __f*_rn intrinsics keep the compiler from contracting or
+// reassociating the error-free steps).
+__device__ __forceinline__ void ff_acc(float& hi, float& lo, float ah, float al, float bh, float bl) {
+  const float p = __fmul_rn(ah, bh);
+  float e = __fmaf_rn(ah, bh, -p);
+  e = __fmaf_rn(ah, bl, e);
+  e = __fmaf_rn(al, bh, e);
+  const float t = __fadd_rn(hi, p);
+  const float z = __fsub_rn(t, hi);
+  const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(t, z)), __fsub_rn(p, z));
+  hi = t;
+  lo = __fadd_rn(lo, __fadd_rn(err, e));
+}
+// (hi, lo) += (h2, l2)
+__device__ __forceinline__ void ff_add(float& hi, float& lo, float h2, float l2) {
+  const float t = __fadd_rn(hi, h2);
+  const float z = __fsub_rn(t, hi);
+  const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(t, z)), __fsub_rn(h2, z));
+  const float l = __fadd_rn(__fadd_rn(lo, l2), err);
+  hi = __fadd_rn(t, l);
+  lo = __fsub_rn(l, __fsub_rn(hi, t));
+}
+__device__ __forceinline__ void ff_norm(float& hi, float& lo) {
+  const float t = __fadd_rn(hi, lo);
+  lo = __fsub_rn(lo, __fsub_rn(t, hi));
+  hi = t;
+}
+
+// Tout[i * S + c] = sum_k Qd[i][k] Vt[c][k] in float-float; Qh / Ql are the
+// hi / lo FP32 parts of the ng x ld row-major block, Vt the gathered FP64
+// vectors.  8 warps, RPW rows per warp, lanes stream float4s of both parts;
+// the K tile of the S vectors is split into (hi, lo) pairs in shared memory.
+template <int S, int RPW>
+__global__ void __launch_bounds__(256) k_dense_ff(const float* __restrict__ Qh, const float* __restrict__ Ql,
+                                                  int64_t ng, int64_t ld, const double* __restrict__ Vt,
+                                                  double* __restrict__ Tout, const int* __restrict__ active) {
+  if (active && *active == 0) return;
+  constexpr int KT = 32 * 4 * 2;
+  extern __shared__ __align__(16) uint8_t dsm[];
+  float2* vt = reinterpret_cast<float2*>(dsm);  // [S][KT] (hi, lo)
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int64_t row0 = (int64_t)blockIdx.x * (8 * RPW) + warp * RPW;
+  float hi[RPW][S], lo[RPW][S];
+#pragma unroll
+  for (int r = 0; r < RPW; ++r)
+#pragma unroll
+    for (int c = 0; c < S; ++c) hi[r][c] = lo[r][c] = 0.0f;
+  for (int64_t k0 = 0; k0 < ld; k0 += KT) {
+    __syncthreads();
+    for (int v = tid; v < S * KT; v += 256) {
+      const int c = v / KT, kk = v % KT;
+      const double x = (k0 + kk < ld) ? Vt[(int64_t)c * ld + k0 + kk] : 0.0;
+      const float xh = __double2float_rn(x);
+      vt[v] = make_float2(xh, __double2float_rn(x - (double)xh));
+    }
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < KT / 128; ++u) {
+      const int kk = u * 128 + lane * 4;
+      if (k0 + kk < ld) {
+        float4 ah[RPW], al[RPW];
+#pragma unroll
+        for (int r = 0; r < RPW; ++r) {
+          if (row0 + r < ng) {
+            ah[r] = __ldg(reinterpret_cast<const float4*>(Qh + (row0 + r) * ld + k0 + kk));
+            al[r] = __ldg(reinterpret_cast<const float4*>(Ql + (row0 + r) * ld + k0 + kk));
+          } else {
+            ah[r] = make_float4(0.f, 0.f, 0.f, 0.f);
+            al[r] = ah[r];
+          }
+        }
+#pragma unroll
+        for (int c = 0; c < S; ++c) {
+          const float4 b01 = *reinterpret_cast<const float4*>(vt + c * KT + kk);
+          const float4 b23 = *reinterpret_cast<const float4*>(vt + c * KT + kk + 2);
+#pragma unroll
+          for (int r = 0; r < RPW; ++r) {
+            ff_acc(hi[r][c], lo[r][c], ah[r].x, al[r].x, b01.x, b01.y);
+            ff_acc(hi[r][c], lo[r][c], ah[r].y, al[r].y, b01.z, b01.w);
+            ff_acc(hi[r][c], lo[r][c], ah[r].z, al[r].z, b23.x, b23.y);
+            ff_acc(hi[r][c], lo[r][c], ah[r].w, al[r].w, b23.z, b23.w);
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < RPW; ++r)
+#pragma unroll
+      for (int c = 0; c < S; ++c) ff_norm(hi[r][c], lo[r][c]);
+  }
+#pragma unroll
+  for (int r = 0; r < RPW; ++r) {
+#pragma unroll
+    for (int c = 0; c < S; ++c) {
+      float h = hi[r][c], l = lo[r][c];
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {
+        const float h2 = __shfl_xor_sync(0xffffffffu, h, off);
+        const float l2 = __shfl_xor_sync(0xffffffffu, l, off);
+        ff_add(h, l, h2, l2);
+      }
+      hi[r][c] = h;
+      lo[r][c] = l;
+    }
+    if (lane == 0 && row0 + r < ng) {
+#pragma unroll
+      for (int c = 0; c < S; ++c) Tout[(row0 + r) * S + c] = (double)hi[r][c] + (double)lo[r][c];
+    }
+  }
+}
+
 // Block-level sum of one double per thread, grouped by column c = tid % S.
 // Returns the total for column (tid % S) in threads tid < S.
 template <int S>

@@ -112,9 +112,12 @@ int cbx_mme_set_qinv_split(cbx_handle* h, const int64_t* a_ptr, const int32_t* a
  * share each matrix read.  use_x0: X holds the initial guess.
  * tol_mode 0: stop on ||r||/||b|| < tol (recursive residual, the reference);
  * tol_mode 1: stop on ||r|| < tol (MatrixFreePCG, src/core/matrix_free_pcg.h:51).
- * precision 0: FP64 throughout; 1: FP32 PCG bulk with FP64 iterative
- * refinement, stopping on the TRUE FP64 residual.  iters / relres (length
- * nrhs, may be NULL) receive CG iterations and the final relative residual. */
+ * precision 0: FP64 throughout; 1: FP32 PCG bulk with iterative refinement
+ * in FP64, stopping on the true residual b - A x: recomputed in FP64, or,
+ * once a correction d is below 2^-8 of x, updated as r -= A d with a
+ * float-float block product (error below that of an FP64 b - A x).
+ * iters / relres (length nrhs, may be NULL) receive CG iterations and the
+ * final relative residual. */
 int cbx_pcg_solve(cbx_handle* h, double lambda, int32_t nrhs, const double* B, double* X,
                   int32_t use_x0, double tol, int32_t maxit, int32_t tol_mode,
                   int32_t precision, int32_t* iters, double* relres);
