@@ -114,12 +114,12 @@ class ClockSampler:
 
 def build_records(cfg, bed):
     """Phenotypes and the fixed-effect design (mu + contemporary group)."""
+    from cosmicblup_gb300.design import fixed_design
     from cosmicblup_gb300.synth import genetic_values, simulate_gblup_records
-    from oracle.mme import build_fixed_design  # design restatement = data preparation only
     g = genetic_values(bed, cfg["n"], cfg["m"], seed=cfg["seed"] + 2, var_a=cfg["var_a"])
     rec = simulate_gblup_records(cfg["n"], cfg["levels"], g, seed=cfg["seed"] + 3, var_e=cfg["var_e"])
-    p, rows, _ = build_fixed_design(rec["cats"])
-    return rec, p, rows
+    d = fixed_design(rec["cats"])
+    return rec, d.p, d.csr()
 
 
 def cpu_pcg_iteration_cost(WtW, Qd, p, lam, iters: int, seed: int = 0) -> float:
@@ -223,7 +223,7 @@ def run_gpu(args, cfg):
     import ctypes as C
     from cosmicblup_gb300 import AIREML, DeviceMME, Handle, RemlConfig, invert_psd
     from cosmicblup_gb300._lib import lib, ptr
-    from cosmicblup_gb300.mme import FP64, MIXED, rows_to_csr
+    from cosmicblup_gb300.mme import FP64, MIXED
     from cosmicblup_gb300.synth import simulate_bed
     from cosmicblup_gb300.vce import MODE_EM
 
@@ -264,7 +264,7 @@ def run_gpu(args, cfg):
 
     dm = DeviceMME(h, rec["y"], rec["aid"], rows, p, n)
     dm.set_qinv_dense(None)
-    fp, fc, fv = rows_to_csr(rows)
+    fp, fc, fv = rows
     h2d_bytes = rec["y"].nbytes + rec["aid"].nbytes + fp.nbytes + fc.nbytes + fv.nbytes
     d2h_bytes = 8 * (p + n) + 16
 
@@ -327,8 +327,9 @@ def run_gpu(args, cfg):
     # ---- CPU baseline: the oracle's FP64 PCG on this operator, bounded sample ----
     cpu = None
     if rank == 0 and not args.no_cpu_baseline and fp64 is not None:
-        from oracle.mme import sparse_data_part
-        WtW, _ = sparse_data_part(rec["aid"], rows, p, n)
+        from oracle.mme import build_fixed_design, sparse_data_part
+        _, orows, _ = build_fixed_design(rec["cats"])
+        WtW, _ = sparse_data_part(rec["aid"], orows, p, n)
         lam = state[1] / state[0]
         iters = 10 if n >= 10000 else 50
         c = cpu_pcg_iteration_cost(WtW, Ginv_host, p, lam, iters)

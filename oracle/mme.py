@@ -32,6 +32,7 @@ def build_fixed_design(cats, nums=None):
             names.append(f"factor{j + 1}_{k}")
             p += 1
     nnum = len(nums[0]) if (nums is not None and n) else 0
+    names += [f"cov{j + 1}" for j in range(nnum)]
     p += nnum
     rows = []
     for i in range(n):
