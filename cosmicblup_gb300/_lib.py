@@ -79,6 +79,10 @@ SIGNATURES = [
     ("cbx_dense_apply_noalloc", C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
     # self-test export (not in the public header)
     ("cbx_selftest_umma", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("cbx_selftest_dense_ff", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_void_p, C.c_int32,
+                                        C.c_int32, C.c_int32, C.c_void_p, C.POINTER(C.c_double)]),
+    ("cbx_selftest_dense_tc", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_void_p, C.c_int32,
+                                        C.c_void_p]),
 ]
 
 

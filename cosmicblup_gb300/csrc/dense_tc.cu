@@ -1,15 +1,20 @@
 // Dense block product on the tensor cores for the FP32 PCG bulk:
 //   Tpart[ks][i][c] = sum_{k in split ks} Qd[i][k] * Vt[c][k]      (S = 16 or 32 columns)
 // with 3xTF32 splitting (hi*hi + hi*lo + lo*hi, FP32 accumulation in TMEM),
-// which keeps FP32-level accuracy on the tf32 tensor path.
+// which keeps FP32-level accuracy on the tf32 tensor path.  The tf32 MMA reads
+// an FP32 operand as its 19 high bits (the 13 low mantissa bits are dropped),
+// so the staged tiles serve as the hi parts unchanged; the converter warps
+// only write the lo parts (a - hi, exact in FP32).  One MMA with N = 2S
+// forms A_hi [B_hi | B_lo]; a second (N = S) adds A_lo B_hi into the upper
+// half, and the epilogue sums the two halves.
 //
 // This replaces, for probe blocks, the CUDA-core product of DenseMatrixAdapter /
 // SplitMatrixAdapter (reference src/core/matrix_adapter.h:125-127, 252-278)
 // applied to every probe of AdaptiveTraceEstimator.  One persistent CTA per SM
 // walks (128-row tile, K split) work units:
 //   warp 0  TMA producer (SWIZZLE_128B tiles of Qd and Vt),
-//   warp 1  TMEM owner and MMA issuer (kind::tf32, M = 128, N = S),
-//   warps 2-5 split each staged tile into tf32 hi / lo parts in shared memory,
+//   warp 1  TMEM owner and MMA issuer (kind::tf32, M = 128, N = 2S and S),
+//   warps 2-5 write the tf32 lo parts of each staged tile to shared memory,
 //   warps 6-9 epilogue (TMEM -> partial sums in global memory).
 // The K splits are summed in a fixed order by the consumer (k_spmv), so the
 // result is deterministic.
@@ -29,8 +34,11 @@ constexpr int THREADS = 320;
 
 template <int S>
 struct Layout {
-  static constexpr int B_BYTES = S * KB * 4;
-  static constexpr int STAGE = 2 * A_BYTES + 2 * 4096;  // A, A_lo, B, B_lo (B padded to 4 KB)
+  static constexpr int B_BYTES = S * KB * 4;             // S rows of 128 bytes
+  static constexpr int OFF_B = 2 * A_BYTES;              // A, A_lo, then B and B_lo back to back
+  static constexpr int OFF_BL = OFF_B + B_BYTES;         // (B_lo rows continue B's 1024-byte groups)
+  static constexpr int STAGE = 2 * A_BYTES + 2 * B_BYTES;
+  static_assert(STAGE % 1024 == 0, "stages must stay 1024-byte aligned for SWIZZLE_128B");
   static constexpr int OFF_BAR = NSTAGE * STAGE;
   static constexpr int SMEM = OFF_BAR + 256 + 1024;     // + alignment slack
 };
@@ -85,16 +93,15 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
       : "memory");
 }
 
-// hi = a with the 13 low mantissa bits cleared (exact tf32), lo = a - hi (exact in FP32)
-__device__ __forceinline__ void split4(float4& v, float4& lo) {
-  float* p = reinterpret_cast<float*>(&v);
+// lo = a - hi with hi = a's 13 low mantissa bits cleared (the tf32 value the
+// MMA reads); exact in FP32
+__device__ __forceinline__ float4 lo4(const float4& v) {
+  const float* p = reinterpret_cast<const float*>(&v);
+  float4 lo;
   float* q = reinterpret_cast<float*>(&lo);
 #pragma unroll
-  for (int e = 0; e < 4; ++e) {
-    const float hi = __uint_as_float(__float_as_uint(p[e]) & 0xFFFFE000u);
-    q[e] = p[e] - hi;
-    p[e] = hi;
-  }
+  for (int e = 0; e < 4; ++e) q[e] = p[e] - __uint_as_float(__float_as_uint(p[e]) & 0xFFFFE000u);
+  return lo;
 }
 
 template <int S>
@@ -123,7 +130,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 1) {
-    tmem_alloc(&bars->tmem, 64);
+    tmem_alloc(&bars->tmem, 128);  // two accumulator buffers of 64 columns
     tmem_relinquish();
   }
   tc_fence_before();
@@ -149,7 +156,7 @@ __global__ void __launch_bounds__(THREADS, 1)
           uint8_t* st = smem + s * LY::STAGE;
           mbar_expect_tx(&bars->full[s], A_BYTES + LY::B_BYTES);
           tma_load_2d(smem_addr(st), &tmA, k * KB, mt * 128, &bars->full[s]);
-          tma_load_2d(smem_addr(st + 2 * A_BYTES), &tmB, k * KB, 0, &bars->full[s]);
+          tma_load_2d(smem_addr(st + LY::OFF_B), &tmB, k * KB, 0, &bars->full[s]);
         }
       }
       if (!ok) fail();
@@ -157,7 +164,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     __syncwarp();
   } else if (warp == 1) {
     if (lane == 0) {
-      constexpr uint32_t ID = idesc_tf32(128, S);
+      constexpr uint32_t ID2 = idesc_tf32(128, 2 * S), ID1 = idesc_tf32(128, S);
       uint32_t g = 0, c = 0;
       bool ok = true;
       for (int u = blockIdx.x; u < nunits && ok; u += gridDim.x, ++c) {
@@ -166,20 +173,19 @@ __global__ void __launch_bounds__(THREADS, 1)
         const uint32_t b = c & 1;
         if (!mbar_wait(&bars->acc_empty[b], ((c >> 1) & 1) ^ 1, abort_flag)) { ok = false; break; }
         tc_fence_after();
-        const uint32_t d = tmem + b * 32;
+        const uint32_t d = tmem + b * 64;
         for (int k = k0; k < k1; ++k, ++g) {
           const uint32_t s = g % NSTAGE;
           if (!mbar_wait(&bars->conv[s], (g / NSTAGE) & 1, abort_flag)) { ok = false; break; }
           tc_fence_after();
           const uint32_t st = smem_addr(smem + s * LY::STAGE);
           const uint64_t dA = sdesc_sw128(st), dAl = sdesc_sw128(st + A_BYTES);
-          const uint64_t dB = sdesc_sw128(st + 2 * A_BYTES), dBl = sdesc_sw128(st + 2 * A_BYTES + 4096);
+          const uint64_t dB = sdesc_sw128(st + LY::OFF_B);  // N = 2S rows: B_hi then B_lo
 #pragma unroll
           for (int j = 0; j < 4; ++j) {  // four K slices of 8 tf32 (32 bytes) per 128-byte row
             const uint32_t first = (k == k0 && j == 0) ? 0u : 1u;
-            umma_tf32(d, dA + 2 * j, dB + 2 * j, ID, first);
-            umma_tf32(d, dA + 2 * j, dBl + 2 * j, ID, 1u);
-            umma_tf32(d, dAl + 2 * j, dB + 2 * j, ID, 1u);
+            umma_tf32(d, dA + 2 * j, dB + 2 * j, ID2, first);      // [A B_hi | A B_lo]
+            umma_tf32(d + S, dAl + 2 * j, dB + 2 * j, ID1, 1u);    // upper half += A_lo B_hi
           }
           umma_commit(&bars->empty[s]);
         }
@@ -193,7 +199,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     }
     __syncwarp();
   } else if (warp < 6) {
-    // converters: split the staged tiles into tf32 hi (in place) and lo
+    // converters: the tf32 lo parts of the staged tiles
     const int t = tid - 64;
     uint32_t g = 0;
     bool ok = true;
@@ -204,23 +210,13 @@ __global__ void __launch_bounds__(THREADS, 1)
         const uint32_t s = g % NSTAGE;
         if (!mbar_wait(&bars->full[s], (g / NSTAGE) & 1, abort_flag)) { ok = false; break; }
         uint8_t* st = smem + s * LY::STAGE;
-        float4* A = reinterpret_cast<float4*>(st);
+        const float4* A = reinterpret_cast<const float4*>(st);
         float4* Al = reinterpret_cast<float4*>(st + A_BYTES);
-#pragma unroll 4
-        for (int i = t; i < A_BYTES / 16; i += 128) {
-          float4 v = A[i], lo;
-          split4(v, lo);
-          A[i] = v;
-          Al[i] = lo;
-        }
-        float4* B = reinterpret_cast<float4*>(st + 2 * A_BYTES);
-        float4* Bl = reinterpret_cast<float4*>(st + 2 * A_BYTES + 4096);
-        for (int i = t; i < LY::B_BYTES / 16; i += 128) {
-          float4 v = B[i], lo;
-          split4(v, lo);
-          B[i] = v;
-          Bl[i] = lo;
-        }
+#pragma unroll 8
+        for (int i = t; i < A_BYTES / 16; i += 128) Al[i] = lo4(A[i]);
+        const float4* B = reinterpret_cast<const float4*>(st + LY::OFF_B);
+        float4* Bl = reinterpret_cast<float4*>(st + LY::OFF_BL);
+        for (int i = t; i < LY::B_BYTES / 16; i += 128) Bl[i] = lo4(B[i]);
         fence_async_smem();
         mbar_arrive(&bars->conv[s]);
       }
@@ -236,9 +232,23 @@ __global__ void __launch_bounds__(THREADS, 1)
       const uint32_t b = c & 1;
       if (!mbar_wait(&bars->acc_full[b], (c >> 1) & 1, abort_flag)) { ok = false; break; }
       tc_fence_after();
+      // columns [0, S): A B_hi; [S, 2S): A B_lo + A_lo B_hi
       uint32_t r[32];
-      tmem_ld32(tmem + (uint32_t(q * 32) << 16) + b * 32, r);
-      tmem_ld_wait();
+      float out[S];
+      const uint32_t ta = tmem + (uint32_t(q * 32) << 16) + b * 64;
+      if constexpr (S == 32) {
+        uint32_t r2[32];
+        tmem_ld32(ta, r);
+        tmem_ld32(ta + 32, r2);
+        tmem_ld_wait();
+#pragma unroll
+        for (int j = 0; j < 32; ++j) out[j] = __uint_as_float(r[j]) + __uint_as_float(r2[j]);
+      } else {
+        tmem_ld32(ta, r);  // 16 + 16 columns
+        tmem_ld_wait();
+#pragma unroll
+        for (int j = 0; j < 16; ++j) out[j] = __uint_as_float(r[j]) + __uint_as_float(r[16 + j]);
+      }
       tc_fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(&bars->acc_empty[b]);
@@ -247,8 +257,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         float4* dst = reinterpret_cast<float4*>(Tpart + ((int64_t)ks * ng + row) * S);
 #pragma unroll
         for (int j = 0; j < S / 4; ++j)
-          dst[j] = make_float4(__uint_as_float(r[4 * j]), __uint_as_float(r[4 * j + 1]),
-                               __uint_as_float(r[4 * j + 2]), __uint_as_float(r[4 * j + 3]));
+          dst[j] = make_float4(out[4 * j], out[4 * j + 1], out[4 * j + 2], out[4 * j + 3]);
       }
     }
     if (!ok) fail();
@@ -256,7 +265,7 @@ __global__ void __launch_bounds__(THREADS, 1)
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
-  if (warp == 1) tmem_dealloc(tmem, 64);
+  if (warp == 1) tmem_dealloc(tmem, 128);
 }
 
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,

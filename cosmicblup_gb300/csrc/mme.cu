@@ -132,6 +132,11 @@ __global__ void k_correction(double* __restrict__ x64, const float* __restrict__
     x64[idx] += d;
   }
 }
+// R -= a * Y
+__global__ void k_axpy_neg(double* __restrict__ R, const double* __restrict__ Y, double a, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    R[i] -= a * Y[i];
+}
 // R -= Y
 __global__ void k_sub_inplace(double* __restrict__ R, const double* __restrict__ Y, int64_t n) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
@@ -249,9 +254,11 @@ void matvec(cbx_handle* h, const sv::OpView<T>& op, Workspace<T, S>& w, const T*
   if (ff) {
     if constexpr (sizeof(T) == 8) {
       const Mme& mm = *h->mme;
-      sv::k_gather_t<T, S><<<grid_for(S * op.ld, 256, 4 * h->num_sms), 256, 0, s>>>(X, w.Vt.p, op.p, op.ng, op.ld,
-                                                                                 op.gmap, active);
-      h->launched("k_gather_t");
+      // (hi, lo) pairs take the space of the FP64 gather buffer
+      float2* vhl = reinterpret_cast<float2*>(w.Vt.p);
+      sv::k_gather_hl<S><<<grid_for(S * op.ld, 256, 4 * h->num_sms), 256, 0, s>>>(X, vhl, op.p, op.ng, op.ld,
+                                                                                op.gmap);
+      h->launched("k_gather_hl");
       constexpr int R = rpw_ff<S>();
       const int smem = S * 256 * (int)sizeof(float2);
       CBX_CUDA(cudaFuncSetAttribute(sv::k_dense_ff<S, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
@@ -262,7 +269,7 @@ void matvec(cbx_handle* h, const sv::OpView<T>& op, Workspace<T, S>& w, const T*
         CBX_CUDA(cudaEventRecord(pr.a, s));
       }
       sv::k_dense_ff<S, R><<<(unsigned)((op.ng + 8 * R - 1) / (8 * R)), 256, smem, s>>>(
-          mm.Qd32.p, mm.Qlo32.p, op.ng, op.ld, w.Vt.p, w.Tout.p, active);
+          mm.Qd32.p, mm.Qlo32.p, op.ng, op.ld, vhl, w.Tout.p, active);
       h->launched("k_dense_ff");
       if (h->prof_on) {
         CBX_CUDA(cudaEventRecord(pr.b, s));
@@ -288,6 +295,26 @@ void matvec(cbx_handle* h, const sv::OpView<T>& op, Workspace<T, S>& w, const T*
       CBX_CUDA(cudaEventRecord(pr.b, s));
       pr.bucket = 0;
       pr.bytes = 4.0 * ((double)op.ng * op.ld + (double)S * op.ld + (double)op.ng * S * tsplit);
+      h->prof.push_back(pr);
+    }
+  } else if (op.Qd && S == 1) {
+    sv::k_gather_t<T, S><<<grid_for(S * op.ld, 256, 4 * h->num_sms), 256, 0, s>>>(X, w.Vt.p, op.p, op.ng, op.ld,
+                                                                               op.gmap, active);
+    h->launched("k_gather_t");
+    constexpr int R = 4, U = sizeof(T) == 4 ? 4 : 2;
+    cbx_handle::ProfRec pr{};
+    if (h->prof_on) {
+      CBX_CUDA(cudaEventCreate(&pr.a));
+      CBX_CUDA(cudaEventCreate(&pr.b));
+      CBX_CUDA(cudaEventRecord(pr.a, s));
+    }
+    sv::k_gemv<T, R, U><<<(unsigned)((op.ng + 8 * R - 1) / (8 * R)), 256, 0, s>>>(op.Qd, op.ng, op.ld, w.Vt.p,
+                                                                                w.Tout.p, active);
+    h->launched("k_gemv");
+    if (h->prof_on) {
+      CBX_CUDA(cudaEventRecord(pr.b, s));
+      pr.bucket = sizeof(T) == 4 ? 0 : 1;
+      pr.bytes = (double)sizeof(T) * ((double)op.ng * op.ld + (double)op.ld + (double)op.ng);
       h->prof.push_back(pr);
     }
   } else if (op.Qd) {
@@ -439,8 +466,9 @@ struct Solver : public SolverBase {
     return norms(h, m, R64.p);
   }
 
+  // have_r0: R64 holds b - A(lam - dlam) X on entry (see ResidCarry)
   void solve(cbx_handle* h, Mme& m, double lam, int ncols, bool use_x0, double tol, int maxit, int abs_tol,
-             int precision, PcgResult& res) {
+             int precision, PcgResult& res, bool have_r0 = false, double dlam = 0.0) {
     cudaStream_t s = h->stream;
     prepare(h, m, lam, precision != 0);
     auto op64 = make_view<double>(m, dinv64.p);
@@ -478,7 +506,15 @@ struct Solver : public SolverBase {
     if (!use_x0) CBX_CUDA(cudaMemsetAsync(Xi.p, 0, n * sizeof(double), s));
     std::vector<double> bn = norms(h, m, Bi.p);
     std::vector<double> rn;
-    if (use_x0) {
+    if (use_x0 && have_r0 && use_resid_ff() && m.Qlo32.p && std::abs(dlam) <= std::ldexp(lam, -7)) {
+      if (dlam != 0.0) {
+        matvec<double, S>(h, op64, w64, Xi.p, Y64.p, 1.0, 0, nullptr, nullptr, nullptr, true);
+        ++res.matvecs;
+        k_axpy_neg<<<grid_for(n, 256, 4 * h->num_sms), 256, 0, s>>>(R64.p, Y64.p, dlam, n);
+        h->launched("k_axpy_neg");
+      }
+      rn = norms(h, m, R64.p);
+    } else if (use_x0) {
       rn = residual(h, m, op64, lam, res.matvecs);
     } else {
       // x0 = 0: the residual is b itself, no FP64 operator application needed
@@ -569,7 +605,8 @@ static int block_width(int ncols) {
 
 template <int S>
 static void solve_chunk(cbx_handle* h, Mme& m, double lam, int nc, const double* B_cm, double* X_cm, bool use_x0,
-                        double tol, int maxit, int abs_tol, int precision, PcgResult& r) {
+                        double tol, int maxit, int abs_tol, int precision, PcgResult& r, const double* r_prev,
+                        double dlam, double* r_out) {
   Solver<S>& sv_ = solver_for<S>(m);
   sv_.prepare(h, m, lam, precision != 0);
   cudaStream_t s = h->stream;
@@ -580,13 +617,22 @@ static void solve_chunk(cbx_handle* h, Mme& m, double lam, int nc, const double*
     k_to_inter<<<grid_for(n, 256, 4 * h->num_sms), 256, 0, s>>>(X_cm, m.dim, nc, S, sv_.Xi.p);
     h->launched("k_to_inter");
   }
-  sv_.solve(h, m, lam, nc, use_x0, tol, maxit, abs_tol, precision, r);
+  const bool have_r0 = use_x0 && precision != 0 && r_prev;
+  if (have_r0) {
+    k_to_inter<<<grid_for(n, 256, 4 * h->num_sms), 256, 0, s>>>(r_prev, m.dim, nc, S, sv_.R64.p);
+    h->launched("k_to_inter");
+  }
+  sv_.solve(h, m, lam, nc, use_x0, tol, maxit, abs_tol, precision, r, have_r0, dlam);
   k_from_inter<<<grid_for(m.dim * nc, 256, 4 * h->num_sms), 256, 0, s>>>(sv_.Xi.p, m.dim, nc, S, X_cm);
   h->launched("k_from_inter");
+  if (r_out && precision != 0) {
+    k_from_inter<<<grid_for(m.dim * nc, 256, 4 * h->num_sms), 256, 0, s>>>(sv_.R64.p, m.dim, nc, S, r_out);
+    h->launched("k_from_inter");
+  }
 }
 
 void pcg_solve(cbx_handle* h, double lam, int ncols, const double* B_cm, double* X_cm, bool use_x0, double tol,
-               int maxit, int abs_tol, int precision, PcgResult& res) {
+               int maxit, int abs_tol, int precision, PcgResult& res, const ResidCarry* carry) {
   CBX_REQUIRE(h->mme, CBX_ERR_STATE, "no mixed-model equations on this handle (cbx_mme_create)");
   Mme& m = *h->mme;
   CBX_REQUIRE(m.has_dense || m.has_sparse, CBX_ERR_STATE, "Qinv not set (cbx_mme_set_qinv_*)");
@@ -596,14 +642,19 @@ void pcg_solve(cbx_handle* h, double lam, int ncols, const double* B_cm, double*
     PcgResult r;
     const double* B = B_cm + (int64_t)c0 * m.dim;
     double* X = X_cm + (int64_t)c0 * m.dim;
+    const double* rp = carry && carry->r_prev ? carry->r_prev + (int64_t)c0 * m.dim : nullptr;
+    double* ro = carry && carry->r_out ? carry->r_out + (int64_t)c0 * m.dim : nullptr;
+    const double dl = carry ? carry->dlam : 0.0;
+#define CBX_CHUNK(W) solve_chunk<W>(h, m, lam, nc, B, X, use_x0, tol, maxit, abs_tol, precision, r, rp, dl, ro)
     switch (block_width(nc)) {
-      case 1: solve_chunk<1>(h, m, lam, nc, B, X, use_x0, tol, maxit, abs_tol, precision, r); break;
-      case 2: solve_chunk<2>(h, m, lam, nc, B, X, use_x0, tol, maxit, abs_tol, precision, r); break;
-      case 4: solve_chunk<4>(h, m, lam, nc, B, X, use_x0, tol, maxit, abs_tol, precision, r); break;
-      case 8: solve_chunk<8>(h, m, lam, nc, B, X, use_x0, tol, maxit, abs_tol, precision, r); break;
-      case 16: solve_chunk<16>(h, m, lam, nc, B, X, use_x0, tol, maxit, abs_tol, precision, r); break;
-      default: solve_chunk<32>(h, m, lam, nc, B, X, use_x0, tol, maxit, abs_tol, precision, r); break;
+      case 1: CBX_CHUNK(1); break;
+      case 2: CBX_CHUNK(2); break;
+      case 4: CBX_CHUNK(4); break;
+      case 8: CBX_CHUNK(8); break;
+      case 16: CBX_CHUNK(16); break;
+      default: CBX_CHUNK(32); break;
     }
+#undef CBX_CHUNK
     res.iters.insert(res.iters.end(), r.iters.begin(), r.iters.end());
     res.status.insert(res.status.end(), r.status.begin(), r.status.end());
     res.relres.insert(res.relres.end(), r.relres.begin(), r.relres.end());
@@ -912,6 +963,7 @@ extern "C" int cbx_mme_set_qinv_dense(cbx_handle* h, const double* Qinv, int64_t
                                cudaMemcpyDeviceToDevice, s));
     m.has_dense = true;
     m.has_sparse = false;
+    m.drop_carry();
     CBX_CUDA(cudaStreamSynchronize(s));
     for (auto& sp : m.solvers) sp.reset();
   });
@@ -943,6 +995,7 @@ extern "C" int cbx_mme_set_qinv_split(cbx_handle* h, const int64_t* a_ptr, const
     upload_csr<float>(s, q, ptr, col, val, m.Qs32);
     m.has_sparse = true;
     m.has_dense = ng > 0;
+    m.drop_carry();
     if (ng > 0) {
       CBX_REQUIRE(Gd && gmap, CBX_ERR_ARG, "dense block or map missing");
       std::vector<int32_t> inv(q, -1);

@@ -62,6 +62,21 @@ struct Mme {
   // warm start of the data solve (the reference keeps last_solution)
   DevBuf<double> last_solution;
   bool has_last = false;
+  // residual b - A(last_lam) last_solution left by a mixed-precision data solve
+  DevBuf<double> last_resid;
+  bool has_last_resid = false;
+  double last_lam = 0.0;
+  // probe solutions of the previous REML iteration (the probe stream repeats
+  // every iteration), with their residuals and lambda per column
+  DevBuf<double> probe_x, probe_r;
+  std::vector<double> probe_lam;   // per stored column
+  std::vector<char> probe_r_ok;    // residual column valid (mixed-precision solve)
+  int probe_seed = -1;
+  void drop_carry() {
+    has_last = has_last_resid = false;
+    probe_lam.clear();
+    probe_r_ok.clear();
+  }
   // persistent solver workspaces, indexed by log2 of the RHS block width
   std::unique_ptr<SolverBase> solvers[6];
   // scratch column-major buffers of the C ABI

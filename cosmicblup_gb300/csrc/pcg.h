@@ -18,8 +18,22 @@ struct PcgResult {
 // with the reference's relative recursive-residual stop; 1: FP32 PCG on the
 // correction equation with FP64 true-residual refinement (stop on the true
 // residual).  abs_tol: stop on ||r|| < tol (MatrixFreePCG) instead.
+// Residual carried between mixed-precision solves of the same right-hand sides
+// at neighbouring lambdas.  r_prev (column-major dim x ncols) = b - A(lam -
+// dlam) x0 for the x0 passed in X; when |dlam| <= 2^-7 lam the initial
+// residual is formed as r_prev - dlam [0; Qinv x0_u] with the float-float
+// block product (error below that of an FP64 b - A x0), otherwise b - A x0 is
+// recomputed in FP64.  r_out receives the final residual b - A(lam) x of a
+// mixed-precision solve.  Either pointer may be null.
+struct ResidCarry {
+  const double* r_prev = nullptr;
+  double dlam = 0.0;
+  double* r_out = nullptr;
+};
+
 void pcg_solve(cbx_handle* h, double lam, int ncols, const double* B_cm, double* X_cm, bool use_x0,
-               double tol, int maxit, int abs_tol, int precision, PcgResult& res);
+               double tol, int maxit, int abs_tol, int precision, PcgResult& res,
+               const ResidCarry* carry = nullptr);
 
 // Y = Qinv X for ncols column-major q-vectors on the device.
 void qinv_apply(cbx_handle* h, int ncols, const double* X_cm, double* Y_cm);

@@ -216,11 +216,20 @@ static void em_iteration(cbx_handle* h, const RemlConfigI& cfg, double& vu, doub
   const int64_t p = m.p, q = m.q, dim = m.dim, n = m.n_rec;
   const double start_vu = vu, start_ve = ve;
   const double lam = ve / std::max(vu, 1e-9);
-  // 1. data solve, warm-started from the previous data solution
+  // 1. data solve, warm-started from the previous data solution (and, in mixed
+  //    precision, from its residual carried to the new lambda)
   m.last_solution.resize(dim);
+  m.last_resid.resize(dim);
   PcgResult r;
-  pcg_solve(h, lam, 1, m.rhs.p, m.last_solution.p, m.has_last, cfg.pcg_tol, cfg.pcg_max_iter, 0, cfg.precision, r);
+  ResidCarry dc;
+  dc.r_prev = (m.has_last && m.has_last_resid) ? m.last_resid.p : nullptr;
+  dc.dlam = lam - m.last_lam;
+  dc.r_out = m.last_resid.p;
+  pcg_solve(h, lam, 1, m.rhs.p, m.last_solution.p, m.has_last, cfg.pcg_tol, cfg.pcg_max_iter, 0, cfg.precision, r,
+            &dc);
   m.has_last = true;
+  m.has_last_resid = cfg.precision != 0;
+  m.last_lam = lam;
   info.pcg_iters += r.iters[0];
   info.matvecs += r.matvecs;
   if (r.status[0] == sv::COL_NONFINITE) throw Error(CBX_ERR_NONFINITE, "non-finite data solve");
@@ -270,8 +279,46 @@ static void em_iteration(cbx_handle* h, const RemlConfigI& cfg, double& vu, doub
     X.resize((size_t)dim * k);
     QW.resize((size_t)q * k);
     CBX_CUDA(cudaMemcpyAsync(B.p, Bh.data(), Bh.size() * sizeof(double), cudaMemcpyHostToDevice, s));
+    // The probe stream restarts at the same seed every REML iteration, so the
+    // previous iteration's solutions of these probes are a warm start (and,
+    // in mixed precision, their residuals carry to the new lambda when all
+    // columns share one previous lambda).
+    if (m.probe_seed != cfg.seed) {
+      m.probe_lam.clear();
+      m.probe_r_ok.clear();
+      m.probe_seed = cfg.seed;
+    }
+    const size_t cap = (size_t)dim * max_s;
+    if (m.probe_x.n < cap) {
+      m.probe_x.resize(cap);
+      m.probe_r.resize(cap);
+      m.probe_lam.clear();
+      m.probe_r_ok.clear();
+    }
+    const bool warm = (int)m.probe_lam.size() >= done + k;
+    bool carry_ok = warm;
+    if (warm)
+      for (int c = done; c < done + k; ++c)
+        carry_ok = carry_ok && m.probe_r_ok[c] && m.probe_lam[c] == m.probe_lam[done];
+    if (warm)
+      CBX_CUDA(cudaMemcpyAsync(X.p, m.probe_x.p + (size_t)done * dim, (size_t)dim * k * sizeof(double),
+                               cudaMemcpyDeviceToDevice, s));
+    ResidCarry pc;
+    pc.r_prev = carry_ok ? m.probe_r.p + (size_t)done * dim : nullptr;
+    pc.dlam = carry_ok ? lam - m.probe_lam[done] : 0.0;
+    pc.r_out = m.probe_r.p + (size_t)done * dim;
     PcgResult pr;
-    pcg_solve(h, lam, k, B.p, X.p, false, cfg.pcg_tol, cfg.pcg_max_iter, 0, cfg.precision, pr);
+    pcg_solve(h, lam, k, B.p, X.p, warm, cfg.pcg_tol, cfg.pcg_max_iter, 0, cfg.precision, pr, &pc);
+    CBX_CUDA(cudaMemcpyAsync(m.probe_x.p + (size_t)done * dim, X.p, (size_t)dim * k * sizeof(double),
+                             cudaMemcpyDeviceToDevice, s));
+    if ((int)m.probe_lam.size() < done + k) {
+      m.probe_lam.resize(done + k);
+      m.probe_r_ok.resize(done + k);
+    }
+    for (int c = done; c < done + k; ++c) {
+      m.probe_lam[c] = lam;
+      m.probe_r_ok[c] = cfg.precision != 0;
+    }
     for (int c = 0; c < k; ++c) {
       info.pcg_iters += pr.iters[c];
       if (pr.status[c] == sv::COL_NONFINITE) throw Error(CBX_ERR_NONFINITE, "non-finite probe solve");

@@ -3,7 +3,10 @@
 // TMEM read-back of the GRM kernel.  Used by the GPU tests to localise layout
 // errors.  All accesses stay inside one 16 KB shared-memory tile set.
 #include <cuda_fp16.h>
+#include <vector>
+#include "dense_tc.h"
 #include "handle.h"
+#include "solver.cuh"
 
 namespace cbx {
 namespace selftest {
@@ -84,6 +87,112 @@ extern "C" int cbx_selftest_umma(cbx_handle* h, const float* A, const float* B, 
     h->launched("k_umma_probe");
     h->check_status("cbx_selftest_umma");
     CBX_CUDA(cudaMemcpyAsync(D, dD.p, 128 * 32 * 4, cudaMemcpyDeviceToHost, h->stream));
+    CBX_CUDA(cudaStreamSynchronize(h->stream));
+  });
+}
+
+// The tensor-core block product alone: Y (ng x S, row-major) = Q (ng x ld,
+// row-major FP32, ld % 4 == 0) V^T with V (S x ld, row-major FP32), S = 16 or
+// 32, summed over its K splits in order on the host.
+extern "C" int cbx_selftest_dense_tc(cbx_handle* h, const float* Q, int64_t ng, int64_t ld, const float* V,
+                                     int32_t S, float* Y) {
+  return cbx_guard(h, [&] {
+    CBX_REQUIRE(S == 16 || S == 32, CBX_ERR_ARG, "S must be 16 or 32");
+    CBX_REQUIRE(ng > 0 && ld > 0 && ld % 4 == 0, CBX_ERR_ARG, "bad block shape");
+    CBX_CUDA(cudaSetDevice(h->device));
+    cbx::DevBuf<float> dQ, dV, dT;
+    const int ks = cbx::dense_tc_ksplit(ng, ld, h->num_sms);
+    dQ.resize((size_t)ng * ld);
+    dV.resize((size_t)S * ld);
+    dT.resize((size_t)ks * ng * S);
+    CBX_CUDA(cudaMemcpyAsync(dQ.p, Q, (size_t)ng * ld * 4, cudaMemcpyHostToDevice, h->stream));
+    CBX_CUDA(cudaMemcpyAsync(dV.p, V, (size_t)S * ld * 4, cudaMemcpyHostToDevice, h->stream));
+    cbx::dense_tc(h, dQ.p, ng, ld, dV.p, S, ks, dT.p, nullptr);
+    h->check_status("cbx_selftest_dense_tc");
+    std::vector<float> T((size_t)ks * ng * S);
+    CBX_CUDA(cudaMemcpyAsync(T.data(), dT.p, T.size() * 4, cudaMemcpyDeviceToHost, h->stream));
+    CBX_CUDA(cudaStreamSynchronize(h->stream));
+    for (int64_t i = 0; i < ng * S; ++i) {
+      float a = 0.0f;
+      for (int k = 0; k < ks; ++k) a += T[(size_t)k * ng * S + i];
+      Y[i] = a;
+    }
+  });
+}
+
+// The float-float block product alone: Y (ng x S, row-major FP64) = Q V^T with
+// Q (ng x ld, row-major FP64, ld % 4 == 0) held as FP32 hi / lo parts and V
+// (S x ld, row-major FP64).  rpw selects rows per warp (S = 32: 1 or 2; S = 16:
+// 2 or 4; S = 1: 8); reps > 0 also times that many launches (ms_out, mean).
+namespace {
+__global__ void k_split_hilo(const double* __restrict__ q, int64_t n, float* __restrict__ hi,
+                             float* __restrict__ lo) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float h = __double2float_rn(q[i]);
+    hi[i] = h;
+    lo[i] = __double2float_rn(q[i] - (double)h);
+  }
+}
+__global__ void k_split_pairs(const double* __restrict__ v, int64_t n, float2* __restrict__ out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float h = __double2float_rn(v[i]);
+    out[i] = make_float2(h, __double2float_rn(v[i] - (double)h));
+  }
+}
+template <int S, int R>
+void launch_ff(cbx_handle* h, const float* qh, const float* ql, int64_t ng, int64_t ld, const float2* v, double* y) {
+  const int smem = S * 256 * (int)sizeof(float2);
+  CBX_CUDA(cudaFuncSetAttribute(cbx::sv::k_dense_ff<S, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  cbx::sv::k_dense_ff<S, R><<<(unsigned)((ng + 8 * R - 1) / (8 * R)), 256, smem, h->stream>>>(qh, ql, ng, ld, v, y,
+                                                                                             nullptr);
+  h->launched("k_dense_ff");
+}
+}  // namespace
+
+extern "C" int cbx_selftest_dense_ff(cbx_handle* h, const double* Q, int64_t ng, int64_t ld, const double* V,
+                                     int32_t S, int32_t rpw, int32_t reps, double* Y, double* ms_out) {
+  return cbx_guard(h, [&] {
+    CBX_REQUIRE(ng > 0 && ld > 0 && ld % 4 == 0, CBX_ERR_ARG, "bad block shape");
+    CBX_CUDA(cudaSetDevice(h->device));
+    cbx::DevBuf<double> dQ, dV, dY;
+    cbx::DevBuf<float> qh, ql;
+    cbx::DevBuf<float2> vhl;
+    dQ.resize((size_t)ng * ld);
+    dV.resize((size_t)S * ld);
+    dY.resize((size_t)ng * S);
+    qh.resize((size_t)ng * ld);
+    ql.resize((size_t)ng * ld);
+    CBX_CUDA(cudaMemcpyAsync(dQ.p, Q, (size_t)ng * ld * 8, cudaMemcpyHostToDevice, h->stream));
+    CBX_CUDA(cudaMemcpyAsync(dV.p, V, (size_t)S * ld * 8, cudaMemcpyHostToDevice, h->stream));
+    k_split_hilo<<<1024, 256, 0, h->stream>>>(dQ.p, ng * ld, qh.p, ql.p);
+    h->launched("k_split_hilo");
+    vhl.resize((size_t)S * ld);
+    k_split_pairs<<<256, 256, 0, h->stream>>>(dV.p, S * ld, vhl.p);
+    h->launched("k_split_pairs");
+    auto run = [&] {
+      if (S == 32 && rpw == 1) launch_ff<32, 1>(h, qh.p, ql.p, ng, ld, vhl.p, dY.p);
+      else if (S == 32 && rpw == 2) launch_ff<32, 2>(h, qh.p, ql.p, ng, ld, vhl.p, dY.p);
+      else if (S == 16 && rpw == 2) launch_ff<16, 2>(h, qh.p, ql.p, ng, ld, vhl.p, dY.p);
+      else if (S == 16 && rpw == 4) launch_ff<16, 4>(h, qh.p, ql.p, ng, ld, vhl.p, dY.p);
+      else if (S == 1 && rpw == 8) launch_ff<1, 8>(h, qh.p, ql.p, ng, ld, vhl.p, dY.p);
+      else throw cbx::Error(CBX_ERR_ARG, "unsupported (S, rpw)");
+    };
+    run();
+    if (reps > 0) {
+      cudaEvent_t a, b;
+      CBX_CUDA(cudaEventCreate(&a));
+      CBX_CUDA(cudaEventCreate(&b));
+      CBX_CUDA(cudaEventRecord(a, h->stream));
+      for (int i = 0; i < reps; ++i) run();
+      CBX_CUDA(cudaEventRecord(b, h->stream));
+      CBX_CUDA(cudaEventSynchronize(b));
+      float ms = 0;
+      CBX_CUDA(cudaEventElapsedTime(&ms, a, b));
+      if (ms_out) *ms_out = ms / reps;
+      cudaEventDestroy(a);
+      cudaEventDestroy(b);
+    }
+    CBX_CUDA(cudaMemcpyAsync(Y, dY.p, (size_t)ng * S * 8, cudaMemcpyDeviceToHost, h->stream));
     CBX_CUDA(cudaStreamSynchronize(h->stream));
   });
 }

@@ -125,12 +125,65 @@ __global__ void __launch_bounds__(256) k_dense(const T* __restrict__ Qd, int64_t
   }
 }
 
+// Single right-hand side: Tout[i] = sum_k Qd[i * ld + k] v[k].  A pure HBM
+// stream: each warp owns RPW rows and keeps U x (RPW + 1) 16-byte loads in
+// flight per lane; v (ld values) is read through the read-only cache.
+template <typename T, int RPW, int U>
+__global__ void __launch_bounds__(256) k_gemv(const T* __restrict__ Qd, int64_t ng, int64_t ld,
+                                              const T* __restrict__ v, T* __restrict__ Tout,
+                                              const int* __restrict__ active) {
+  if (active && *active == 0) return;
+  using V = typename Vec16<T>::type;
+  constexpr int VEC = Vec16<T>::n;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t row0 = ((int64_t)blockIdx.x * 8 + warp) * RPW;
+  if (row0 >= ng) return;
+  const int64_t nvec = ld / VEC;
+  const V* vv = reinterpret_cast<const V*>(v);
+  const V* rows[RPW];
+#pragma unroll
+  for (int r = 0; r < RPW; ++r)
+    rows[r] = reinterpret_cast<const V*>(Qd + (row0 + r < ng ? row0 + r : row0) * ld);
+  T acc[RPW];
+#pragma unroll
+  for (int r = 0; r < RPW; ++r) acc[r] = T(0);
+  for (int64_t j0 = lane; j0 < nvec; j0 += 32 * U) {
+    V a[U][RPW], b[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int64_t j = j0 + u * 32;
+      if (j < nvec) {
+        b[u] = __ldg(vv + j);
+#pragma unroll
+        for (int r = 0; r < RPW; ++r) a[u][r] = __ldg(rows[r] + j);
+      } else {
+        memset(&b[u], 0, sizeof(V));
+#pragma unroll
+        for (int r = 0; r < RPW; ++r) memset(&a[u][r], 0, sizeof(V));
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+#pragma unroll
+      for (int r = 0; r < RPW; ++r) acc[r] += dot16(a[u][r], b[u]);
+  }
+#pragma unroll
+  for (int r = 0; r < RPW; ++r) {
+    T t = acc[r];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) t += __shfl_xor_sync(0xffffffffu, t, off);
+    if (lane == 0 && row0 + r < ng) Tout[row0 + r] = t;
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Float-float ("double-single") block product for the refinement residual.
 //
 // GB300 runs FP64 at 1.25 TFLOP/s, so an FP64 product with 32 right-hand
-// sides is FP64-bound (2 ng^2 S flops).  The residual needs ~46-bit accuracy,
-// not FP64 units: with Qd = Qh + Ql (Qh = fl32(Qd), Ql = fl32(Qd - Qh)) and
+// sides is FP64-bound (2 ng^2 S flops).  The mixed solver's recursive
+// residual update r -= A d for a correction d that is small next to x needs
+// the product only to ~46 bits, relative to |Qd| |d|: with Qd = Qh + Ql
+// (Qh = fl32(Qd), Ql = fl32(Qd - Qh)) and
 // x = xh + xl likewise, each term is
 //   Qh xh  exactly, as p + e with p = fl(Qh xh), e = fma(Qh, xh, -p),
 //   + Qh xl + Ql xh (FP32, relative 2^-24 of terms that are 2^-24 small),
@@ -165,13 +218,29 @@ __device__ __forceinline__ void ff_norm(float& hi, float& lo) {
   hi = t;
 }
 
-// Tout[i * S + c] = sum_k Qd[i][k] Vt[c][k] in float-float; Qh / Ql are the
-// hi / lo FP32 parts of the ng x ld row-major block, Vt the gathered FP64
-// vectors.  8 warps, RPW rows per warp, lanes stream float4s of both parts;
-// the K tile of the S vectors is split into (hi, lo) pairs in shared memory.
+// Vhl[c * ld + k] = (hi, lo) FP32 parts of X[(p + gmap[k]) * S + c] for k < ng,
+// (0, 0) in the padding: the gathered vectors of the float-float product, split
+// once here so that the product kernel does no FP64 arithmetic.
+template <int S>
+__global__ void k_gather_hl(const double* __restrict__ X, float2* __restrict__ Vhl, int64_t p, int64_t ng,
+                            int64_t ld, const int32_t* __restrict__ gmap) {
+  const int64_t total = (int64_t)S * ld;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = idx / ld, k = idx - c * ld;
+    const double x = k < ng ? X[(p + gmap[k]) * S + c] : 0.0;
+    const float xh = __double2float_rn(x);
+    Vhl[idx] = make_float2(xh, __double2float_rn(x - (double)xh));
+  }
+}
+
+// Tout[i * S + c] = sum_k Qd[i][k] V[c][k] in float-float; Qh / Ql are the
+// hi / lo FP32 parts of the ng x ld row-major block, Vhl the (hi, lo) parts of
+// the gathered vectors.  8 warps, RPW rows per warp, lanes stream float4s of
+// both block parts; the K tile of the S vectors is staged in shared memory.
 template <int S, int RPW>
 __global__ void __launch_bounds__(256) k_dense_ff(const float* __restrict__ Qh, const float* __restrict__ Ql,
-                                                  int64_t ng, int64_t ld, const double* __restrict__ Vt,
+                                                  int64_t ng, int64_t ld, const float2* __restrict__ Vhl,
                                                   double* __restrict__ Tout, const int* __restrict__ active) {
   if (active && *active == 0) return;
   constexpr int KT = 32 * 4 * 2;
@@ -188,9 +257,7 @@ __global__ void __launch_bounds__(256) k_dense_ff(const float* __restrict__ Qh, 
     __syncthreads();
     for (int v = tid; v < S * KT; v += 256) {
       const int c = v / KT, kk = v % KT;
-      const double x = (k0 + kk < ld) ? Vt[(int64_t)c * ld + k0 + kk] : 0.0;
-      const float xh = __double2float_rn(x);
-      vt[v] = make_float2(xh, __double2float_rn(x - (double)xh));
+      vt[v] = (k0 + kk < ld) ? Vhl[(int64_t)c * ld + k0 + kk] : make_float2(0.f, 0.f);
     }
     __syncthreads();
 #pragma unroll
@@ -271,7 +338,7 @@ __device__ __forceinline__ double block_sum_cols(double v, double* red /*[NT]*/)
 // them).  They are cut into segments of at most FIX_SEG entries; k_fix_seg
 // computes one partial sum per (segment, column) and k_spmv adds a row's
 // segment partials in order.
-constexpr int FIX_SEG = 1024;
+constexpr int FIX_SEG = 256;
 
 template <typename T, int S>
 __global__ void __launch_bounds__(NT) k_fix_seg(OpView<T> op, const int32_t* __restrict__ seg_row,
@@ -283,9 +350,15 @@ __global__ void __launch_bounds__(NT) k_fix_seg(OpView<T> op, const int32_t* __r
   const int sg = blockIdx.x;
   constexpr int G = NT / S;
   const int tid = threadIdx.x, c = tid % S, g = tid / S;
-  T acc = T(0);
-  for (int32_t j = seg_lo[sg] + g; j < seg_hi[sg]; j += G) acc += op.Dval[j] * X[(int64_t)op.Dcol[j] * S + c];
-  redT[tid] = acc;
+  T acc[4] = {T(0), T(0), T(0), T(0)};
+  const int32_t hi = seg_hi[sg];
+  int32_t j = seg_lo[sg] + g;
+  for (; j + 3 * G < hi; j += 4 * G) {
+#pragma unroll
+    for (int u = 0; u < 4; ++u) acc[u] += op.Dval[j + u * G] * X[(int64_t)op.Dcol[j + u * G] * S + c];
+  }
+  for (; j < hi; j += G) acc[0] += op.Dval[j] * X[(int64_t)op.Dcol[j] * S + c];
+  redT[tid] = (acc[0] + acc[1]) + (acc[2] + acc[3]);
   __syncthreads();
   if (tid < S) {
     T s = T(0);
@@ -314,13 +387,21 @@ __global__ void __launch_bounds__(NT) k_spmv(OpView<T> op, const T* __restrict__
   const int nfix = (int)p;
   double pq = 0.0;  // this thread's share for column tid % S
   if ((int)blockIdx.x < nfix) {
+    // fixed-effect row: sum its segment partials, NT / S groups in parallel,
+    // groups combined in a fixed order
     const int64_t i = blockIdx.x;
+    constexpr int GS = NT / S;
+    const int c = tid % S, g = tid / S;
+    T s = T(0);
+    if (use_D)
+      for (int32_t k = fix_seg_ptr[i] + g; k < fix_seg_ptr[i + 1]; k += GS) s += seg_part[(int64_t)k * S + c];
+    redT[tid] = s;
+    __syncthreads();
     if (tid < S) {
-      T s = T(0);
-      if (use_D)
-        for (int32_t k = fix_seg_ptr[i]; k < fix_seg_ptr[i + 1]; ++k) s += seg_part[(int64_t)k * S + tid];
-      Y[i * S + tid] = s;
-      if (P) pq = (double)P[i * S + tid] * (double)s;
+      T t = T(0);
+      for (int gg = 0; gg < GS; ++gg) t += redT[gg * S + tid];
+      Y[i * S + tid] = t;
+      if (P) pq = (double)P[i * S + tid] * (double)t;
     }
   } else {
     constexpr int G = 32 / S;
@@ -486,10 +567,18 @@ __device__ __forceinline__ void col_sums(const double* __restrict__ part, int nb
   const int t = threadIdx.x;
   const int G = blockDim.x / S;
   const int c = t % S, g = t / S;
-  double v = 0.0;
-  if (g < G)
-    for (int b = g; b < nblk; b += G) v += part[(int64_t)b * stride + c];
-  red[t] = v;
+  // 8 independent partial sums per thread keep 8 loads in flight; they are
+  // combined in a fixed order, so the total does not depend on timing
+  double v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  if (g < G) {
+    int b = g;
+    for (; b + 7 * G < nblk; b += 8 * G) {
+#pragma unroll
+      for (int u = 0; u < 8; ++u) v[u] += part[(int64_t)(b + u * G) * stride + c];
+    }
+    for (; b < nblk; b += G) v[0] += part[(int64_t)b * stride + c];
+  }
+  red[t] = ((v[0] + v[1]) + (v[2] + v[3])) + ((v[4] + v[5]) + (v[6] + v[7]));
   __syncthreads();
   if (t < S) {
     double a = 0.0;

@@ -173,3 +173,53 @@ def test_mixed_probe_block_tensor_cores(handle, gblup, k):
         true = np.linalg.norm(B[:, c] - A @ X[:, c]) / np.linalg.norm(B[:, c])
         assert true < 1e-10 and rr[c] < 1e-10, (c, true)
         assert rel(X[:, c], Xe[:, c]) < 1e-8, c
+
+
+@pytest.mark.parametrize("S", [16, 32])
+def test_dense_tc_product_accuracy(handle, S):
+    """The tcgen05 3xTF32 block product alone against an FP64 product: its
+    error must be at FP32 level (a few 2^-24 of sum |Q||V| per entry), far
+    below what plain TF32 (2^-11) would give."""
+    from cosmicblup_gb300._lib import lib, ptr
+    rng = np.random.default_rng(70 + S)
+    ng, ld = 1000, 3000
+    Q = rng.standard_normal((ng, ld)).astype(np.float32)
+    Q[:, ::7] *= 1e3                      # wide dynamic range along K
+    V = rng.standard_normal((S, ld)).astype(np.float32)
+    Y = np.zeros((ng, S), dtype=np.float32)
+    handle.check(lib().cbx_selftest_dense_tc(handle.raw, ptr(Q), ng, ld, ptr(V), S, ptr(Y)))
+    exact = Q.astype(np.float64) @ V.astype(np.float64).T
+    scale = np.abs(Q).astype(np.float64) @ np.abs(V).astype(np.float64).T
+    err = np.abs(Y - exact) / scale
+    assert err.max() < 2e-6, err.max()
+
+
+@pytest.mark.parametrize("S,rpw", [(32, 1), (32, 2), (16, 4), (1, 8)])
+def test_dense_ff_product_accuracy(handle, S, rpw):
+    """The float-float block product alone against an exact (integer-checked)
+    reference: error within ~2^-44 of sum |Q||V| per entry, on a block with a
+    large common offset (the cancellation an eigen-bent G^-1 produces)."""
+    import ctypes as C
+    from cosmicblup_gb300._lib import lib, ptr
+    rng = np.random.default_rng(80 + S + rpw)
+    ng, ld = 700, 2048
+    Q = rng.standard_normal((ng, ld)) + 150.0
+    V = rng.standard_normal((S, ld))
+    V -= V.mean(axis=1, keepdims=True)   # strong cancellation against the offset
+    Y = np.zeros((ng, S))
+    ms = C.c_double(0)
+    handle.check(lib().cbx_selftest_dense_ff(handle.raw, ptr(Q), ng, ld, ptr(V), S, rpw, 0, ptr(Y), C.byref(ms)))
+    import math
+
+    # exact dot products of FP64 inputs: math.fsum over exactly split products
+    def xdot(a, b):
+        ah = a.astype(np.float32).astype(np.float64)
+        bh = b.astype(np.float32).astype(np.float64)
+        parts = [ah * bh, ah * (b - bh), (a - ah) * bh, (a - ah) * (b - bh)]
+        return math.fsum(np.concatenate(parts))
+    rows = range(0, ng, 37)
+    scale = np.abs(Q) @ np.abs(V).T
+    for i in rows:
+        for c in range(S):
+            err = abs(Y[i, c] - xdot(Q[i], V[c])) / scale[i, c]
+            assert err < 6e-14, (i, c, err)
