@@ -77,7 +77,9 @@ SIGNATURES = [
     ("cbx_mt_solve", C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
                                C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("cbx_dense_apply_noalloc", C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
-    # self-test export (not in the public header)
+    # diagnostics and self-test exports (not in the public header)
+    ("cbx_trace_enable", C.c_int, [C.c_void_p, C.c_int32]),
+    ("cbx_trace_read", C.c_int, [C.c_void_p, C.c_char_p, C.c_int64]),
     ("cbx_selftest_umma", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("cbx_selftest_dense_ff", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_void_p, C.c_int32,
                                         C.c_int32, C.c_int32, C.c_void_p, C.POINTER(C.c_double)]),
@@ -152,6 +154,21 @@ class Handle:
         ms = C.c_double(0)
         self.check(lib().cbx_timer_stop(self.raw, C.byref(ms)))
         return ms.value
+
+    def trace(self, on: bool) -> None:
+        """Start (or stop) the per-launch trace of this handle's stream."""
+        self.check(lib().cbx_trace_enable(self.raw, 1 if on else 0))
+
+    def trace_read(self) -> list[tuple[str, int, float]]:
+        """(kernel, launches, ms) since the trace started, most expensive first;
+        each launch is charged the time since the previous one finished."""
+        buf = C.create_string_buffer(1 << 16)
+        self.check(lib().cbx_trace_read(self.raw, buf, len(buf)))
+        out = []
+        for line in buf.value.decode().splitlines():
+            name, cnt, ms = line.split("\t")
+            out.append((name, int(cnt), float(ms)))
+        return out
 
     def launches(self) -> int:
         return int(lib().cbx_launch_count(self.raw))

@@ -1,4 +1,8 @@
 // Handle lifetime and bookkeeping entry points of the C ABI.
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <map>
 #include "handle.h"
 
 void cbx_handle::check_status(const char* what) {
@@ -67,6 +71,9 @@ int cbx_destroy(cbx_handle* h) {
     tmp->libs_slot.reset();
     tmp->status.release();
     for (auto& r : tmp->prof) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
+    for (auto& t : tmp->trace) cudaEventDestroy(t.second);
+    for (auto& e : tmp->trace_pool) cudaEventDestroy(e);
+    if (tmp->trace_start) cudaEventDestroy(tmp->trace_start);
     if (tmp->timer_a) cudaEventDestroy(tmp->timer_a);
     if (tmp->timer_b) cudaEventDestroy(tmp->timer_b);
     if (tmp->stream) cudaStreamDestroy(tmp->stream);
@@ -107,6 +114,56 @@ int cbx_timer_stop(cbx_handle* h, double* ms) {
     float t = 0;
     CBX_CUDA(cudaEventElapsedTime(&t, h->timer_a, h->timer_b));
     if (ms) *ms = t;
+  });
+}
+
+// Launch trace (diagnostics, not in the public header).  cbx_trace_enable(h, 1)
+// starts a trace; cbx_trace_read writes "name<TAB>launches<TAB>ms" lines, most
+// expensive first, into buf (NUL-terminated, truncated at cap) and clears it.
+int cbx_trace_enable(cbx_handle* h, int32_t on) {
+  return cbx_guard(h, [&] {
+    CBX_CUDA(cudaSetDevice(h->device));
+    for (auto& t : h->trace) h->trace_pool.push_back(t.second);
+    h->trace.clear();
+    h->trace_on = on != 0;
+    if (h->trace_on) {
+      if (!h->trace_start) CBX_CUDA(cudaEventCreate(&h->trace_start));
+      CBX_CUDA(cudaEventRecord(h->trace_start, h->stream));
+    }
+  });
+}
+
+int cbx_trace_read(cbx_handle* h, char* buf, int64_t cap) {
+  return cbx_guard(h, [&] {
+    CBX_REQUIRE(buf && cap > 0, CBX_ERR_ARG, "no buffer");
+    CBX_CUDA(cudaSetDevice(h->device));
+    CBX_CUDA(cudaStreamSynchronize(h->stream));
+    std::map<std::string, std::pair<int64_t, double>> agg;
+    cudaEvent_t prev = h->trace_start;
+    for (auto& t : h->trace) {
+      float ms = 0.f;
+      if (prev) CBX_CUDA(cudaEventElapsedTime(&ms, prev, t.second));
+      auto& a = agg[t.first];
+      a.first += 1;
+      a.second += ms;
+      prev = t.second;
+    }
+    std::vector<std::pair<double, std::string>> rows;
+    for (auto& kv : agg) {
+      char line[256];
+      snprintf(line, sizeof line, "%s\t%lld\t%.4f\n", kv.first.c_str(), (long long)kv.second.first,
+               kv.second.second);
+      rows.emplace_back(kv.second.second, line);
+    }
+    std::sort(rows.begin(), rows.end(), [](auto& a, auto& b) { return a.first > b.first; });
+    std::string out;
+    for (auto& r : rows) out += r.second;
+    const size_t n = std::min<size_t>(out.size(), (size_t)cap - 1);
+    memcpy(buf, out.data(), n);
+    buf[n] = 0;
+    for (auto& t : h->trace) h->trace_pool.push_back(t.second);
+    h->trace.clear();
+    if (h->trace_on) CBX_CUDA(cudaEventRecord(h->trace_start, h->stream));
   });
 }
 

@@ -1,5 +1,5 @@
 // Dense block product on the tensor cores for the FP32 PCG bulk:
-//   Tpart[ks][i][c] = sum_{k in split ks} Qd[i][k] * Vt[c][k]      (S = 16 or 32 columns)
+//   Tpart[ks][i][c] = sum_{k in split ks} Qd[i][k] * Vt[c][k]      (S = 16, 32 or 64 columns)
 // with 3xTF32 splitting (hi*hi + hi*lo + lo*hi, FP32 accumulation in TMEM),
 // which keeps FP32-level accuracy on the tf32 tensor path.  The tf32 MMA reads
 // an FP32 operand as its 19 high bits (the 13 low mantissa bits are dropped),
@@ -34,6 +34,7 @@ constexpr int THREADS = 320;
 
 template <int S>
 struct Layout {
+  static constexpr uint32_t TMEM_COLS = 4 * S;         // two accumulator buffers of 2S columns
   static constexpr int B_BYTES = S * KB * 4;             // S rows of 128 bytes
   static constexpr int OFF_B = 2 * A_BYTES;              // A, A_lo, then B and B_lo back to back
   static constexpr int OFF_BL = OFF_B + B_BYTES;         // (B_lo rows continue B's 1024-byte groups)
@@ -130,7 +131,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 1) {
-    tmem_alloc(&bars->tmem, 128);  // two accumulator buffers of 64 columns
+    tmem_alloc(&bars->tmem, LY::TMEM_COLS);
     tmem_relinquish();
   }
   tc_fence_before();
@@ -173,7 +174,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         const uint32_t b = c & 1;
         if (!mbar_wait(&bars->acc_empty[b], ((c >> 1) & 1) ^ 1, abort_flag)) { ok = false; break; }
         tc_fence_after();
-        const uint32_t d = tmem + b * 64;
+        const uint32_t d = tmem + b * 2 * S;
         for (int k = k0; k < k1; ++k, ++g) {
           const uint32_t s = g % NSTAGE;
           if (!mbar_wait(&bars->conv[s], (g / NSTAGE) & 1, abort_flag)) { ok = false; break; }
@@ -235,14 +236,17 @@ __global__ void __launch_bounds__(THREADS, 1)
       // columns [0, S): A B_hi; [S, 2S): A B_lo + A_lo B_hi
       uint32_t r[32];
       float out[S];
-      const uint32_t ta = tmem + (uint32_t(q * 32) << 16) + b * 64;
-      if constexpr (S == 32) {
-        uint32_t r2[32];
-        tmem_ld32(ta, r);
-        tmem_ld32(ta + 32, r2);
-        tmem_ld_wait();
+      const uint32_t ta = tmem + (uint32_t(q * 32) << 16) + b * 2 * S;
+      if constexpr (S >= 32) {
 #pragma unroll
-        for (int j = 0; j < 32; ++j) out[j] = __uint_as_float(r[j]) + __uint_as_float(r2[j]);
+        for (int j0 = 0; j0 < S; j0 += 32) {
+          uint32_t r2[32];
+          tmem_ld32(ta + j0, r);
+          tmem_ld32(ta + S + j0, r2);
+          tmem_ld_wait();
+#pragma unroll
+          for (int j = 0; j < 32; ++j) out[j0 + j] = __uint_as_float(r[j]) + __uint_as_float(r2[j]);
+        }
       } else {
         tmem_ld32(ta, r);  // 16 + 16 columns
         tmem_ld_wait();
@@ -265,7 +269,7 @@ __global__ void __launch_bounds__(THREADS, 1)
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
-  if (warp == 1) tmem_dealloc(tmem, 128);
+  if (warp == 1) tmem_dealloc(tmem, LY::TMEM_COLS);
 }
 
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
@@ -321,7 +325,7 @@ int dense_tc_ksplit(int64_t ng, int64_t ld, int num_sms) {
 
 void dense_tc(cbx_handle* h, const float* Qd, int64_t ng, int64_t ld, const float* Vt, int S, int ksplit, float* Tpart,
               const int* active) {
-  CBX_REQUIRE(S == 16 || S == 32, CBX_ERR_ARG, "dense_tc supports 16 or 32 columns");
+  CBX_REQUIRE(S == 16 || S == 32 || S == 64, CBX_ERR_ARG, "dense_tc supports 16, 32 or 64 columns");
   CBX_REQUIRE(ld % 4 == 0, CBX_ERR_ARG, "row pitch must be a multiple of 4");
   const CUtensorMap ma = dtc::make_map(Qd, ld, ng, 128);
   const CUtensorMap mb = dtc::make_map(Vt, ld, S, S);
@@ -331,7 +335,12 @@ void dense_tc(cbx_handle* h, const float* Qd, int64_t ng, int64_t ld, const floa
   const int mtiles = (int)((ng + 127) / 128);
   const int nunits = mtiles * ksplit;
   const int grid = std::min(nunits, h->num_sms);
-  if (S == 32) {
+  if (S == 64) {
+    constexpr int SM = dtc::Layout<64>::SMEM;
+    CBX_CUDA(cudaFuncSetAttribute(dtc::k_dense_tf32<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, SM));
+    dtc::k_dense_tf32<64><<<grid, dtc::THREADS, SM, h->stream>>>(ma, mb, (int)ng, ksteps, ksplit, kps, nunits, Tpart,
+                                                                 active, h->status.p);
+  } else if (S == 32) {
     constexpr int SM = dtc::Layout<32>::SMEM;
     CBX_CUDA(cudaFuncSetAttribute(dtc::k_dense_tf32<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, SM));
     dtc::k_dense_tf32<32><<<grid, dtc::THREADS, SM, h->stream>>>(ma, mb, (int)ng, ksteps, ksplit, kps, nunits, Tpart,

@@ -41,12 +41,32 @@ struct cbx_handle {
   std::vector<ProfRec> prof;
   cudaEvent_t timer_a = nullptr, timer_b = nullptr;
 
+  // optional launch trace (diagnostics): an event after every launch, so the
+  // time between consecutive events is charged to the later launch (its own
+  // run time plus any idle gap before it, host syncs included)
+  bool trace_on = false;
+  std::vector<std::pair<const char*, cudaEvent_t>> trace;
+  std::vector<cudaEvent_t> trace_pool;
+  cudaEvent_t trace_start = nullptr;
+
   // count a kernel launch and check the launch error
   void launched(const char* what) {
     ++launches;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess)
       throw cbx::Error(CBX_ERR_CUDA, std::string("launch ") + what + ": " + cudaGetErrorString(e));
+    if (trace_on) trace_mark(what);
+  }
+  void trace_mark(const char* what) {
+    cudaEvent_t ev;
+    if (trace_pool.empty()) {
+      if (cudaEventCreate(&ev) != cudaSuccess) return;
+    } else {
+      ev = trace_pool.back();
+      trace_pool.pop_back();
+    }
+    cudaEventRecord(ev, stream);
+    trace.emplace_back(what, ev);
   }
   // read the device status word, reset it, and throw on a device-side failure
   void check_status(const char* what);

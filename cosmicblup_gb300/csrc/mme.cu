@@ -17,6 +17,7 @@
 #include "pcg.h"
 #include "solver.cuh"
 #include "dense_tc.h"
+#include "dense.h"
 #include <cstdlib>
 
 namespace cbx {
@@ -64,20 +65,41 @@ __global__ void k_pitch_copy(const double* __restrict__ src, int64_t n, int64_t 
   }
 }
 
-// dst[i * ld + k] = fl32(src - fl32(src)) (k < n), 0 in the padding: the low
-// FP32 part of the float-float copy of the block
-__global__ void k_pitch_lo(const double* __restrict__ src, int64_t n, int64_t ld, float* __restrict__ dst) {
+// Low-precision copies of an n x n block (row-major, pitch n) minus a constant:
+// hi[i * ld + k] = fl32(src - shift), lo = fl32(src - shift - hi) for k < n;
+// padding columns are zero.
+__global__ void k_lowp_block(const double* __restrict__ src, int64_t n, int64_t ld, double shift,
+                             float* __restrict__ hi, float* __restrict__ lo) {
   const int64_t total = n * ld;
   for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
        idx += (int64_t)gridDim.x * blockDim.x) {
     const int64_t i = idx / ld, k = idx - i * ld;
+    float h = 0.0f, l = 0.0f;
     if (k < n) {
-      const double v = src[i * n + k];
-      dst[idx] = __double2float_rn(v - (double)__double2float_rn(v));
-    } else {
-      dst[idx] = 0.0f;
+      const double v = src[i * n + k] - shift;
+      h = __double2float_rn(v);
+      l = __double2float_rn(v - (double)h);
     }
+    hi[idx] = h;
+    lo[idx] = l;
   }
+}
+
+// Per-block partial sums of the off-diagonal entries of an n x n block.
+__global__ void k_offdiag_part(const double* __restrict__ src, int64_t n, double* __restrict__ part) {
+  __shared__ double red[256];
+  double acc = 0.0;
+  const int64_t total = n * n;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x)
+    if (idx / n != idx % n) acc += src[idx];
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = red[0];
 }
 
 // column-major (dim x ncols) -> interleaved (dim x S), zero in unused columns
@@ -132,10 +154,26 @@ __global__ void k_correction(double* __restrict__ x64, const float* __restrict__
     x64[idx] += d;
   }
 }
-// R -= a * Y
-__global__ void k_axpy_neg(double* __restrict__ R, const double* __restrict__ Y, double a, int64_t n) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    R[i] -= a * Y[i];
+// Residual carried to a new lambda.  With r' = b - A(lam') x for lam' = lam -
+// dlam, A(lam') x = W'W x + lam' [0; Qinv x_u] gives lam' [0; Qinv x_u] =
+// b - r' - W'W x, so b - A(lam) x = r' - (dlam / lam') (b - r' - W'W x) on
+// the random rows and r' on the fixed rows: only the sparse W'W is applied.
+// Interleaved blocks (row i, column c at i * S + c); f = dlam / lam'.
+__global__ void k_carry_resid(const int32_t* __restrict__ Dptr, const int32_t* __restrict__ Dcol,
+                              const double* __restrict__ Dval, int64_t p, int64_t dim, int S,
+                              const double* __restrict__ B, const double* __restrict__ X, double f,
+                              double* __restrict__ R) {
+  const int64_t total = (dim - p) * S;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = p + idx / S;
+    const int c = (int)(idx % S);
+    double t = 0.0;
+    for (int32_t j = Dptr[i]; j < Dptr[i + 1]; ++j) t += Dval[j] * X[(int64_t)Dcol[j] * S + c];
+    const int64_t e = i * S + c;
+    const double r = R[e];
+    R[e] = r - f * ((B[e] - r) - t);
+  }
 }
 // R -= Y
 __global__ void k_sub_inplace(double* __restrict__ R, const double* __restrict__ Y, int64_t n) {
@@ -185,13 +223,13 @@ sv::OpView<float> make_view<float>(Mme& m, const float* dinv) {
 // rows per warp of the dense kernel: RPW * S accumulators <= 64 doubles / 128 floats
 template <typename T, int S>
 constexpr int rpw() {
-  return sizeof(T) == 8 ? (S <= 8 ? 8 : (S == 16 ? 4 : 2)) : (S <= 16 ? 8 : 4);
+  return sizeof(T) == 8 ? (S <= 8 ? 8 : (S == 16 ? 4 : (S == 32 ? 2 : 1))) : (S <= 16 ? 8 : (S == 32 ? 4 : 2));
 }
 
 template <typename T, int S>
 struct Workspace {
   DevBuf<T> R, Z, P, Q, Vt, Tout, X;
-  DevBuf<double> part, pq_part, rz_fix, tol;
+  DevBuf<double> part, pq_part, rz_fix, tol, colsum;
   DevBuf<T> seg_part;
   DevBuf<sv::Col> col;
   DevBuf<int> active;
@@ -201,7 +239,7 @@ struct Workspace {
     if (dim == m.dim && (!m.has_dense || Vt.n == (size_t)S * m.ld)) return;
     const int64_t n = m.dim * S;
     R.resize(n); Z.resize(n); P.resize(n); Q.resize(n); X.resize(n);
-    if (m.has_dense) { Vt.resize((size_t)S * m.ld); Tout.resize((size_t)m.ng * S * 8); }
+    if (m.has_dense) { Vt.resize((size_t)S * m.ld); Tout.resize((size_t)m.ng * S * 8); colsum.resize(S); }
     nblk_vec = (int)grid_for(n, sv::NT, 2 * num_sms);
     nblk_spmv = (int)m.p + (int)grid_for(m.dim - m.p, 8, 8 * num_sms);
     part.resize((size_t)nblk_vec * 3 * S);
@@ -236,52 +274,140 @@ static bool use_resid_ff() {
   return v == 1;
 }
 
-template <int S>
-constexpr int rpw_ff() {
-  return S >= 32 ? 2 : (S >= 8 ? 4 : 8);
+// Recursive-residual threshold of the mixed solver: a correction d updates
+// r -= A d in float-float when ||d|| <= 2^-recur_shift ||x|| in every column
+// (environment CBX_RECUR_SHIFT, default 4).
+static int env_int(const char* name, int def) {
+  const char* e = std::getenv(name);
+  return (e && *e) ? std::atoi(e) : def;
+}
+static int recur_shift() {
+  static int v = env_int("CBX_RECUR_SHIFT", 4);
+  return v;
 }
 
+template <int S>
+constexpr int rpw_ff() {
+  return S >= 64 ? 1 : (S >= 32 ? 2 : (S >= 8 ? 4 : 8));
+}
+
+// Vt[c * ld + k] = X[(p + gmap[k]) * xs + c] for c < ncols, k < ng (the gathered
+// dense-block rows of an interleaved block, as columns of a column-major
+// ld x ncols matrix).
+__global__ void k_gather_cols(const double* __restrict__ X, int xs, int ncols, double* __restrict__ Vt, int64_t p,
+                              int64_t ng, int64_t ld, const int32_t* __restrict__ gmap) {
+  const int64_t total = (int64_t)ncols * ld;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = idx / ld, k = idx - c * ld;
+    Vt[idx] = k < ng ? X[(p + gmap[k]) * xs + c] : 0.0;
+  }
+}
+
+// Float-float block products are FP32-issue-bound, so they run on the
+// populated columns only, in power-of-two pieces of at most 32 columns written
+// into the S-wide output.
+template <int W>
+static void ff_piece(cbx_handle* h, const sv::OpView<double>& op, const double* X, int xs, double* Vt,
+                     double* Tout, const int* active) {
+  cudaStream_t s = h->stream;
+  const Mme& mm = *h->mme;
+  // (hi, lo) pairs take the space of the FP64 gather buffer
+  float2* vhl = reinterpret_cast<float2*>(Vt);
+  sv::k_gather_hl<W><<<grid_for(W * op.ld, 256, 4 * h->num_sms), 256, 0, s>>>(X, vhl, op.p, op.ng, op.ld, op.gmap,
+                                                                            xs);
+  h->launched("k_gather_hl<f64>");
+  constexpr int R = rpw_ff<W>();
+  const int smem = W * 256 * (int)sizeof(float2);
+  CBX_CUDA(cudaFuncSetAttribute(sv::k_dense_ff<W, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  sv::k_dense_ff<W, R><<<(unsigned)((op.ng + 8 * R - 1) / (8 * R)), 256, smem, s>>>(mm.Qd32.p, mm.Qlo32.p, op.ng,
+                                                                                   op.ld, vhl, Tout, active, xs);
+  h->launched("k_dense_ff<f64>");
+}
+
+// Tout[:, 0:ncols] (rows S apart) of the dense block product in FP64
+// accuracy: float-float on the CUDA cores (ff), or cuBLAS DGEMM / DGEMV on the
+// gathered columns (the block is an ng x ng column-major matrix with leading
+// dimension ld; it is symmetric, so either orientation gives Qinv X).
+static void dense64(cbx_handle* h, const sv::OpView<double>& op, const double* X, int S, int ncols, double* Vt,
+                    double* Tout, const int* active, bool ff, double* colsum) {
+  if (ff) {
+    // the compensated FP64 column sums that restore the block's shift
+    sv::k_colsum_x<<<ncols, 256, 0, h->stream>>>(X, S, op.p, op.ng, op.gmap, colsum);
+    h->launched("k_colsum_x<f64>");
+    for (int c0 = 0; c0 < ncols;) {
+      const int left = std::min(ncols - c0, 32);
+      int w = 1;
+      while (2 * w <= left) w <<= 1;
+      switch (w) {
+        case 1: ff_piece<1>(h, op, X + c0, S, Vt, Tout + c0, active); break;
+        case 2: ff_piece<2>(h, op, X + c0, S, Vt, Tout + c0, active); break;
+        case 4: ff_piece<4>(h, op, X + c0, S, Vt, Tout + c0, active); break;
+        case 8: ff_piece<8>(h, op, X + c0, S, Vt, Tout + c0, active); break;
+        case 16: ff_piece<16>(h, op, X + c0, S, Vt, Tout + c0, active); break;
+        default: ff_piece<32>(h, op, X + c0, S, Vt, Tout + c0, active); break;
+      }
+      c0 += w;
+    }
+    return;
+  }
+  cudaStream_t s = h->stream;
+  k_gather_cols<<<grid_for((int64_t)ncols * op.ld, 256, 4 * h->num_sms), 256, 0, s>>>(X, S, ncols, Vt, op.p, op.ng,
+                                                                                     op.ld, op.gmap);
+  h->launched("k_gather_cols<f64>");
+  Libs& L = libs(h);
+  const double one = 1.0, zero = 0.0;
+  if (ncols == 1) {
+    // Tout[i * S] = sum_k Q(k, i) v(k)
+    CBX_BLAS(cublasDgemv(L.blas, CUBLAS_OP_T, (int)op.ng, (int)op.ng, &one, op.Qd, (int)op.ld, Vt, 1, &zero, Tout,
+                         S));
+  } else {
+    // Tout^T (ncols x ng, leading dimension S) = Vt^T (ncols x ng) * Q (ng x ng)
+    CBX_BLAS(cublasDgemm(L.blas, CUBLAS_OP_T, CUBLAS_OP_N, ncols, (int)op.ng, (int)op.ng, &one, Vt, (int)op.ld,
+                         op.Qd, (int)op.ld, &zero, Tout, S));
+  }
+  h->launched("cublas_dgemm<f64>");
+}
+
+// Y = use_D * W'W X + lam [0; Qinv X_u] for an S-wide interleaved block whose
+// first ncols columns are populated (the rest are zero or ignored); optional
+// pq partials sum_i P[i] Y[i] for the PCG step.
 template <typename T, int S>
 void matvec(cbx_handle* h, const sv::OpView<T>& op, Workspace<T, S>& w, const T* X, T* Y, double lam, int use_D,
-            const T* P, double* pq_part, const int* active, bool ff = false) {
+            const T* P, double* pq_part, const int* active, bool ff = false, int ncols = S) {
   cudaStream_t s = h->stream;
   int tsplit = 1;
-  if constexpr (sizeof(T) == 8) {
-    ff = ff && op.Qd && h->mme->Qlo32.p && h->mme->Qd32.p;
-  } else {
-    ff = false;
-  }
-  if (ff) {
-    if constexpr (sizeof(T) == 8) {
-      const Mme& mm = *h->mme;
-      // (hi, lo) pairs take the space of the FP64 gather buffer
-      float2* vhl = reinterpret_cast<float2*>(w.Vt.p);
-      sv::k_gather_hl<S><<<grid_for(S * op.ld, 256, 4 * h->num_sms), 256, 0, s>>>(X, vhl, op.p, op.ng, op.ld,
-                                                                                op.gmap);
-      h->launched("k_gather_hl");
-      constexpr int R = rpw_ff<S>();
-      const int smem = S * 256 * (int)sizeof(float2);
-      CBX_CUDA(cudaFuncSetAttribute(sv::k_dense_ff<S, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-      cbx_handle::ProfRec pr{};
-      if (h->prof_on) {
-        CBX_CUDA(cudaEventCreate(&pr.a));
-        CBX_CUDA(cudaEventCreate(&pr.b));
-        CBX_CUDA(cudaEventRecord(pr.a, s));
-      }
-      sv::k_dense_ff<S, R><<<(unsigned)((op.ng + 8 * R - 1) / (8 * R)), 256, smem, s>>>(
-          mm.Qd32.p, mm.Qlo32.p, op.ng, op.ld, vhl, w.Tout.p, active);
-      h->launched("k_dense_ff");
-      if (h->prof_on) {
-        CBX_CUDA(cudaEventRecord(pr.b, s));
-        pr.bucket = 1;
-        pr.bytes = 8.0 * ((double)op.ng * op.ld + (double)S * op.ld + (double)op.ng * S);
-        h->prof.push_back(pr);
-      }
+  // The FP32 and float-float products use the shifted copies and add
+  // qshift * (column sums) back; the FP64 product uses the block itself.
+  const double* colsum = op.Qd ? w.colsum.p : nullptr;
+  const double tshift = h->mme->qshift;
+  if (!op.Qd) {
+  } else if constexpr (sizeof(T) == 8) {
+    ff = ff && h->mme->Qlo32.p && h->mme->Qd32.p;
+    if (!ff) colsum = nullptr;
+    cbx_handle::ProfRec pr{};
+    if (h->prof_on) {
+      CBX_CUDA(cudaEventCreate(&pr.a));
+      CBX_CUDA(cudaEventCreate(&pr.b));
+      CBX_CUDA(cudaEventRecord(pr.a, s));
     }
-  } else if (op.Qd && sizeof(T) == 4 && (S == 16 || S == 32) && use_dense_tc()) {
+    if (ncols < S) {
+      CBX_CUDA(cudaMemsetAsync(w.Tout.p, 0, (size_t)op.ng * S * sizeof(double), s));
+      CBX_CUDA(cudaMemsetAsync(w.colsum.p, 0, S * sizeof(double), s));
+    }
+    dense64(h, op, X, S, ncols, w.Vt.p, w.Tout.p, active, ff, w.colsum.p);
+    if (h->prof_on) {
+      CBX_CUDA(cudaEventRecord(pr.b, s));
+      pr.bucket = 1;
+      pr.bytes = 8.0 * (double)op.ng * op.ld + 8.0 * ncols * ((double)op.ld + (double)op.ng);
+      h->prof.push_back(pr);
+    }
+  } else if ((S == 16 || S == 32 || S == 64) && use_dense_tc()) {
     sv::k_gather_t<T, S><<<grid_for(S * op.ld, 256, 4 * h->num_sms), 256, 0, s>>>(X, w.Vt.p, op.p, op.ng, op.ld,
                                                                                op.gmap, active);
-    h->launched("k_gather_t");
+    h->launched("k_gather_t<f32>");
+    sv::k_colsum_vt<T><<<S, 256, 0, s>>>(w.Vt.p, op.ld, op.ng, w.colsum.p);
+    h->launched("k_colsum_vt<f32>");
     tsplit = dense_tc_ksplit(op.ng, op.ld, h->num_sms);
     cbx_handle::ProfRec pr{};
     if (h->prof_on) {
@@ -297,30 +423,30 @@ void matvec(cbx_handle* h, const sv::OpView<T>& op, Workspace<T, S>& w, const T*
       pr.bytes = 4.0 * ((double)op.ng * op.ld + (double)S * op.ld + (double)op.ng * S * tsplit);
       h->prof.push_back(pr);
     }
-  } else if (op.Qd && S == 1) {
+  } else if (S == 1) {
     sv::k_gather_t<T, S><<<grid_for(S * op.ld, 256, 4 * h->num_sms), 256, 0, s>>>(X, w.Vt.p, op.p, op.ng, op.ld,
                                                                                op.gmap, active);
-    h->launched("k_gather_t");
-    constexpr int R = 4, U = sizeof(T) == 4 ? 4 : 2;
+    h->launched("k_gather_t<f32>");
     cbx_handle::ProfRec pr{};
     if (h->prof_on) {
       CBX_CUDA(cudaEventCreate(&pr.a));
       CBX_CUDA(cudaEventCreate(&pr.b));
       CBX_CUDA(cudaEventRecord(pr.a, s));
     }
-    sv::k_gemv<T, R, U><<<(unsigned)((op.ng + 8 * R - 1) / (8 * R)), 256, 0, s>>>(op.Qd, op.ng, op.ld, w.Vt.p,
-                                                                                w.Tout.p, active);
-    h->launched("k_gemv");
+    sv::k_colsum_vt<T><<<S, 256, 0, s>>>(w.Vt.p, op.ld, op.ng, w.colsum.p);
+    h->launched("k_colsum_vt<f32>");
+    sv::k_gemv<T, 4, 4><<<(unsigned)((op.ng + 31) / 32), 256, 0, s>>>(op.Qd, op.ng, op.ld, w.Vt.p, w.Tout.p, active);
+    h->launched("k_gemv<f32>");
     if (h->prof_on) {
       CBX_CUDA(cudaEventRecord(pr.b, s));
-      pr.bucket = sizeof(T) == 4 ? 0 : 1;
-      pr.bytes = (double)sizeof(T) * ((double)op.ng * op.ld + (double)op.ld + (double)op.ng);
+      pr.bucket = 0;
+      pr.bytes = 4.0 * ((double)op.ng * op.ld + (double)op.ld + (double)op.ng);
       h->prof.push_back(pr);
     }
-  } else if (op.Qd) {
+  } else {
     sv::k_gather_t<T, S><<<grid_for(S * op.ld, 256, 4 * h->num_sms), 256, 0, s>>>(X, w.Vt.p, op.p, op.ng, op.ld,
                                                                                op.gmap, active);
-    h->launched("k_gather_t");
+    h->launched("k_gather_t<f32>");
     constexpr int R = rpw<T, S>();
     constexpr int KT = 32 * sv::Vec16<T>::n * 4;
     const int smem = S * KT * (int)sizeof(T);
@@ -331,25 +457,28 @@ void matvec(cbx_handle* h, const sv::OpView<T>& op, Workspace<T, S>& w, const T*
       CBX_CUDA(cudaEventCreate(&pr.b));
       CBX_CUDA(cudaEventRecord(pr.a, s));
     }
+    sv::k_colsum_vt<T><<<S, 256, 0, s>>>(w.Vt.p, op.ld, op.ng, w.colsum.p);
+    h->launched("k_colsum_vt<f32>");
     sv::k_dense<T, S, R><<<(unsigned)((op.ng + 8 * R - 1) / (8 * R)), 256, smem, s>>>(op.Qd, op.ng, op.ld, w.Vt.p,
                                                                                      w.Tout.p, active);
-    h->launched("k_dense");
+    h->launched("k_dense<f32>");
     if (h->prof_on) {
       CBX_CUDA(cudaEventRecord(pr.b, s));
-      pr.bucket = sizeof(T) == 4 ? 0 : 1;
+      pr.bucket = 0;
       // algorithmic bytes: the dense block once, the S gathered vectors, the S outputs
-      pr.bytes = (double)sizeof(T) * ((double)op.ng * op.ld + (double)S * op.ld + (double)op.ng * S);
+      pr.bytes = 4.0 * ((double)op.ng * op.ld + (double)S * op.ld + (double)op.ng * S);
       h->prof.push_back(pr);
     }
   }
   if (use_D && h->mme->nseg > 0) {
     const Mme& mm = *h->mme;
     sv::k_fix_seg<T, S><<<mm.nseg, sv::NT, 0, s>>>(op, mm.seg_row.p, mm.seg_lo.p, mm.seg_hi.p, X, w.seg_part.p, active);
-    h->launched("k_fix_seg");
+    h->launched(sizeof(T) == 4 ? "k_fix_seg<f32>" : "k_fix_seg<f64>");
   }
-  sv::k_spmv<T, S><<<w.nblk_spmv, sv::NT, 0, s>>>(op, X, w.Tout.p, tsplit, h->mme->fix_seg_ptr.p, w.seg_part.p,
+  sv::k_spmv<T, S><<<w.nblk_spmv, sv::NT, 0, s>>>(op, X, w.Tout.p, tsplit, colsum, tshift, h->mme->fix_seg_ptr.p,
+                                                  w.seg_part.p,
                                                   (T)lam, use_D, Y, P, pq_part, active);
-  h->launched("k_spmv");
+  h->launched(sizeof(T) == 4 ? "k_spmv<f32>" : "k_spmv<f64>");
 }
 
 // Multi-RHS PCG in precision T on interleaved vectors; X receives the solution
@@ -361,41 +490,44 @@ void run_pcg(cbx_handle* h, Mme& m, const sv::OpView<T>& op, Workspace<T, S>& w,
   cudaStream_t s = h->stream;
   const int64_t n = m.dim * S;
   if (use_x0) {
-    matvec<T, S>(h, op, w, X, w.Q.p, lam, 1, nullptr, nullptr, nullptr);
+    matvec<T, S>(h, op, w, X, w.Q.p, lam, 1, nullptr, nullptr, nullptr, false, ncols);
     ++matvecs;
   } else {
     CBX_CUDA(cudaMemsetAsync(X, 0, n * sizeof(T), s));
   }
   sv::k_init_resid<T, S><<<w.nblk_vec, sv::NT, 0, s>>>(op, B, w.Q.p, use_x0 ? 1 : 0, w.R.p, w.Z.p, w.part.p);
-  h->launched("k_init_resid");
+  h->launched(sizeof(T) == 4 ? "k_init_resid<f32>" : "k_init_resid<f64>");
   if (m.p > 0) {
     sv::k_fixed<T, S><<<(unsigned)m.p, sv::NT, 0, s>>>(op, w.R.p, w.Z.p, nullptr, w.rz_fix.p);
-    h->launched("k_fixed");
+    h->launched(sizeof(T) == 4 ? "k_fixed<f32>" : "k_fixed<f64>");
   }
   std::vector<double> tolv(S, 1.0);
   for (int c = 0; c < ncols; ++c) tolv[c] = tol_col[c];
   CBX_CUDA(cudaMemcpyAsync(w.tol.p, tolv.data(), S * sizeof(double), cudaMemcpyHostToDevice, s));
   sv::k_scalar_init<S><<<1, sv::NT, 0, s>>>(w.col.p, ncols, w.part.p, w.nblk_vec, w.rz_fix.p, m.p, abs_tol, w.active.p);
-  h->launched("k_scalar_init");
+  h->launched(sizeof(T) == 4 ? "k_scalar_init<f32>" : "k_scalar_init<f64>");
   CBX_CUDA(cudaMemcpyAsync(w.P.p, w.Z.p, n * sizeof(T), cudaMemcpyDeviceToDevice, s));
   int host_active = 1;
-  const int CHECK = 8;
+  // host check of the active-column count every CHECK iterations; the FP64
+  // block product is slow enough (and cannot skip finished blocks) to check
+  // after every iteration
+  const int CHECK = (sizeof(T) == 8 && op.Qd) ? 1 : 8;
   for (int it = 0; it < maxit && host_active; it += CHECK) {
     for (int j = 0; j < CHECK; ++j) {
-      matvec<T, S>(h, op, w, w.P.p, w.Q.p, lam, 1, w.P.p, w.pq_part.p, w.active.p);
+      matvec<T, S>(h, op, w, w.P.p, w.Q.p, lam, 1, w.P.p, w.pq_part.p, w.active.p, false, ncols);
       sv::k_scalar_alpha<S><<<1, sv::NT, 0, s>>>(w.col.p, w.pq_part.p, w.nblk_spmv);
-      h->launched("k_scalar_alpha");
+      h->launched(sizeof(T) == 4 ? "k_scalar_alpha<f32>" : "k_scalar_alpha<f64>");
       sv::k_update<T, S><<<w.nblk_vec, sv::NT, 0, s>>>(op, w.col.p, X, w.R.p, w.Z.p, w.P.p, w.Q.p, w.part.p);
-      h->launched("k_update");
+      h->launched(sizeof(T) == 4 ? "k_update<f32>" : "k_update<f64>");
       if (m.p > 0) {
         sv::k_fixed<T, S><<<(unsigned)m.p, sv::NT, 0, s>>>(op, w.R.p, w.Z.p, w.col.p, w.rz_fix.p);
-        h->launched("k_fixed");
+        h->launched(sizeof(T) == 4 ? "k_fixed<f32>" : "k_fixed<f64>");
       }
       sv::k_scalar_beta<S><<<1, sv::NT, 0, s>>>(w.col.p, w.part.p, w.nblk_vec, w.rz_fix.p, m.p, w.tol.p, abs_tol,
                                             maxit, w.active.p);
-      h->launched("k_scalar_beta");
+      h->launched(sizeof(T) == 4 ? "k_scalar_beta<f32>" : "k_scalar_beta<f64>");
       sv::k_pupdate<T, S><<<w.nblk_vec, sv::NT, 0, s>>>(m.dim, w.col.p, w.Z.p, w.P.p);
-      h->launched("k_pupdate");
+      h->launched(sizeof(T) == 4 ? "k_pupdate<f32>" : "k_pupdate<f64>");
       ++matvecs;
     }
     CBX_CUDA(cudaMemcpyAsync(&host_active, w.active.p, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -456,9 +588,12 @@ struct Solver : public SolverBase {
   }
 
   // R64 = B - A X in FP64; returns ||R64|| per column
-  std::vector<double> residual(cbx_handle* h, Mme& m, const sv::OpView<double>& op, double lam, int64_t& mv) {
+  // R64 = B - A X in FP64 accuracy (ff: the float-float product of the shifted
+  // block, whose error is relative to the block without its common offset)
+  std::vector<double> residual(cbx_handle* h, Mme& m, const sv::OpView<double>& op, double lam, int64_t& mv,
+                               int ncols, bool ff = false) {
     cudaStream_t s = h->stream;
-    matvec<double, S>(h, op, w64, Xi.p, Y64.p, lam, 1, nullptr, nullptr, nullptr);
+    matvec<double, S>(h, op, w64, Xi.p, Y64.p, lam, 1, nullptr, nullptr, nullptr, ff, ncols);
     ++mv;
     const int64_t n = m.dim * S;
     k_sub<<<grid_for(n, 256, 4 * h->num_sms), 256, 0, s>>>(Bi.p, Y64.p, n, R64.p);
@@ -486,7 +621,7 @@ struct Solver : public SolverBase {
       for (int c = 0; c < ncols; ++c) need_true |= cols[c].status != sv::COL_CONVERGED;
       std::vector<double> rn, bn;
       if (need_true) {
-        rn = residual(h, m, op64, lam, res.matvecs);
+        rn = residual(h, m, op64, lam, res.matvecs, ncols);
         bn = norms(h, m, Bi.p);
       }
       for (int c = 0; c < ncols; ++c) {
@@ -506,16 +641,16 @@ struct Solver : public SolverBase {
     if (!use_x0) CBX_CUDA(cudaMemsetAsync(Xi.p, 0, n * sizeof(double), s));
     std::vector<double> bn = norms(h, m, Bi.p);
     std::vector<double> rn;
-    if (use_x0 && have_r0 && use_resid_ff() && m.Qlo32.p && std::abs(dlam) <= std::ldexp(lam, -7)) {
+    if (use_x0 && have_r0 && lam - dlam > 0.0) {
+      // b - A(lam) x0 from the carried b - A(lam - dlam) x0, without a dense product
       if (dlam != 0.0) {
-        matvec<double, S>(h, op64, w64, Xi.p, Y64.p, 1.0, 0, nullptr, nullptr, nullptr, true);
-        ++res.matvecs;
-        k_axpy_neg<<<grid_for(n, 256, 4 * h->num_sms), 256, 0, s>>>(R64.p, Y64.p, dlam, n);
-        h->launched("k_axpy_neg");
+        k_carry_resid<<<grid_for((m.dim - m.p) * S, 256, 4 * h->num_sms), 256, 0, s>>>(
+            m.D64.ptr.p, m.D64.col.p, m.D64.val.p, m.p, m.dim, S, Bi.p, Xi.p, dlam / (lam - dlam), R64.p);
+        h->launched("k_carry_resid");
       }
       rn = norms(h, m, R64.p);
     } else if (use_x0) {
-      rn = residual(h, m, op64, lam, res.matvecs);
+      rn = residual(h, m, op64, lam, res.matvecs, ncols, use_resid_ff());
     } else {
       // x0 = 0: the residual is b itself, no FP64 operator application needed
       CBX_CUDA(cudaMemcpyAsync(R64.p, Bi.p, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
@@ -545,27 +680,28 @@ struct Solver : public SolverBase {
       k_correction<<<grid_for(n, 256, 4 * h->num_sms), 256, 0, s>>>(Xi.p, D32.p, scale.p, m.dim, S, Dc64.p);
       h->launched("k_correction");
       res.refinements += 1;
-      // Residual of the new iterate.  A correction that is small next to the
-      // solution (||d|| <= 2^-8 ||x|| in every column) updates it as r -= A d
-      // with the float-float block product: that product's error is bounded
-      // by ~2^-46 |A| |d| <= 2^-54 |A| |x|, below the rounding of an FP64
-      // b - A x.  Otherwise (the first correction from x0 = 0, where d = x)
-      // r = b - A x is recomputed in FP64.
+      // Residual of the new iterate, with the float-float product of the
+      // shifted block: its error is ~2^-46 of |Qd - shift| |v| per row, below
+      // the rounding of an FP64 product with the unshifted block when the
+      // block carries a large common offset (an eigen-bent G^-1).  A
+      // correction that is small next to the solution (||d|| <= 2^-4 ||x|| in
+      // every column) updates r -= A d; otherwise (the first correction from
+      // x0 = 0, where d = x) r = b - A x is formed afresh.
       bool recursive = use_resid_ff() && m.Qlo32.p;
       if (recursive) {
         const std::vector<double> dn = norms(h, m, Dc64.p), xn = norms(h, m, Xi.p);
         for (int c = 0; c < ncols; ++c)
-          if (sc[c] > 0 && !(dn[c] <= std::ldexp(xn[c], -8))) recursive = false;
+          if (sc[c] > 0 && !(dn[c] <= std::ldexp(xn[c], -recur_shift()))) recursive = false;
       }
       std::vector<double> rn_new;
       if (recursive) {
-        matvec<double, S>(h, op64, w64, Dc64.p, Y64.p, lam, 1, nullptr, nullptr, nullptr, true);
+        matvec<double, S>(h, op64, w64, Dc64.p, Y64.p, lam, 1, nullptr, nullptr, nullptr, true, ncols);
         ++res.matvecs;
         k_sub_inplace<<<grid_for(n, 256, 4 * h->num_sms), 256, 0, s>>>(R64.p, Y64.p, n);
         h->launched("k_sub_inplace");
         rn_new = norms(h, m, R64.p);
       } else {
-        rn_new = residual(h, m, op64, lam, res.matvecs);
+        rn_new = residual(h, m, op64, lam, res.matvecs, ncols, use_resid_ff());
       }
       for (int c = 0; c < ncols; ++c) {
         if (sc[c] <= 0) continue;
@@ -583,23 +719,23 @@ struct Solver : public SolverBase {
   }
 
   // Y = Qinv X on interleaved blocks (u part only is meaningful)
-  void qinv(cbx_handle* h, Mme& m) {
+  void qinv(cbx_handle* h, Mme& m, int ncols) {
     prepare(h, m, 1.0, false);
     auto op = make_view<double>(m, dinv64.p);
-    matvec<double, S>(h, op, w64, Xi.p, Y64.p, 1.0, 0, nullptr, nullptr, nullptr);
+    matvec<double, S>(h, op, w64, Xi.p, Y64.p, 1.0, 0, nullptr, nullptr, nullptr, false, ncols);
   }
 };
 
 template <int S>
 static Solver<S>& solver_for(Mme& m) {
-  constexpr int idx = S == 1 ? 0 : S == 2 ? 1 : S == 4 ? 2 : S == 8 ? 3 : S == 16 ? 4 : 5;
+  constexpr int idx = S == 1 ? 0 : S == 2 ? 1 : S == 4 ? 2 : S == 8 ? 3 : S == 16 ? 4 : S == 32 ? 5 : 6;
   if (!m.solvers[idx]) m.solvers[idx].reset(new Solver<S>());
   return *static_cast<Solver<S>*>(m.solvers[idx].get());
 }
 
-static int block_width(int ncols) {
+static int block_width(int ncols, int max_w = 32) {
   int S = 1;
-  while (S < ncols && S < 32) S <<= 1;
+  while (S < ncols && S < max_w) S <<= 1;
   return S;
 }
 
@@ -637,8 +773,13 @@ void pcg_solve(cbx_handle* h, double lam, int ncols, const double* B_cm, double*
   Mme& m = *h->mme;
   CBX_REQUIRE(m.has_dense || m.has_sparse, CBX_ERR_STATE, "Qinv not set (cbx_mme_set_qinv_*)");
   res = PcgResult{};
-  for (int c0 = 0; c0 < ncols; c0 += 32) {
-    const int nc = std::min(32, ncols - c0);
+  // Mixed precision takes up to 64 columns per block: its PCG bulk reads the
+  // FP32 block once per iteration for all of them, and the FP64-class
+  // refinement products run on the populated columns only.  The FP64 solver's
+  // product is FP64-bound, so it stays at 32.
+  const int chunk = precision != 0 ? 64 : 32;
+  for (int c0 = 0; c0 < ncols; c0 += chunk) {
+    const int nc = std::min(chunk, ncols - c0);
     PcgResult r;
     const double* B = B_cm + (int64_t)c0 * m.dim;
     double* X = X_cm + (int64_t)c0 * m.dim;
@@ -646,13 +787,14 @@ void pcg_solve(cbx_handle* h, double lam, int ncols, const double* B_cm, double*
     double* ro = carry && carry->r_out ? carry->r_out + (int64_t)c0 * m.dim : nullptr;
     const double dl = carry ? carry->dlam : 0.0;
 #define CBX_CHUNK(W) solve_chunk<W>(h, m, lam, nc, B, X, use_x0, tol, maxit, abs_tol, precision, r, rp, dl, ro)
-    switch (block_width(nc)) {
+    switch (block_width(nc, chunk)) {
       case 1: CBX_CHUNK(1); break;
       case 2: CBX_CHUNK(2); break;
       case 4: CBX_CHUNK(4); break;
       case 8: CBX_CHUNK(8); break;
       case 16: CBX_CHUNK(16); break;
-      default: CBX_CHUNK(32); break;
+      case 32: CBX_CHUNK(32); break;
+      default: CBX_CHUNK(64); break;
     }
 #undef CBX_CHUNK
     res.iters.insert(res.iters.end(), r.iters.begin(), r.iters.end());
@@ -677,7 +819,7 @@ static void qinv_chunk(cbx_handle* h, Mme& m, int nc, const double* X_cm, double
                              nc, cudaMemcpyDeviceToDevice, s));
   k_to_inter<<<grid_for(n, 256, 4 * h->num_sms), 256, 0, s>>>(tmp.p, m.dim, nc, S, sv_.Xi.p);
   h->launched("k_to_inter");
-  sv_.qinv(h, m);
+  sv_.qinv(h, m, nc);
   k_from_inter<<<grid_for(m.dim * nc, 256, 4 * h->num_sms), 256, 0, s>>>(sv_.Y64.p, m.dim, nc, S, tmp.p);
   h->launched("k_from_inter");
   CBX_CUDA(cudaMemcpy2DAsync(Y_cm, m.q * sizeof(double), tmp.p + m.p, m.dim * sizeof(double), m.q * sizeof(double),
@@ -700,6 +842,34 @@ void qinv_apply(cbx_handle* h, int ncols, const double* X_cm, double* Y_cm) {
       default: qinv_chunk<32>(h, m, nc, X, Y); break;
     }
   }
+}
+
+// Y[c * q + u] = ((B - R)[c * dim + p + u] - (D X)[c * dim + p + u]) / lam: the
+// random rows of lam [0; Qinv u] = (b - r) - W'W x for a solution x whose true
+// residual r = b - A x is known.
+__global__ void k_qinv_from_solution(const int32_t* __restrict__ Dptr, const int32_t* __restrict__ Dcol,
+                                     const double* __restrict__ Dval, int64_t p, int64_t q, int64_t dim, int ncols,
+                                     const double* __restrict__ B, const double* __restrict__ X,
+                                     const double* __restrict__ R, double inv_lam, double* __restrict__ Y) {
+  const int64_t total = q * ncols;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = idx / q, u = idx - c * q, i = p + u;
+    const double* x = X + c * dim;
+    double t = 0.0;
+    for (int32_t j = Dptr[i]; j < Dptr[i + 1]; ++j) t += Dval[j] * x[Dcol[j]];
+    Y[idx] = ((B[c * dim + i] - R[c * dim + i]) - t) * inv_lam;
+  }
+}
+
+void qinv_from_solution(cbx_handle* h, double lam, int ncols, const double* B_cm, const double* X_cm,
+                        const double* R_cm, double* Y_cm) {
+  CBX_REQUIRE(h->mme, CBX_ERR_STATE, "no mixed-model equations on this handle");
+  CBX_REQUIRE(lam > 0, CBX_ERR_ARG, "lambda must be positive");
+  Mme& m = *h->mme;
+  k_qinv_from_solution<<<grid_for(m.q * ncols, 256, 4 * h->num_sms), 256, 0, h->stream>>>(
+      m.D64.ptr.p, m.D64.col.p, m.D64.val.p, m.p, m.q, m.dim, ncols, B_cm, X_cm, R_cm, 1.0 / lam, Y_cm);
+  h->launched("k_qinv_from_solution");
 }
 
 double record_residual(cbx_handle* h, const double* sol_dev, double* e_dev) {
@@ -921,6 +1091,38 @@ extern "C" int cbx_mme_create(cbx_handle* h, int64_t n_rec, int64_t p, int64_t q
   });
 }
 
+// The dense block on the device: the FP64 copy (pitch ld) and the shifted
+// low-precision copies (see Mme::qshift).  The shift
+// is the mean off-diagonal entry, summed in a fixed order.
+static void upload_dense(cbx_handle* h, Mme& m, const double* src, int64_t ng) {
+  cudaStream_t s = h->stream;
+  m.ng = ng;
+  m.ld = (ng + 3) / 4 * 4;
+  m.Qd64.resize((size_t)ng * m.ld);
+  k_pitch_copy<double><<<grid_for(ng * m.ld, 256, 8 * h->num_sms), 256, 0, s>>>(src, ng, m.ld, m.Qd64.p);
+  h->launched("k_pitch_copy");
+  double shift = 0.0;
+  if (ng > 1) {
+    const unsigned g = (unsigned)(4 * h->num_sms);
+    DevBuf<double> part;
+    part.resize(g);
+    k_offdiag_part<<<g, 256, 0, s>>>(src, ng, part.p);
+    h->launched("k_offdiag_part");
+    std::vector<double> ph(g);
+    CBX_CUDA(cudaMemcpyAsync(ph.data(), part.p, g * sizeof(double), cudaMemcpyDeviceToHost, s));
+    CBX_CUDA(cudaStreamSynchronize(s));
+    double t = 0.0;
+    for (double v : ph) t += v;
+    shift = t / ((double)ng * (double)(ng - 1));
+  }
+  m.qshift = std::isfinite(shift) ? shift : 0.0;
+  m.Qd32.resize((size_t)ng * m.ld);
+  m.Qlo32.resize((size_t)ng * m.ld);
+  k_lowp_block<<<grid_for(ng * m.ld, 256, 8 * h->num_sms), 256, 0, s>>>(src, ng, m.ld, m.qshift, m.Qd32.p,
+                                                                       m.Qlo32.p);
+  h->launched("k_lowp_block");
+}
+
 // Dense Qinv (q x q, symmetric, row- or column-major alike).  Qinv == NULL uses
 // the matrix left on the device by cbx_invert_psd.
 extern "C" int cbx_mme_set_qinv_dense(cbx_handle* h, const double* Qinv, int64_t q) {
@@ -940,17 +1142,7 @@ extern "C" int cbx_mme_set_qinv_dense(cbx_handle* h, const double* Qinv, int64_t
       CBX_REQUIRE(h->Ginv.p && h->Ginv_n == q, CBX_ERR_STATE, "no device G inverse of matching order");
       src = h->Ginv.p;
     }
-    m.ng = q;
-    m.ld = (q + 3) / 4 * 4;
-    m.Qd64.resize((size_t)q * m.ld);
-    m.Qd32.resize((size_t)q * m.ld);
-    k_pitch_copy<double><<<grid_for(q * m.ld, 256, 8 * h->num_sms), 256, 0, s>>>(src, q, m.ld, m.Qd64.p);
-    h->launched("k_pitch_copy");
-    k_pitch_copy<float><<<grid_for(q * m.ld, 256, 8 * h->num_sms), 256, 0, s>>>(src, q, m.ld, m.Qd32.p);
-    h->launched("k_pitch_copy");
-    m.Qlo32.resize((size_t)q * m.ld);
-    k_pitch_lo<<<grid_for(q * m.ld, 256, 8 * h->num_sms), 256, 0, s>>>(src, q, m.ld, m.Qlo32.p);
-    h->launched("k_pitch_lo");
+    upload_dense(h, m, src, q);
     std::vector<int32_t> idm(q);
     for (int64_t i = 0; i < q; ++i) idm[i] = (int32_t)i;
     m.gmap.resize(q);
@@ -1008,17 +1200,7 @@ extern "C" int cbx_mme_set_qinv_split(cbx_handle* h, const int64_t* a_ptr, const
       DevBuf<double> tmp;
       tmp.resize((size_t)ng * ng);
       CBX_CUDA(cudaMemcpyAsync(tmp.p, Gd, (size_t)ng * ng * sizeof(double), cudaMemcpyHostToDevice, s));
-      m.ng = ng;
-      m.ld = (ng + 3) / 4 * 4;
-      m.Qd64.resize((size_t)ng * m.ld);
-      m.Qd32.resize((size_t)ng * m.ld);
-      k_pitch_copy<double><<<grid_for(ng * m.ld, 256, 8 * h->num_sms), 256, 0, s>>>(tmp.p, ng, m.ld, m.Qd64.p);
-      h->launched("k_pitch_copy");
-      k_pitch_copy<float><<<grid_for(ng * m.ld, 256, 8 * h->num_sms), 256, 0, s>>>(tmp.p, ng, m.ld, m.Qd32.p);
-      h->launched("k_pitch_copy");
-      m.Qlo32.resize((size_t)ng * m.ld);
-      k_pitch_lo<<<grid_for(ng * m.ld, 256, 8 * h->num_sms), 256, 0, s>>>(tmp.p, ng, m.ld, m.Qlo32.p);
-      h->launched("k_pitch_lo");
+      upload_dense(h, m, tmp.p, ng);
       m.gmap.resize(ng);
       m.ginv.resize(q);
       CBX_CUDA(cudaMemcpyAsync(m.gmap.p, gmap, ng * sizeof(int32_t), cudaMemcpyHostToDevice, s));

@@ -46,8 +46,14 @@ struct Mme {
   bool has_dense = false, has_sparse = false;
   int64_t ng = 0, ld = 0;          // dense block order and row pitch (multiple of 4)
   DevBuf<double> Qd64;             // ng x ld row-major
-  DevBuf<float> Qd32;
-  DevBuf<float> Qlo32;             // fl32(Qd64 - Qd32): with Qd32 the float-float block
+  // Low-precision copies hold the block minus a constant, Qd - qshift (qshift
+  // = the mean off-diagonal entry), so that a large common offset -- an
+  // eigen-bent G^-1 adds clamp^-1 / n to every entry -- does not eat the FP32
+  // mantissa; the products add qshift * (column sum) back, the column sums
+  // taken in FP64.  ng x ld each.
+  DevBuf<float> Qd32;              // fl32(Qd - qshift)
+  DevBuf<float> Qlo32;             // fl32(Qd - qshift - Qd32): with Qd32 the float-float block
+  double qshift = 0.0;
   DevBuf<int32_t> gmap;            // ng -> u index
   DevBuf<int32_t> ginv;            // q -> dense index or -1
   Csr<double> Qs64;
@@ -78,7 +84,7 @@ struct Mme {
     probe_r_ok.clear();
   }
   // persistent solver workspaces, indexed by log2 of the RHS block width
-  std::unique_ptr<SolverBase> solvers[6];
+  std::unique_ptr<SolverBase> solvers[7];
   // scratch column-major buffers of the C ABI
   DevBuf<double> io_b, io_x;
 };

@@ -20,11 +20,10 @@ struct PcgResult {
 // residual).  abs_tol: stop on ||r|| < tol (MatrixFreePCG) instead.
 // Residual carried between mixed-precision solves of the same right-hand sides
 // at neighbouring lambdas.  r_prev (column-major dim x ncols) = b - A(lam -
-// dlam) x0 for the x0 passed in X; when |dlam| <= 2^-7 lam the initial
-// residual is formed as r_prev - dlam [0; Qinv x0_u] with the float-float
-// block product (error below that of an FP64 b - A x0), otherwise b - A x0 is
-// recomputed in FP64.  r_out receives the final residual b - A(lam) x of a
-// mixed-precision solve.  Either pointer may be null.
+// dlam) x0 for the x0 passed in X; the initial residual at lam follows from it
+// exactly with one sparse W'W product (k_carry_resid), no dense product.
+// r_out receives the final residual b - A(lam) x of a mixed-precision solve.
+// Either pointer may be null.
 struct ResidCarry {
   const double* r_prev = nullptr;
   double dlam = 0.0;
@@ -37,6 +36,14 @@ void pcg_solve(cbx_handle* h, double lam, int ncols, const double* B_cm, double*
 
 // Y = Qinv X for ncols column-major q-vectors on the device.
 void qinv_apply(cbx_handle* h, int ncols, const double* X_cm, double* Y_cm);
+
+// Y = Qinv X_u for solutions X of A(lam) X = B whose true residuals R = B - A X
+// are known (the mixed solver returns them): from A x = W'W x + lam [0; Qinv u],
+// Qinv u = ((b - r)_u - (W'W x)_u) / lam, which needs only the sparse W'W.  Its
+// error is that of r, i.e. of an FP64 residual.  Column-major: B, X, R are
+// dim x ncols, Y is q x ncols.
+void qinv_from_solution(cbx_handle* h, double lam, int ncols, const double* B_cm, const double* X_cm,
+                        const double* R_cm, double* Y_cm);
 
 // Record residual e = y - W sol (sol: dim) on the device; returns e'e.
 double record_residual(cbx_handle* h, const double* sol_dev, double* e_dev);

@@ -210,133 +210,233 @@ static double y_variance(const Mme& m) {
 }
 
 // One EM iteration (vce.cpp:1490-1574).
+//
+// The reference solves the data system, then the probe batches of the
+// adaptive trace estimator, one right-hand side at a time.  Here the probe
+// batches needed before the estimator's first check are one multi-RHS block,
+// and in mixed precision the data right-hand side joins that block (the
+// systems share the matrix, so one read of the dense block per PCG iteration
+// serves them all).  Results per column are those of separate solves: every
+// column runs its own CG recurrence and refinement.
 static void em_iteration(cbx_handle* h, const RemlConfigI& cfg, double& vu, double& ve, IterInfo& info) {
   Mme& m = *h->mme;
   cudaStream_t s = h->stream;
   const int64_t p = m.p, q = m.q, dim = m.dim, n = m.n_rec;
   const double start_vu = vu, start_ve = ve;
   const double lam = ve / std::max(vu, 1e-9);
-  // 1. data solve, warm-started from the previous data solution (and, in mixed
-  //    precision, from its residual carried to the new lambda)
+  const bool mixed = cfg.precision != 0;
   m.last_solution.resize(dim);
   m.last_resid.resize(dim);
-  PcgResult r;
-  ResidCarry dc;
-  dc.r_prev = (m.has_last && m.has_last_resid) ? m.last_resid.p : nullptr;
-  dc.dlam = lam - m.last_lam;
-  dc.r_out = m.last_resid.p;
-  pcg_solve(h, lam, 1, m.rhs.p, m.last_solution.p, m.has_last, cfg.pcg_tol, cfg.pcg_max_iter, 0, cfg.precision, r,
-            &dc);
-  m.has_last = true;
-  m.has_last_resid = cfg.precision != 0;
-  m.last_lam = lam;
-  info.pcg_iters += r.iters[0];
-  info.matvecs += r.matvecs;
-  if (r.status[0] == sv::COL_NONFINITE) throw Error(CBX_ERR_NONFINITE, "non-finite data solve");
-  // 2. residual sum of squares
-  const double e_sse = record_residual(h, m.last_solution.p, nullptr);
-  // 3. u' Qinv u
-  DevBuf<double> Qu;
-  Qu.resize(q);
-  qinv_apply(h, 1, m.last_solution.p + p, Qu.p);
-  const auto u_h = d2h(h, m.last_solution.p + p, q);
-  const auto Qu_h = d2h(h, Qu.p, q);
-  const double uQu = dot_h(u_h, Qu_h);
-  // 4. Hutchinson trace of Qinv C^uu with the reference's probe schedule
+
+  // Hutchinson schedule of the reference (vce.cpp:1266-1315,
+  // adaptive_trace_estimator.cpp:11-81): batches of 16 probes, batch b seeded
+  // seed + (first probe index), at least min_s and at most max_s probes, stop
+  // at SE / |mean| < 0.05 checked after each batch once min_s are done.
   const int n_samp = std::max(5, cfg.mc_samples / 2);
   int min_s = std::max(30, n_samp / 3), max_s = std::max(100, n_samp);
   if (min_s <= 0) min_s = 10;
   if (max_s < min_s) max_s = min_s;
   const int batch = 16;  // max(16, 4 * threads) with one thread
-  double tsum = 0, tsq = 0;
-  int done = 0;
-  DevBuf<double> B, X, QW;
-  bool stop = false;
-  while (done < max_s && !stop) {
-    // solve as many consecutive batches at once as are needed before the next check
+  if (m.probe_seed != cfg.seed) {
+    m.probe_lam.clear();
+    m.probe_r_ok.clear();
+    m.probe_seed = cfg.seed;
+  }
+  const size_t cap = (size_t)dim * max_s;
+  if (m.probe_x.n < cap) {
+    m.probe_x.resize(cap);
+    m.probe_r.resize(cap);
+    m.probe_lam.clear();
+    m.probe_r_ok.clear();
+  }
+
+  // the probe group starting at `done`: batches solved before the next check
+  struct Group {
     std::vector<std::pair<int, int>> batches;  // (start, size)
+    int k = 0;
+    std::vector<double> Z;                     // q x k
+  };
+  auto make_group = [&](int done) {
+    Group g;
     int next = done;
     do {
       const int sz = std::min(batch, max_s - next);
-      batches.push_back({next, sz});
+      g.batches.push_back({next, sz});
       next += sz;
     } while (next < min_s && next < max_s);
-    const int k = next - done;
-    std::vector<double> Bh((size_t)dim * k, 0.0);
-    std::vector<double> Z((size_t)q * k);
+    g.k = next - done;
+    g.Z.resize((size_t)q * g.k);
     int col = 0;
-    for (auto& bt : batches) {
+    for (auto& bt : g.batches) {
       std::mt19937_64 gen((unsigned long)(cfg.seed + bt.first));
       std::uniform_int_distribution<int> dist(0, 1);
       for (int j = 0; j < bt.second; ++j, ++col)
-        for (int64_t i = 0; i < q; ++i) {
-          const double z = dist(gen) == 0 ? -1.0 : 1.0;
-          Z[(size_t)col * q + i] = z;
-          Bh[(size_t)col * dim + p + i] = z;
-        }
+        for (int64_t i = 0; i < q; ++i) g.Z[(size_t)col * q + i] = dist(gen) == 0 ? -1.0 : 1.0;
     }
-    B.resize((size_t)dim * k);
-    X.resize((size_t)dim * k);
-    QW.resize((size_t)q * k);
-    CBX_CUDA(cudaMemcpyAsync(B.p, Bh.data(), Bh.size() * sizeof(double), cudaMemcpyHostToDevice, s));
-    // The probe stream restarts at the same seed every REML iteration, so the
-    // previous iteration's solutions of these probes are a warm start (and,
-    // in mixed precision, their residuals carry to the new lambda when all
-    // columns share one previous lambda).
-    if (m.probe_seed != cfg.seed) {
-      m.probe_lam.clear();
-      m.probe_r_ok.clear();
-      m.probe_seed = cfg.seed;
-    }
-    const size_t cap = (size_t)dim * max_s;
-    if (m.probe_x.n < cap) {
-      m.probe_x.resize(cap);
-      m.probe_r.resize(cap);
-      m.probe_lam.clear();
-      m.probe_r_ok.clear();
-    }
-    const bool warm = (int)m.probe_lam.size() >= done + k;
-    bool carry_ok = warm;
-    if (warm)
-      for (int c = done; c < done + k; ++c)
-        carry_ok = carry_ok && m.probe_r_ok[c] && m.probe_lam[c] == m.probe_lam[done];
-    if (warm)
-      CBX_CUDA(cudaMemcpyAsync(X.p, m.probe_x.p + (size_t)done * dim, (size_t)dim * k * sizeof(double),
-                               cudaMemcpyDeviceToDevice, s));
-    ResidCarry pc;
-    pc.r_prev = carry_ok ? m.probe_r.p + (size_t)done * dim : nullptr;
-    pc.dlam = carry_ok ? lam - m.probe_lam[done] : 0.0;
-    pc.r_out = m.probe_r.p + (size_t)done * dim;
-    PcgResult pr;
-    pcg_solve(h, lam, k, B.p, X.p, warm, cfg.pcg_tol, cfg.pcg_max_iter, 0, cfg.precision, pr, &pc);
-    CBX_CUDA(cudaMemcpyAsync(m.probe_x.p + (size_t)done * dim, X.p, (size_t)dim * k * sizeof(double),
-                             cudaMemcpyDeviceToDevice, s));
+    return g;
+  };
+  // The probe stream restarts at the same seed every REML iteration, so the
+  // previous iteration's solutions of these probes are a warm start, and in
+  // mixed precision their residuals carry to the new lambda.
+  auto probes_warm = [&](int done, int k) { return (int)m.probe_lam.size() >= done + k; };
+  auto probes_carry = [&](int done, int k) {
+    bool ok = probes_warm(done, k);
+    if (ok)
+      for (int c = done; c < done + k; ++c) ok = ok && m.probe_r_ok[c] && m.probe_lam[c] == m.probe_lam[done];
+    return ok;
+  };
+  auto record_probes = [&](int done, int k) {
     if ((int)m.probe_lam.size() < done + k) {
       m.probe_lam.resize(done + k);
       m.probe_r_ok.resize(done + k);
     }
     for (int c = done; c < done + k; ++c) {
       m.probe_lam[c] = lam;
-      m.probe_r_ok[c] = cfg.precision != 0;
+      m.probe_r_ok[c] = mixed;
     }
-    for (int c = 0; c < k; ++c) {
+  };
+  auto count = [&](const PcgResult& pr, int c0, int k, const char* what) {
+    for (int c = c0; c < c0 + k; ++c) {
       info.pcg_iters += pr.iters[c];
-      if (pr.status[c] == sv::COL_NONFINITE) throw Error(CBX_ERR_NONFINITE, "non-finite probe solve");
+      if (pr.status[c] == sv::COL_NONFINITE) throw Error(CBX_ERR_NONFINITE, what);
     }
+  };
+
+  int done = 0;
+  Group g0 = make_group(0);
+  DevBuf<double> B, X, QW;
+  // --- 1. the data solve (with the first probe group in mixed precision)
+  const bool data_warm = m.has_last;
+  const bool merge = mixed && data_warm == probes_warm(0, g0.k);
+  if (merge) {
+    const int k = g0.k, nc = 1 + k;
+    std::vector<double> Bh((size_t)dim * nc, 0.0);
+    CBX_CUDA(cudaMemcpyAsync(Bh.data(), m.rhs.p, dim * sizeof(double), cudaMemcpyDeviceToHost, s));
+    CBX_CUDA(cudaStreamSynchronize(s));
+    for (int c = 0; c < k; ++c)
+      for (int64_t i = 0; i < q; ++i) Bh[(size_t)(1 + c) * dim + p + i] = g0.Z[(size_t)c * q + i];
+    B.resize((size_t)dim * nc);
+    X.resize((size_t)dim * nc);
+    DevBuf<double> R;
+    R.resize((size_t)dim * nc);
+    CBX_CUDA(cudaMemcpyAsync(B.p, Bh.data(), Bh.size() * sizeof(double), cudaMemcpyHostToDevice, s));
+    const bool carry = data_warm && m.has_last_resid && probes_carry(0, k) && m.last_lam == m.probe_lam[0];
+    if (data_warm) {
+      CBX_CUDA(cudaMemcpyAsync(X.p, m.last_solution.p, dim * sizeof(double), cudaMemcpyDeviceToDevice, s));
+      CBX_CUDA(cudaMemcpyAsync(X.p + dim, m.probe_x.p, (size_t)dim * k * sizeof(double), cudaMemcpyDeviceToDevice,
+                               s));
+      if (carry) {
+        CBX_CUDA(cudaMemcpyAsync(R.p, m.last_resid.p, dim * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        CBX_CUDA(cudaMemcpyAsync(R.p + dim, m.probe_r.p, (size_t)dim * k * sizeof(double),
+                                 cudaMemcpyDeviceToDevice, s));
+      }
+    }
+    ResidCarry rc;
+    rc.r_prev = carry ? R.p : nullptr;
+    rc.dlam = carry ? lam - m.last_lam : 0.0;
+    rc.r_out = R.p;
+    PcgResult pr;
+    pcg_solve(h, lam, nc, B.p, X.p, data_warm, cfg.pcg_tol, cfg.pcg_max_iter, 0, cfg.precision, pr, &rc);
+    if (h->trace_on) h->trace_mark("#em: data + probe solve");
     info.matvecs += pr.matvecs;
-    // Qinv C^uu z for each probe: gather the u rows (strided by dim) into q x k
-    DevBuf<double> Wu;
-    Wu.resize((size_t)q * k);
-    CBX_CUDA(cudaMemcpy2DAsync(Wu.p, q * sizeof(double), X.p + p, dim * sizeof(double), q * sizeof(double), k,
+    count(pr, 0, 1, "non-finite data solve");
+    count(pr, 1, k, "non-finite probe solve");
+    CBX_CUDA(cudaMemcpyAsync(m.last_solution.p, X.p, dim * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    CBX_CUDA(cudaMemcpyAsync(m.last_resid.p, R.p, dim * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    CBX_CUDA(cudaMemcpyAsync(m.probe_x.p, X.p + dim, (size_t)dim * k * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    CBX_CUDA(cudaMemcpyAsync(m.probe_r.p, R.p + dim, (size_t)dim * k * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    record_probes(0, k);
+  } else {
+    // data solve alone, warm-started from the previous data solution (and, in
+    // mixed precision, from its residual carried to the new lambda)
+    PcgResult r;
+    ResidCarry dc;
+    dc.r_prev = (m.has_last && m.has_last_resid) ? m.last_resid.p : nullptr;
+    dc.dlam = lam - m.last_lam;
+    dc.r_out = m.last_resid.p;
+    pcg_solve(h, lam, 1, m.rhs.p, m.last_solution.p, m.has_last, cfg.pcg_tol, cfg.pcg_max_iter, 0, cfg.precision,
+              r, &dc);
+    if (h->trace_on) h->trace_mark("#em: data solve");
+    info.matvecs += r.matvecs;
+    count(r, 0, 1, "non-finite data solve");
+  }
+  m.has_last = true;
+  m.has_last_resid = mixed;
+  m.last_lam = lam;
+  // --- 2. residual sum of squares
+  const double e_sse = record_residual(h, m.last_solution.p, nullptr);
+  // --- 3. u' Qinv u
+  DevBuf<double> Qu;
+  Qu.resize(q);
+  if (mixed)
+    qinv_from_solution(h, lam, 1, m.rhs.p, m.last_solution.p, m.last_resid.p, Qu.p);
+  else
+    qinv_apply(h, 1, m.last_solution.p + p, Qu.p);
+  const auto u_h = d2h(h, m.last_solution.p + p, q);
+  const auto Qu_h = d2h(h, Qu.p, q);
+  const double uQu = dot_h(u_h, Qu_h);
+  if (h->trace_on) h->trace_mark("#em: e'e and u'Qinv u");
+  // --- 4. Hutchinson trace of Qinv C^uu
+  double tsum = 0, tsq = 0;
+  bool stop = false;
+  bool first = true;
+  while (done < max_s && !stop) {
+    Group g = first ? std::move(g0) : make_group(done);
+    const int k = g.k;
+    // B / X / residual columns of this group (dim x k each)
+    const double *Bg, *Xg, *Rg;
+    DevBuf<double> Bp, Xp;
+    if (first && merge) {
+      Bg = B.p + dim;
+      Xg = m.probe_x.p;
+      Rg = m.probe_r.p;
+    } else {
+      std::vector<double> Bh((size_t)dim * k, 0.0);
+      for (int c = 0; c < k; ++c)
+        for (int64_t i = 0; i < q; ++i) Bh[(size_t)c * dim + p + i] = g.Z[(size_t)c * q + i];
+      Bp.resize((size_t)dim * k);
+      Xp.resize((size_t)dim * k);
+      CBX_CUDA(cudaMemcpyAsync(Bp.p, Bh.data(), Bh.size() * sizeof(double), cudaMemcpyHostToDevice, s));
+      const bool warm = probes_warm(done, k), carry = probes_carry(done, k);
+      if (warm)
+        CBX_CUDA(cudaMemcpyAsync(Xp.p, m.probe_x.p + (size_t)done * dim, (size_t)dim * k * sizeof(double),
+                                 cudaMemcpyDeviceToDevice, s));
+      ResidCarry pc;
+      pc.r_prev = carry ? m.probe_r.p + (size_t)done * dim : nullptr;
+      pc.dlam = carry ? lam - m.probe_lam[done] : 0.0;
+      pc.r_out = m.probe_r.p + (size_t)done * dim;
+      PcgResult pr;
+      pcg_solve(h, lam, k, Bp.p, Xp.p, warm, cfg.pcg_tol, cfg.pcg_max_iter, 0, cfg.precision, pr, &pc);
+      if (h->trace_on) h->trace_mark("#em: probe solve");
+      CBX_CUDA(cudaMemcpyAsync(m.probe_x.p + (size_t)done * dim, Xp.p, (size_t)dim * k * sizeof(double),
                                cudaMemcpyDeviceToDevice, s));
-    qinv_apply(h, k, Wu.p, QW.p);
+      record_probes(done, k);
+      count(pr, 0, k, "non-finite probe solve");
+      info.matvecs += pr.matvecs;
+      Bg = Bp.p;
+      Xg = Xp.p;
+      Rg = m.probe_r.p + (size_t)done * dim;
+    }
+    first = false;
+    // Qinv C^uu z for each probe: from the solutions and their true residuals
+    // in mixed precision, else the product with the u rows (strided by dim)
+    QW.resize((size_t)q * k);
+    if (mixed) {
+      qinv_from_solution(h, lam, k, Bg, Xg, Rg, QW.p);
+    } else {
+      DevBuf<double> Wu;
+      Wu.resize((size_t)q * k);
+      CBX_CUDA(cudaMemcpy2DAsync(Wu.p, q * sizeof(double), Xg + p, dim * sizeof(double), q * sizeof(double), k,
+                                 cudaMemcpyDeviceToDevice, s));
+      qinv_apply(h, k, Wu.p, QW.p);
+    }
     const auto QWh = d2h(h, QW.p, (size_t)q * k);
-    col = 0;
-    for (auto& bt : batches) {
+    int col = 0;
+    for (auto& bt : g.batches) {
       double bs = 0, bq = 0;
       for (int j = 0; j < bt.second; ++j, ++col) {
         double v = 0;
-        for (int64_t i = 0; i < q; ++i) v += Z[(size_t)col * q + i] * QWh[(size_t)col * q + i];
+        for (int64_t i = 0; i < q; ++i) v += g.Z[(size_t)col * q + i] * QWh[(size_t)col * q + i];
         bs += v;
         bq += v * v;
       }
@@ -352,7 +452,7 @@ static void em_iteration(cbx_handle* h, const RemlConfigI& cfg, double& vu, doub
     }
   }
   const double tr = tsum / done;
-  // 5. updates (vce.cpp:1554-1569)
+  // --- 5. updates (vce.cpp:1554-1569)
   const double y_var = y_variance(m);
   const double vu_new = (uQu + tr * start_ve) / (double)q;
   vu = stabilize(vu_new, start_vu, y_var);
@@ -386,12 +486,23 @@ static void reml_gradient(cbx_handle* h, double vu, double ve, int nprobe, int s
   DevBuf<double> sol;
   sol.resize(dim);
   PcgResult r;
-  pcg_solve(h, lam, 1, m.rhs.p, sol.p, false, pcg_tol, pcg_maxit, 0, precision, r);
+  // mixed precision returns the true residual, from which Qinv u follows
+  // without a dense product (qinv_from_solution)
+  DevBuf<double> res;
+  ResidCarry rc;
+  if (precision != 0) {
+    res.resize(dim);
+    rc.r_out = res.p;
+  }
+  pcg_solve(h, lam, 1, m.rhs.p, sol.p, false, pcg_tol, pcg_maxit, 0, precision, r, &rc);
   iters += r.iters[0];
   const double e_sse = record_residual(h, sol.p, nullptr);
   DevBuf<double> Qu;
   Qu.resize(q);
-  qinv_apply(h, 1, sol.p + p, Qu.p);
+  if (precision != 0)
+    qinv_from_solution(h, lam, 1, m.rhs.p, sol.p, res.p, Qu.p);
+  else
+    qinv_apply(h, 1, sol.p + p, Qu.p);
   const double uQu = dot_h(d2h(h, sol.p + p, q), d2h(h, Qu.p, q));
   const int64_t total = exact ? q : nprobe;
   CBX_REQUIRE(total > 0, CBX_ERR_ARG, "nprobe must be positive");
@@ -417,18 +528,27 @@ static void reml_gradient(cbx_handle* h, double vu, double ve, int nprobe, int s
         }
       }
     }
-    DevBuf<double> B, X, Wu, QW;
+    DevBuf<double> B, X, Wu, QW, R;
     B.resize((size_t)dim * k);
     X.resize((size_t)dim * k);
-    Wu.resize((size_t)q * k);
     QW.resize((size_t)q * k);
     CBX_CUDA(cudaMemcpyAsync(B.p, Bh.data(), Bh.size() * sizeof(double), cudaMemcpyHostToDevice, s));
     PcgResult pr;
-    pcg_solve(h, lam, k, B.p, X.p, false, pcg_tol, pcg_maxit, 0, precision, pr);
+    ResidCarry pc;
+    if (precision != 0) {
+      R.resize((size_t)dim * k);
+      pc.r_out = R.p;
+    }
+    pcg_solve(h, lam, k, B.p, X.p, false, pcg_tol, pcg_maxit, 0, precision, pr, &pc);
     for (int c = 0; c < k; ++c) iters += pr.iters[c];
-    CBX_CUDA(cudaMemcpy2DAsync(Wu.p, q * sizeof(double), X.p + p, dim * sizeof(double), q * sizeof(double), k,
-                               cudaMemcpyDeviceToDevice, s));
-    qinv_apply(h, k, Wu.p, QW.p);
+    if (precision != 0) {
+      qinv_from_solution(h, lam, k, B.p, X.p, R.p, QW.p);
+    } else {
+      Wu.resize((size_t)q * k);
+      CBX_CUDA(cudaMemcpy2DAsync(Wu.p, q * sizeof(double), X.p + p, dim * sizeof(double), q * sizeof(double), k,
+                                 cudaMemcpyDeviceToDevice, s));
+      qinv_apply(h, k, Wu.p, QW.p);
+    }
     const auto QWh = d2h(h, QW.p, (size_t)q * k);
     for (int j = 0; j < k; ++j) {
       double v = 0;

@@ -97,7 +97,7 @@ extern "C" int cbx_selftest_umma(cbx_handle* h, const float* A, const float* B, 
 extern "C" int cbx_selftest_dense_tc(cbx_handle* h, const float* Q, int64_t ng, int64_t ld, const float* V,
                                      int32_t S, float* Y) {
   return cbx_guard(h, [&] {
-    CBX_REQUIRE(S == 16 || S == 32, CBX_ERR_ARG, "S must be 16 or 32");
+    CBX_REQUIRE(S == 16 || S == 32 || S == 64, CBX_ERR_ARG, "S must be 16, 32 or 64");
     CBX_REQUIRE(ng > 0 && ld > 0 && ld % 4 == 0, CBX_ERR_ARG, "bad block shape");
     CBX_CUDA(cudaSetDevice(h->device));
     cbx::DevBuf<float> dQ, dV, dT;

@@ -46,27 +46,29 @@ __device__ __forceinline__ double dot16(const double2& a, const double2& b) {
   return a.x * b.x + a.y * b.y;
 }
 
-// Vt[c * ld + k] = X[(p + gmap[k]) * S + c] for k < ng, 0 for ng <= k < ld.
+// Vt[c * ld + k] = X[(p + gmap[k]) * xs + c] for k < ng, 0 for ng <= k < ld
+// (S columns of a block whose rows are xs apart; xs = S for the whole block).
 template <typename T, int S>
 __global__ void k_gather_t(const T* __restrict__ X, T* __restrict__ Vt, int64_t p, int64_t ng,
                            int64_t ld, const int32_t* __restrict__ gmap,
-                           const int* __restrict__ active) {
+                           const int* __restrict__ active, int xs = S) {
   if (active && *active == 0) return;
   const int64_t total = (int64_t)S * ld;
   for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
        idx += (int64_t)gridDim.x * blockDim.x) {
     const int64_t c = idx / ld, k = idx - c * ld;
-    Vt[idx] = k < ng ? X[(p + gmap[k]) * S + c] : T(0);
+    Vt[idx] = k < ng ? X[(p + gmap[k]) * xs + c] : T(0);
   }
 }
 
-// Dense block product Tout[i * S + c] = sum_k Qd[i * ld + k] * Vt[c * ld + k].
+// Dense block product Tout[i * os + c] = sum_k Qd[i * ld + k] * Vt[c * ld + k]
+// (os = S unless the S columns are a piece of a wider block).
 // 8 warps per block, RPW rows per warp; lanes stream 16-byte vectors of each
 // row; the S right-hand sides of a K tile are staged in shared memory.
 template <typename T, int S, int RPW>
 __global__ void __launch_bounds__(256) k_dense(const T* __restrict__ Qd, int64_t ng, int64_t ld,
                                                const T* __restrict__ Vt, T* __restrict__ Tout,
-                                               const int* __restrict__ active) {
+                                               const int* __restrict__ active, int os = S) {
   if (active && *active == 0) return;
   using V = typename Vec16<T>::type;
   constexpr int VEC = Vec16<T>::n;
@@ -120,7 +122,7 @@ __global__ void __launch_bounds__(256) k_dense(const T* __restrict__ Qd, int64_t
     }
     if (lane == 0 && row0 + r < ng) {
 #pragma unroll
-      for (int c = 0; c < S; ++c) Tout[(row0 + r) * S + c] = acc[r][c];
+      for (int c = 0; c < S; ++c) Tout[(row0 + r) * os + c] = acc[r][c];
     }
   }
 }
@@ -131,7 +133,7 @@ __global__ void __launch_bounds__(256) k_dense(const T* __restrict__ Qd, int64_t
 template <typename T, int RPW, int U>
 __global__ void __launch_bounds__(256) k_gemv(const T* __restrict__ Qd, int64_t ng, int64_t ld,
                                               const T* __restrict__ v, T* __restrict__ Tout,
-                                              const int* __restrict__ active) {
+                                              const int* __restrict__ active, int os = 1) {
   if (active && *active == 0) return;
   using V = typename Vec16<T>::type;
   constexpr int VEC = Vec16<T>::n;
@@ -172,7 +174,7 @@ __global__ void __launch_bounds__(256) k_gemv(const T* __restrict__ Qd, int64_t 
     T t = acc[r];
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) t += __shfl_xor_sync(0xffffffffu, t, off);
-    if (lane == 0 && row0 + r < ng) Tout[row0 + r] = t;
+    if (lane == 0 && row0 + r < ng) Tout[(row0 + r) * os] = t;
   }
 }
 
@@ -223,15 +225,69 @@ __device__ __forceinline__ void ff_norm(float& hi, float& lo) {
 // once here so that the product kernel does no FP64 arithmetic.
 template <int S>
 __global__ void k_gather_hl(const double* __restrict__ X, float2* __restrict__ Vhl, int64_t p, int64_t ng,
-                            int64_t ld, const int32_t* __restrict__ gmap) {
+                            int64_t ld, const int32_t* __restrict__ gmap, int xs = S) {
   const int64_t total = (int64_t)S * ld;
   for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
        idx += (int64_t)gridDim.x * blockDim.x) {
     const int64_t c = idx / ld, k = idx - c * ld;
-    const double x = k < ng ? X[(p + gmap[k]) * S + c] : 0.0;
+    const double x = k < ng ? X[(p + gmap[k]) * xs + c] : 0.0;
     const float xh = __double2float_rn(x);
     Vhl[idx] = make_float2(xh, __double2float_rn(x - (double)xh));
   }
+}
+
+// out[c] = sum_k X[(p + gmap[k]) * xs + c] over the dense-block rows, in FP64
+// with Neumaier compensation (the column sums that restore the shift of the
+// float-float block: the sum cancels almost completely for a solution with a
+// small component along an eigen-bent direction, so plain summation would
+// lose the digits that the shift multiplies).  One block of 256 threads per
+// column, combined in a fixed order.
+__device__ __forceinline__ void two_sum_acc(double& s, double& e, double x) {
+  const double t = __dadd_rn(s, x);
+  const double z = __dsub_rn(t, s);
+  e = __dadd_rn(e, __dadd_rn(__dsub_rn(s, __dsub_rn(t, z)), __dsub_rn(x, z)));
+  s = t;
+}
+static __global__ void __launch_bounds__(256) k_colsum_x(const double* __restrict__ X, int xs, int64_t p,
+                                                         int64_t ng, const int32_t* __restrict__ gmap,
+                                                         double* __restrict__ out) {
+  __shared__ double rs[256], re[256];
+  const int c = blockIdx.x, tid = threadIdx.x;
+  double s = 0.0, e = 0.0;
+  for (int64_t k = tid; k < ng; k += 256) two_sum_acc(s, e, X[(p + gmap[k]) * xs + c]);
+  rs[tid] = s;
+  re[tid] = e;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (tid < o) {
+      double a = rs[tid], ea = re[tid];
+      two_sum_acc(a, ea, rs[tid + o]);
+      rs[tid] = a;
+      re[tid] = __dadd_rn(ea, re[tid + o]);
+    }
+    __syncthreads();
+  }
+  if (tid == 0) out[c] = __dadd_rn(rs[0], re[0]);
+}
+
+// out[c] = sum_k Vt[c * ld + k] (k < ng) in FP64: the column sums of the
+// gathered vectors of an FP32 product with the shifted block (FP64 holds the
+// sum of FP32 values with 29 spare bits, so cancellation costs nothing that
+// the FP32 solve can see).  One block of 256 threads per column, fixed order.
+template <typename T>
+__global__ void __launch_bounds__(256) k_colsum_vt(const T* __restrict__ Vt, int64_t ld, int64_t ng,
+                                                   double* __restrict__ out) {
+  __shared__ double red[256];
+  const int c = blockIdx.x, tid = threadIdx.x;
+  double acc = 0.0;
+  for (int64_t k = tid; k < ng; k += 256) acc += (double)Vt[(int64_t)c * ld + k];
+  red[tid] = acc;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (tid < o) red[tid] += red[tid + o];
+    __syncthreads();
+  }
+  if (tid == 0) out[c] = red[0];
 }
 
 // Tout[i * S + c] = sum_k Qd[i][k] V[c][k] in float-float; Qh / Ql are the
@@ -241,7 +297,8 @@ __global__ void k_gather_hl(const double* __restrict__ X, float2* __restrict__ V
 template <int S, int RPW>
 __global__ void __launch_bounds__(256) k_dense_ff(const float* __restrict__ Qh, const float* __restrict__ Ql,
                                                   int64_t ng, int64_t ld, const float2* __restrict__ Vhl,
-                                                  double* __restrict__ Tout, const int* __restrict__ active) {
+                                                  double* __restrict__ Tout, const int* __restrict__ active,
+                                                  int os = S) {
   if (active && *active == 0) return;
   constexpr int KT = 32 * 4 * 2;
   extern __shared__ __align__(16) uint8_t dsm[];
@@ -310,7 +367,7 @@ __global__ void __launch_bounds__(256) k_dense_ff(const float* __restrict__ Qh, 
     }
     if (lane == 0 && row0 + r < ng) {
 #pragma unroll
-      for (int c = 0; c < S; ++c) Tout[(row0 + r) * S + c] = (double)hi[r][c] + (double)lo[r][c];
+      for (int c = 0; c < S; ++c) Tout[(row0 + r) * os + c] = (double)hi[r][c] + (double)lo[r][c];
     }
   }
 }
@@ -320,6 +377,16 @@ __global__ void __launch_bounds__(256) k_dense_ff(const float* __restrict__ Qh, 
 template <int S>
 __device__ __forceinline__ double block_sum_cols(double v, double* red /*[NT]*/) {
   const int tid = threadIdx.x;
+  if constexpr (S > 32) {
+    // a warp spans part of one column set: sum the S-strided threads directly
+    red[tid] = v;
+    __syncthreads();
+    double t = 0.0;
+    if (tid < S)
+      for (int w = 0; w < (int)blockDim.x / S; ++w) t += red[w * S + tid];
+    __syncthreads();
+    return t;
+  }
 #pragma unroll
   for (int off = 16; off >= S; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
   // now lanes < S of each warp hold that warp's per-column sums
@@ -369,11 +436,15 @@ __global__ void __launch_bounds__(NT) k_fix_seg(OpView<T> op, const int32_t* __r
 }
 
 // Y = use_D * D X + lam * [0; Qs X_u + scatter(Tout)]; optional pq partials sum_i P[i]Y[i].
+// Tout holds tsplit partial products (ng x S each).  When colsum is given the
+// product was taken with the shifted block Qd - tshift, and tshift * colsum[c]
+// (colsum: the column sums of the gathered block rows) is added back.
 // Blocks [0, nfix) take fixed-effect rows (one block per row); the others take
 // random-effect rows, one warp per row, in a grid-stride loop.
 template <typename T, int S>
 __global__ void __launch_bounds__(NT) k_spmv(OpView<T> op, const T* __restrict__ X,
                                              const T* __restrict__ Tout, int tsplit,
+                                             const double* __restrict__ colsum, double tshift,
                                              const int32_t* __restrict__ fix_seg_ptr,
                                              const T* __restrict__ seg_part, T lam, int use_D,
                                              T* __restrict__ Y, const T* __restrict__ P,
@@ -403,6 +474,70 @@ __global__ void __launch_bounds__(NT) k_spmv(OpView<T> op, const T* __restrict__
       Y[i * S + tid] = t;
       if (P) pq = (double)P[i * S + tid] * (double)t;
     }
+  } else if constexpr (S > 32) {
+    // one warp per row, CPL columns per lane (c = lane + 32 j)
+    constexpr int CPL = S / 32;
+    double pqv[CPL];
+#pragma unroll
+    for (int j = 0; j < CPL; ++j) pqv[j] = 0.0;
+    const int64_t nwarps = (int64_t)(gridDim.x - nfix) * (NT / 32);
+    for (int64_t i = p + (int64_t)(blockIdx.x - nfix) * (NT / 32) + warp; i < op.dim; i += nwarps) {
+      T acc[CPL], qv[CPL];
+#pragma unroll
+      for (int j = 0; j < CPL; ++j) acc[j] = qv[j] = T(0);
+      if (use_D) {
+        for (int32_t e = op.Dptr[i]; e < op.Dptr[i + 1]; ++e) {
+          const T dv = op.Dval[e];
+          const T* xr = X + (int64_t)op.Dcol[e] * S + lane;
+#pragma unroll
+          for (int j = 0; j < CPL; ++j) acc[j] += dv * xr[32 * j];
+        }
+      }
+      const int64_t u = i - p;
+      if (op.Sptr) {
+        for (int32_t e = op.Sptr[u]; e < op.Sptr[u + 1]; ++e) {
+          const T sv = op.Sval[e];
+          const T* xr = X + (p + op.Scol[e]) * S + lane;
+#pragma unroll
+          for (int j = 0; j < CPL; ++j) qv[j] += sv * xr[32 * j];
+        }
+      }
+      if (op.Qd) {
+        const int32_t k = op.ginv[u];
+        if (k >= 0) {
+          for (int t = 0; t < tsplit; ++t) {
+            const T* tr = Tout + ((int64_t)t * op.ng + k) * S + lane;
+#pragma unroll
+            for (int j = 0; j < CPL; ++j) qv[j] += tr[32 * j];
+          }
+          if (colsum) {
+#pragma unroll
+            for (int j = 0; j < CPL; ++j) qv[j] += (T)(tshift * colsum[lane + 32 * j]);
+          }
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < CPL; ++j) {
+        const T yv = acc[j] + lam * qv[j];
+        Y[i * S + lane + 32 * j] = yv;
+        if (P) pqv[j] += (double)P[i * S + lane + 32 * j] * (double)yv;
+      }
+    }
+    if (pq_part) {
+      // per column: the 8 warps' sums in warp order
+#pragma unroll
+      for (int j = 0; j < CPL; ++j) {
+        red[tid] = pqv[j];
+        __syncthreads();
+        if (tid < 32) {
+          double t = 0.0;
+          for (int w = 0; w < NT / 32; ++w) t += red[w * 32 + tid];
+          pq_part[(int64_t)blockIdx.x * S + 32 * j + tid] = t;
+        }
+        __syncthreads();
+      }
+    }
+    return;
   } else {
     constexpr int G = 32 / S;
     const int c = lane % S, g = lane / S;
@@ -430,6 +565,7 @@ __global__ void __launch_bounds__(NT) k_spmv(OpView<T> op, const T* __restrict__
           if (k >= 0) {
             // K-split partial sums of the dense block product, in a fixed order
             for (int t = 0; t < tsplit; ++t) qv += Tout[((int64_t)t * op.ng + k) * S + c];
+            if (colsum) qv += (T)(tshift * colsum[c]);
           }
         }
         const T yv = acc + lam * qv;

@@ -66,10 +66,14 @@ def test_em_iteration_matches_oracle(handle, prob, precision):
     assert relerr(r.var_e, o.var_e) < 1e-6
 
 
-def test_em_solve_three_iterations(handle, prob):
+@pytest.mark.parametrize("precision", [FP64, MIXED])
+def test_em_solve_three_iterations(handle, prob, precision):
+    """Consecutive EM iterations: from the second on, the data and probe
+    solves are warm-started from the previous iteration and (mixed precision)
+    their residuals are carried to the new lambda."""
     o = OracleREML(prob["mme"], prob["Gi"], 1.0, 1.0, max_iter=3)
     o.solve(dense_exact=False)
-    r = AIREML(dev(handle, prob), 1.0, 1.0, RemlConfig.default(mode=MODE_EM, max_iter=3))
+    r = AIREML(dev(handle, prob), 1.0, 1.0, RemlConfig.default(mode=MODE_EM, max_iter=3, precision=precision))
     r.solve()
     assert r.iterations == o.iterations
     assert relerr(r.var_u, o.var_u) < 1e-6
