@@ -337,17 +337,17 @@ void dense_tc(cbx_handle* h, const float* Qd, int64_t ng, int64_t ld, const floa
   const int grid = std::min(nunits, h->num_sms);
   if (S == 64) {
     constexpr int SM = dtc::Layout<64>::SMEM;
-    CBX_CUDA(cudaFuncSetAttribute(dtc::k_dense_tf32<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, SM));
+    ensure_smem((const void*)dtc::k_dense_tf32<64>, SM, h->device);
     dtc::k_dense_tf32<64><<<grid, dtc::THREADS, SM, h->stream>>>(ma, mb, (int)ng, ksteps, ksplit, kps, nunits, Tpart,
                                                                  active, h->status.p);
   } else if (S == 32) {
     constexpr int SM = dtc::Layout<32>::SMEM;
-    CBX_CUDA(cudaFuncSetAttribute(dtc::k_dense_tf32<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, SM));
+    ensure_smem((const void*)dtc::k_dense_tf32<32>, SM, h->device);
     dtc::k_dense_tf32<32><<<grid, dtc::THREADS, SM, h->stream>>>(ma, mb, (int)ng, ksteps, ksplit, kps, nunits, Tpart,
                                                                  active, h->status.p);
   } else {
     constexpr int SM = dtc::Layout<16>::SMEM;
-    CBX_CUDA(cudaFuncSetAttribute(dtc::k_dense_tf32<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, SM));
+    ensure_smem((const void*)dtc::k_dense_tf32<16>, SM, h->device);
     dtc::k_dense_tf32<16><<<grid, dtc::THREADS, SM, h->stream>>>(ma, mb, (int)ng, ksteps, ksplit, kps, nunits, Tpart,
                                                                  active, h->status.p);
   }

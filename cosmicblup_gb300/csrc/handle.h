@@ -8,6 +8,9 @@
 #include "devbuf.h"
 #include "mme.h"
 #include <memory>
+#include <mutex>
+#include <set>
+#include <tuple>
 
 
 struct cbx_handle {
@@ -71,6 +74,19 @@ struct cbx_handle {
   // read the device status word, reset it, and throw on a device-side failure
   void check_status(const char* what);
 };
+
+// cudaFuncSetAttribute(MaxDynamicSharedMemorySize) once per (kernel, device,
+// size): later calls make no API call, so launch sequences that may be
+// captured into a CUDA graph contain only stream work.
+inline void ensure_smem(const void* fn, int bytes, int device) {
+  static std::mutex mu;
+  static std::set<std::tuple<const void*, int, int>> done;
+  std::lock_guard<std::mutex> lk(mu);
+  const auto key = std::make_tuple(fn, device, bytes);
+  if (done.count(key)) return;
+  CBX_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  done.insert(key);
+}
 
 // Run fn, translating exceptions to status codes stored in h->last_error.
 template <typename F>

@@ -241,7 +241,7 @@ struct Workspace {
     R.resize(n); Z.resize(n); P.resize(n); Q.resize(n); X.resize(n);
     if (m.has_dense) { Vt.resize((size_t)S * m.ld); Tout.resize((size_t)m.ng * S * 8); colsum.resize(S); }
     nblk_vec = (int)grid_for(n, sv::NT, 2 * num_sms);
-    nblk_spmv = (int)m.p + (int)grid_for(m.dim - m.p, 8, 8 * num_sms);
+    nblk_spmv = (int)m.p + (int)grid_for(m.dim - m.p, 8, 2 * num_sms);
     part.resize((size_t)nblk_vec * 3 * S);
     pq_part.resize((size_t)nblk_spmv * S);
     rz_fix.resize((size_t)std::max<int64_t>(m.p, 1) * S);
@@ -286,6 +286,13 @@ static int recur_shift() {
   return v;
 }
 
+// CUDA graphs for the PCG iteration body (environment CBX_GRAPHS=0 launches
+// every kernel from the host instead)
+static bool use_graphs() {
+  static int v = env_int("CBX_GRAPHS", 1);
+  return v != 0;
+}
+
 template <int S>
 constexpr int rpw_ff() {
   return S >= 64 ? 1 : (S >= 32 ? 2 : (S >= 8 ? 4 : 8));
@@ -319,7 +326,7 @@ static void ff_piece(cbx_handle* h, const sv::OpView<double>& op, const double* 
   h->launched("k_gather_hl<f64>");
   constexpr int R = rpw_ff<W>();
   const int smem = W * 256 * (int)sizeof(float2);
-  CBX_CUDA(cudaFuncSetAttribute(sv::k_dense_ff<W, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  ensure_smem((const void*)sv::k_dense_ff<W, R>, smem, h->device);
   sv::k_dense_ff<W, R><<<(unsigned)((op.ng + 8 * R - 1) / (8 * R)), 256, smem, s>>>(mm.Qd32.p, mm.Qlo32.p, op.ng,
                                                                                    op.ld, vhl, Tout, active, xs);
   h->launched("k_dense_ff<f64>");
@@ -450,7 +457,7 @@ void matvec(cbx_handle* h, const sv::OpView<T>& op, Workspace<T, S>& w, const T*
     constexpr int R = rpw<T, S>();
     constexpr int KT = 32 * sv::Vec16<T>::n * 4;
     const int smem = S * KT * (int)sizeof(T);
-    CBX_CUDA(cudaFuncSetAttribute(sv::k_dense<T, S, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    ensure_smem((const void*)sv::k_dense<T, S, R>, smem, h->device);
     cbx_handle::ProfRec pr{};
     if (h->prof_on) {
       CBX_CUDA(cudaEventCreate(&pr.a));
@@ -504,7 +511,8 @@ void run_pcg(cbx_handle* h, Mme& m, const sv::OpView<T>& op, Workspace<T, S>& w,
   std::vector<double> tolv(S, 1.0);
   for (int c = 0; c < ncols; ++c) tolv[c] = tol_col[c];
   CBX_CUDA(cudaMemcpyAsync(w.tol.p, tolv.data(), S * sizeof(double), cudaMemcpyHostToDevice, s));
-  sv::k_scalar_init<S><<<1, sv::NT, 0, s>>>(w.col.p, ncols, w.part.p, w.nblk_vec, w.rz_fix.p, m.p, abs_tol, w.active.p);
+  sv::k_scalar_init<S><<<1, sv::NTS, 0, s>>>(w.col.p, ncols, w.part.p, w.nblk_vec, w.rz_fix.p, m.p, abs_tol,
+                                             w.active.p);
   h->launched(sizeof(T) == 4 ? "k_scalar_init<f32>" : "k_scalar_init<f64>");
   CBX_CUDA(cudaMemcpyAsync(w.P.p, w.Z.p, n * sizeof(T), cudaMemcpyDeviceToDevice, s));
   int host_active = 1;
@@ -512,10 +520,10 @@ void run_pcg(cbx_handle* h, Mme& m, const sv::OpView<T>& op, Workspace<T, S>& w,
   // block product is slow enough (and cannot skip finished blocks) to check
   // after every iteration
   const int CHECK = (sizeof(T) == 8 && op.Qd) ? 1 : 8;
-  for (int it = 0; it < maxit && host_active; it += CHECK) {
+  auto iterations = [&]() {
     for (int j = 0; j < CHECK; ++j) {
       matvec<T, S>(h, op, w, w.P.p, w.Q.p, lam, 1, w.P.p, w.pq_part.p, w.active.p, false, ncols);
-      sv::k_scalar_alpha<S><<<1, sv::NT, 0, s>>>(w.col.p, w.pq_part.p, w.nblk_spmv);
+      sv::k_scalar_alpha<S><<<1, sv::NTS, 0, s>>>(w.col.p, w.pq_part.p, w.nblk_spmv);
       h->launched(sizeof(T) == 4 ? "k_scalar_alpha<f32>" : "k_scalar_alpha<f64>");
       sv::k_update<T, S><<<w.nblk_vec, sv::NT, 0, s>>>(op, w.col.p, X, w.R.p, w.Z.p, w.P.p, w.Q.p, w.part.p);
       h->launched(sizeof(T) == 4 ? "k_update<f32>" : "k_update<f64>");
@@ -523,16 +531,56 @@ void run_pcg(cbx_handle* h, Mme& m, const sv::OpView<T>& op, Workspace<T, S>& w,
         sv::k_fixed<T, S><<<(unsigned)m.p, sv::NT, 0, s>>>(op, w.R.p, w.Z.p, w.col.p, w.rz_fix.p);
         h->launched(sizeof(T) == 4 ? "k_fixed<f32>" : "k_fixed<f64>");
       }
-      sv::k_scalar_beta<S><<<1, sv::NT, 0, s>>>(w.col.p, w.part.p, w.nblk_vec, w.rz_fix.p, m.p, w.tol.p, abs_tol,
-                                            maxit, w.active.p);
+      sv::k_scalar_beta<S><<<1, sv::NTS, 0, s>>>(w.col.p, w.part.p, w.nblk_vec, w.rz_fix.p, m.p, w.tol.p, abs_tol,
+                                                 maxit, w.active.p);
       h->launched(sizeof(T) == 4 ? "k_scalar_beta<f32>" : "k_scalar_beta<f64>");
       sv::k_pupdate<T, S><<<w.nblk_vec, sv::NT, 0, s>>>(m.dim, w.col.p, w.Z.p, w.P.p);
       h->launched(sizeof(T) == 4 ? "k_pupdate<f32>" : "k_pupdate<f64>");
-      ++matvecs;
     }
-    CBX_CUDA(cudaMemcpyAsync(&host_active, w.active.p, sizeof(int), cudaMemcpyDeviceToHost, s));
-    CBX_CUDA(cudaStreamSynchronize(s));
+  };
+  // After the first CHECK iterations (run eagerly: short solves pay no graph
+  // set-up, and one-time function attributes are set outside any capture),
+  // the CHECK-iteration body is captured once as a CUDA graph and replayed:
+  // one launch per CHECK iterations instead of ~10 per iteration.  Every
+  // kernel in it still skips its work once no column is active.
+  const bool graphs = CHECK > 1 && !h->prof_on && !h->trace_on && use_graphs();
+  cudaGraphExec_t gexec = nullptr;
+  int64_t graph_launches = 0;
+  try {
+    for (int it = 0; it < maxit && host_active; it += CHECK) {
+      if (it > 0 && graphs && !gexec) {
+        cudaGraph_t g = nullptr;
+        const int64_t l0 = h->launches;
+        CBX_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        try {
+          iterations();
+        } catch (...) {
+          cudaStreamEndCapture(s, &g);
+          if (g) cudaGraphDestroy(g);
+          throw;
+        }
+        CBX_CUDA(cudaStreamEndCapture(s, &g));
+        graph_launches = h->launches - l0;
+        h->launches = l0;
+        const cudaError_t e = cudaGraphInstantiate(&gexec, g, 0);
+        cudaGraphDestroy(g);
+        CBX_CUDA(e);
+      }
+      if (gexec) {
+        CBX_CUDA(cudaGraphLaunch(gexec, s));
+        h->launches += graph_launches;
+      } else {
+        iterations();
+      }
+      matvecs += CHECK;
+      CBX_CUDA(cudaMemcpyAsync(&host_active, w.active.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+      CBX_CUDA(cudaStreamSynchronize(s));
+    }
+  } catch (...) {
+    if (gexec) cudaGraphExecDestroy(gexec);
+    throw;
   }
+  if (gexec) CBX_CUDA(cudaGraphExecDestroy(gexec));
   out.resize(S);
   CBX_CUDA(cudaMemcpyAsync(out.data(), w.col.p, S * sizeof(sv::Col), cudaMemcpyDeviceToHost, s));
   CBX_CUDA(cudaStreamSynchronize(s));

@@ -13,7 +13,8 @@
 namespace cbx {
 namespace sv {
 
-constexpr int NT = 256;  // threads per block of the vector kernels
+constexpr int NT = 256;    // threads per block of the vector kernels
+constexpr int NTS = 1024;  // threads of the single-block scalar steps (partial sums read in parallel)
 
 // Per-column CG state (device).
 struct Col {
@@ -728,7 +729,7 @@ __device__ __forceinline__ void col_sums(const double* __restrict__ part, int nb
 template <int S>
 __global__ void k_scalar_init(Col* col, int ncols, const double* part, int nblk,
                               const double* rz_fix, int64_t p, int abs_tol, int* active_count) {
-  __shared__ double red[NT];
+  __shared__ double red[NTS];
   __shared__ double sums[3][S];
   for (int j = 0; j < 3; ++j) {
     col_sums<S>(part + (int64_t)j * S, nblk, 3 * S, red);
@@ -761,7 +762,7 @@ __global__ void k_scalar_init(Col* col, int ncols, const double* part, int nblk,
 // alpha = rz / p'Ap, breakdown handling (pcg_solver.h:482-498).
 template <int S>
 __global__ void k_scalar_alpha(Col* col, const double* pq_part, int nblk) {
-  __shared__ double red[NT];
+  __shared__ double red[NTS];
   col_sums<S>(pq_part, nblk, S, red);
   const int c = threadIdx.x;
   if (c >= S) return;
@@ -790,7 +791,7 @@ template <int S>
 __global__ void k_scalar_beta(Col* col, const double* part, int nblk, const double* rz_fix,
                               int64_t p, const double* tol_col, int abs_tol, int maxit,
                               int* active_count) {
-  __shared__ double red[NT];
+  __shared__ double red[NTS];
   __shared__ double sums[3][S];
   for (int j = 0; j < 2; ++j) {
     col_sums<S>(part + (int64_t)j * S, nblk, 2 * S, red);
