@@ -49,6 +49,12 @@ CONFIGS = {
                 var_a=0.3, var_e=0.7, levels=200, seed=2100),
     "c1": dict(name="gblup_n2000_m10000_sex2", n=2000, m=10000, p_lo=0.05, miss=0.01,
                var_a=0.4, var_e=0.6, levels=2, seed=1000),
+    # single-step GBLUP: 10 generations x 20,000 animals (500 sires x 10,000 dams
+    # per generation, 5 % unknown parents), the last 20,000 genotyped at m =
+    # 50,000; H^-1 = A^-1 + [0; (0.95 G + 0.05 A22)^-1 - A22^-1]; 500 herd-years
+    "c3": dict(name="ssgblup_ped200000_geno20000_m50000_hy500", kind="ssgblup", n_gen=10, per_gen=20000,
+               n_sires=500, n_dams=10000, p_unknown=0.05, n=20000, m=50000, p_lo=0.01, miss=0.02,
+               var_a=0.35, var_e=0.65, levels=500, seed=3000),
 }
 WORK_FILE = os.path.join(ROOT, "profiles", "reml_iteration_work.md")
 
@@ -122,22 +128,35 @@ def build_records(cfg, bed):
     return rec, d.p, d.csr()
 
 
-def cpu_pcg_iteration_cost(WtW, Qd, p, lam, iters: int, seed: int = 0) -> float:
-    """Seconds per FP64 PCG iteration of the oracle on the operator W'W + lam [0; Qd].
+def cpu_pcg_iteration_cost(WtW, Qd, p, lam, iters: int, seed: int = 0, Ainv=None, gmap=None) -> float:
+    """Seconds per FP64 PCG iteration of the oracle on the operator W'W + lam [0; Qinv]
+    with Qinv = Qd (dense), or Ainv + S Qd S^T (sparse Ainv, dense block Qd on
+    the rows gmap) when Ainv is given.
 
     Runs a fixed number of iterations (tol = 0) with the block-Jacobi
     preconditioner; numpy/BLAS uses every host thread."""
     from oracle.mme import pcg
     dim = WtW.shape[0]
     d = WtW.diagonal().copy()
-    d[p:] += lam * np.diag(Qd)
+    if Ainv is None:
+        d[p:] += lam * np.diag(Qd)
+    else:
+        dq = Ainv.diagonal().copy()
+        dq[gmap] += np.diag(Qd)
+        d[p:] += lam * dq
     A11 = WtW[:p, :p].toarray()
     A11[np.diag_indices(p)] += max(1e-8 * np.abs(np.diag(A11)).max(), 1e-6)
     dinv = 1.0 / d[p:]
 
     def matvec(v):
         y = WtW @ v
-        y[p:] += lam * (Qd @ v[p:])
+        if Ainv is None:
+            y[p:] += lam * (Qd @ v[p:])
+        else:
+            u = v[p:]
+            qu = Ainv @ u
+            qu[gmap] += Qd @ u[gmap]
+            y[p:] += lam * qu
         return y
 
     def prec(v):
@@ -166,7 +185,7 @@ def read_work_file():
 
 def read_traffic():
     try:
-        txt = open(os.path.join(ROOT, "profiles", "k_dense_tf32_n8192.md")).read()
+        txt = open(os.path.join(ROOT, "profiles", "k_dense_tf32_s64_n8192.md")).read()
         m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", txt)
         return float(m.group(1)) if m else None
     except OSError:
@@ -239,9 +258,23 @@ def run_gpu(args, cfg):
     phases = {}
     h = Handle(local)
 
+    ss = cfg.get("kind") == "ssgblup"
     t0 = time.perf_counter()
     bed, _ = simulate_bed(n, m, seed=cfg["seed"], p_lo=cfg["p_lo"], miss=cfg["miss"])
-    rec, p, rows = build_records(cfg, bed)
+    if ss:
+        from cosmicblup_gb300.synth import pedigree_breeding_values, simulate_gblup_records, simulate_pedigree
+        from cosmicblup_gb300.design import fixed_design
+        sire, dam = simulate_pedigree(cfg["n_gen"], cfg["per_gen"], cfg["n_sires"], cfg["n_dams"],
+                                      seed=cfg["seed"] + 1, p_unknown=cfg["p_unknown"])
+        q = sire.size
+        gmap = np.arange(q - n, q, dtype=np.int32)  # the last generation is genotyped
+        a = pedigree_breeding_values(sire, dam, cfg["var_a"], seed=cfg["seed"] + 2)
+        rec = simulate_gblup_records(q, cfg["levels"], a, seed=cfg["seed"] + 3, var_e=cfg["var_e"])
+        d = fixed_design(rec["cats"])
+        p, rows = d.p, d.csr()
+    else:
+        q = n
+        rec, p, rows = build_records(cfg, bed)
     phases["synthetic_data_s"] = time.perf_counter() - t0
 
     # GRM on the tensor cores
@@ -257,16 +290,28 @@ def run_gpu(args, cfg):
            "tops_int8_equivalent": gops / (gms * 1e-3) / 1e12 if gms > 0 else None,
            "note": "2 n^2 m_valid integer ops; exact f16 digit GEMMs on tcgen05 (no int8 MMA on sm_103a)"}
 
-    # eigen-bent G^-1 (FP64, cuSOLVER syevd + GEMM); host copy for the CPU baseline
-    t0 = time.perf_counter()
-    Ginv_host = invert_psd(h, None, n, download=(rank == 0 and not args.no_cpu_baseline))
-    phases["g_inverse_s"] = time.perf_counter() - t0
-
-    dm = DeviceMME(h, rec["y"], rec["aid"], rows, p, n)
-    dm.set_qinv_dense(None)
+    dm = DeviceMME(h, rec["y"], rec["aid"], rows, p, q)
+    want_host = rank == 0 and not args.no_cpu_baseline
+    Ainv_h = Gd_h = Ginv_host = None
+    if ss:
+        # H^-1 blocks on the device: A^-1 (Henderson), A22 by the pedigree
+        # recursion, tuneG + blend, eigen-bent Gb^-1 and A22^-1 (FP64)
+        from cosmicblup_gb300 import ainv_henderson, ssgblup_qinv
+        t0 = time.perf_counter()
+        Ainv_h = ainv_henderson(h, dam, sire)
+        _, Gd_h = ssgblup_qinv(dm, dam, sire, gmap, G=None, return_blocks=True)
+        phases["hinv_setup_s"] = time.perf_counter() - t0
+    else:
+        # eigen-bent G^-1 (FP64, cuSOLVER syevd + GEMM); host copy for the CPU baseline
+        t0 = time.perf_counter()
+        Ginv_host = invert_psd(h, None, n, download=want_host)
+        phases["g_inverse_s"] = time.perf_counter() - t0
+        dm.set_qinv_dense(None)
     fp, fc, fv = rows
     h2d_bytes = rec["y"].nbytes + rec["aid"].nbytes + fp.nbytes + fc.nbytes + fv.nbytes
-    d2h_bytes = 8 * (p + n) + 16
+    if ss:
+        h2d_bytes += sum(x.nbytes for x in Ainv_h) + Gd_h.nbytes + gmap.nbytes
+    d2h_bytes = 8 * (p + q) + 16
 
     # ---- mixed-precision REML iterations (the headline) ----
     r = AIREML(dm, 0.5, 0.5, RemlConfig.default(mode=MODE_EM, precision=MIXED))
@@ -316,8 +361,11 @@ def run_gpu(args, cfg):
     e2e_steps = max(1, min(args.steps, 3))
     h.timer_start()
     for _ in range(e2e_steps):
-        dm2 = DeviceMME(h, rec["y"], rec["aid"], (fp, fc, fv), p, n)
-        dm2.set_qinv_dense(None)
+        dm2 = DeviceMME(h, rec["y"], rec["aid"], (fp, fc, fv), p, q)
+        if ss:
+            dm2.set_qinv_split(*Ainv_h, Gd=Gd_h, gmap=gmap)
+        else:
+            dm2.set_qinv_dense(None)
         r2 = AIREML(dm2, *state, RemlConfig.default(mode=MODE_EM, precision=MIXED, max_iter=1))
         r2.solve()
     ms_e2e = h.timer_stop()
@@ -326,20 +374,29 @@ def run_gpu(args, cfg):
 
     # ---- CPU baseline: the oracle's FP64 PCG on this operator, bounded sample ----
     cpu = None
-    if rank == 0 and not args.no_cpu_baseline and fp64 is not None:
+    if want_host and fp64 is not None:
         from oracle.mme import build_fixed_design, sparse_data_part
         _, orows, _ = build_fixed_design(rec["cats"])
-        WtW, _ = sparse_data_part(rec["aid"], orows, p, n)
+        WtW, _ = sparse_data_part(rec["aid"], orows, p, q)
         lam = state[1] / state[0]
         iters = 10 if n >= 10000 else 50
-        c = cpu_pcg_iteration_cost(WtW, Ginv_host, p, lam, iters)
+        if ss:
+            import scipy.sparse as sp
+            ap, ac, av = Ainv_h
+            Ainv = sp.csr_matrix((av, ac, ap), shape=(q, q))
+            c = cpu_pcg_iteration_cost(WtW, Gd_h, p, lam, iters, Ainv=Ainv, gmap=gmap)
+        else:
+            c = cpu_pcg_iteration_cost(WtW, Ginv_host, p, lam, iters)
         # one RHS at a time on the CPU: every CG iteration of every solve plus
-        # the initial residual of each solve is one operator application
-        work = fp64["pcg_iterations_per_step"] + fp64["solves_per_step"]
+        # the initial residual of each solve is one operator application; the
+        # count of the reference's algorithm (probes from x0 = 0) where it was
+        # recorded for this workload, else the FP64 path's
+        work = read_work_file() if cfg["name"].startswith("gblup_n20000") else None
+        if work is None:
+            work = fp64["pcg_iterations_per_step"] + fp64["solves_per_step"]
         cpu = {"value": 1.0 / (c * work), "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
                "sample": f"oracle FP64 PCG, {iters} iterations on this operator (numpy/BLAS, all threads); "
-                         f"scaled by {work:.0f} single-RHS operator applications per REML iteration "
-                         f"(the FP64 path's count)"}
+                         f"scaled by {work:.0f} single-RHS operator applications per REML iteration"}
 
     if rank != 0:
         return
@@ -350,7 +407,8 @@ def run_gpu(args, cfg):
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
         "data": "synthetic (seeded generator with the workload's shapes)",
-        "config": {"workload": cfg["name"], "n_animals": n, "n_snps": m, "fixed_levels": cfg["levels"],
+        "config": {"workload": cfg["name"], "n_animals": q, "n_genotyped": n, "n_snps": m,
+                   "fixed_levels": cfg["levels"],
                    "step": "one EM+Hutchinson AI-REML iteration (data solve + probe solves, relres 1e-10)",
                    "precision": "mixed: FP32 PCG bulk + FP64 refinement on the true residual",
                    "l2": "inputs larger than L2 (1.6 GB FP32 G^-1 block read per PCG iteration)",
@@ -365,7 +423,8 @@ def run_gpu(args, cfg):
         "clocks": clk,
         "e2e": e2e,
         "gpu_launches": int(launches),
-        "roofline": {"bound": "hbm", "kernel": "k_dense<float> (G^-1 block x probe block)",
+        "roofline": {"bound": "hbm",
+                     "kernel": "k_dense_tf32<64> (tcgen05 3xTF32, G^-1 block x [data | 32 probes])",
                      "achieved": ach, "peak": hbm_peak, "unit": "GB/s",
                      "frac": (ach / hbm_peak) if ach else None, "traffic": traffic,
                      "peak_source": peak_src, "launches": dl, "avg_launch_ms": dms / dl if dl else None},

@@ -286,6 +286,17 @@ static int recur_shift() {
   return v;
 }
 
+// Floor of the inner FP32 solve's relative tolerance in the mixed solver
+// (environment CBX_INNER_TOL_MIN, default 1e-5).
+static double inner_tol_min() {
+  static double v = [] {
+    const char* e = std::getenv("CBX_INNER_TOL_MIN");
+    const double x = (e && *e) ? std::atof(e) : 1e-5;
+    return (x > 0 && x < 1e-1) ? x : 1e-5;
+  }();
+  return v;
+}
+
 // CUDA graphs for the PCG iteration body (environment CBX_GRAPHS=0 launches
 // every kernel from the host instead)
 static bool use_graphs() {
@@ -715,7 +726,7 @@ struct Solver : public SolverBase {
         if (!done[c] && res.iters[c] < maxit) {
           sc[c] = rn[c] > 0 ? rn[c] : 1.0;
           const double need = abs_tol ? tol / rn[c] : tol * bn[c] / rn[c];
-          itol[c] = std::min(1e-2, std::max(1e-5, 0.5 * need));
+          itol[c] = std::min(1e-2, std::max(inner_tol_min(), 0.5 * need));
           inner_max = std::max(inner_max, maxit - res.iters[c]);
         }
       if (inner_max == 0) break;

@@ -507,7 +507,9 @@ static void reml_gradient(cbx_handle* h, double vu, double ve, int nprobe, int s
   const int64_t total = exact ? q : nprobe;
   CBX_REQUIRE(total > 0, CBX_ERR_ARG, "nprobe must be positive");
   double tsum = 0.0;
-  const int64_t blk = 32;
+  // mixed precision reads the FP32 block once per iteration for up to 64
+  // columns; the FP64 product is FP64-bound, so 32 there
+  const int64_t blk = precision != 0 ? 64 : 32;
   // probe generator state: the reference's batches of 16 from mt19937_64(seed + done)
   std::mt19937_64 gen;
   std::uniform_int_distribution<int> dist(0, 1);

@@ -164,3 +164,21 @@ def simulate_mt_records(bed: bytes, n: int, m: int, seed: int, Vg: np.ndarray, V
     for k in range(1, n_levels):
         X[lvl == k, k] = 1.0
     return {"Y": Y, "X": X, "level": lvl}
+
+
+def pedigree_breeding_values(sire: np.ndarray, dam: np.ndarray, var_a: float, seed: int) -> np.ndarray:
+    """Breeding values down a pedigree listed parents first:
+    a_i = (a_sire + a_dam) / 2 + m_i, m_i ~ N(0, d_i var_a) with the Mendelian
+    sampling fraction d_i = 1/2, 3/4 or 1 for two, one or no known parents
+    (inbreeding ignored).  Unknown parents contribute 0."""
+    rng = np.random.default_rng(seed)
+    n = sire.size
+    known = (sire >= 0).astype(np.int64) + (dam >= 0).astype(np.int64)
+    d = np.where(known == 2, 0.5, np.where(known == 1, 0.75, 1.0))
+    m = rng.normal(0.0, 1.0, size=n) * np.sqrt(d * var_a)
+    a = np.zeros(n)
+    for i in range(n):
+        pa = (a[sire[i]] if sire[i] >= 0 else 0.0) + (a[dam[i]] if dam[i] >= 0 else 0.0)
+        a[i] = 0.5 * pa + m[i]
+    return a
+

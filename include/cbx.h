@@ -259,7 +259,7 @@ int cbx_mt_solve(cbx_handle* h, int64_t n, int32_t t, int64_t p, const double* Y
  *   grad_e = (e'e - var_e (n - p - q + lambda tr)) / (2 var_e^2)
  * tr = tr(Qinv C^uu) is estimated from nprobe Rademacher probes (the
  * reference's stream: batches of 16 from mt19937_64(seed + done)) solved as
- * multi-RHS blocks together with the data solve, or computed exactly from the
+ * multi-RHS blocks (64 columns in mixed precision, 32 in FP64), or computed exactly from the
  * q unit vectors when exact_trace != 0.  precision as cbx_pcg_solve.
  * trace / pcg_iters may be NULL. */
 int cbx_reml_gradient(cbx_handle* h, double var_u, double var_e, int32_t nprobe, int32_t seed,
