@@ -51,12 +51,11 @@ constexpr int RAW_D = NDIG * KSTEP * 2;                            // 448
 constexpr int RAW_BYTES = 1792;
 constexpr int OFF_STAGE = 0;
 constexpr int OFF_RAW = OFF_STAGE + NSTAGE * STAGE_BYTES;          // 116736
-constexpr int OFF_LUT = OFF_RAW + NRAW * RAW_BYTES;                // 123904
-constexpr int OFF_XX = OFF_LUT + 256 * 16;                         // 128000
-constexpr int OFF_L = OFF_XX + TILE_N * TILE_M * 4;                // 144384
-constexpr int OFF_Q = OFF_L + TILE_N * TILE_M * 8;                 // 177152
-constexpr int OFF_BAR = OFF_Q + TILE_N * TILE_M * 8;               // 209920
-constexpr int SMEM_BYTES = OFF_BAR + 256;                          // 210176
+constexpr int OFF_XX = OFF_RAW + NRAW * RAW_BYTES;                 // 123904
+constexpr int OFF_L = OFF_XX + TILE_N * TILE_M * 4;                // 140288
+constexpr int OFF_Q = OFF_L + TILE_N * TILE_M * 8;                 // 173056
+constexpr int OFF_BAR = OFF_Q + TILE_N * TILE_M * 8;               // 205824
+constexpr int SMEM_BYTES = OFF_BAR + 256;                          // 206080
 static_assert(SMEM_BYTES <= 232448, "shared memory budget");
 
 struct Args {
@@ -97,6 +96,24 @@ __device__ __forceinline__ void st_shared_v4(uint32_t addr, uint32_t a, uint32_t
                : "memory");
 }
 
+// One BED byte (4 codes, first SNP in the low bits) -> f16 pairs of the
+// allele counts x (code 00 -> 2, 10 -> 1, 01 / 11 -> 0) and of the observed
+// mask o (code 01 -> 0, else 1): x01 / o01 hold SNPs 0 and 1 (SNP 0 in the low
+// half), x23 / o23 SNPs 2 and 3.  Byte permutes pick each f16's high byte from
+// a 4-entry table indexed by the code (the low bytes are zero), so the decode
+// touches no shared memory.
+__device__ __forceinline__ void decode_byte(uint32_t b, uint32_t& x01, uint32_t& x23, uint32_t& o01,
+                                            uint32_t& o23) {
+  constexpr uint32_t kX = 0x003C0040u;  // high bytes of 2.0, 0, 1.0, 0 by code
+  constexpr uint32_t kO = 0x3C3C003Cu;  // high bytes of 1.0, 0, 1.0, 1.0 by code
+  const uint32_t s01 = 0x0404u | ((b & 3u) << 4) | (((b >> 2) & 3u) << 12);
+  const uint32_t s23 = 0x0404u | (((b >> 4) & 3u) << 4) | (((b >> 6) & 3u) << 12);
+  x01 = __byte_perm(kX, 0u, s01);
+  x23 = __byte_perm(kX, 0u, s23);
+  o01 = __byte_perm(kO, 0u, s01);
+  o23 = __byte_perm(kO, 0u, s23);
+}
+
 __device__ __forceinline__ uint32_t hmul2u(uint32_t a, uint32_t b) {
   __half2 r = __hmul2(*reinterpret_cast<__half2*>(&a), *reinterpret_cast<__half2*>(&b));
   return *reinterpret_cast<uint32_t*>(&r);
@@ -125,22 +142,6 @@ __global__ void __launch_bounds__(THREADS, 1) k_grm_tc(Args args) {
     mbar_init(&bars->drain, 1);
     bars->abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-  }
-  // code byte (4 SNPs) -> {X01, X23, O01, O23} as f16 pairs
-  if (tid >= 64 && tid < 192) {
-    for (int b = tid - 64; b < 256; b += 128) {
-      uint16_t xs[4], os[4];
-      for (int q = 0; q < 4; ++q) {
-        const int c = (b >> (2 * q)) & 3;
-        xs[q] = c == 0 ? 0x4000 : (c == 2 ? 0x3C00 : 0);   // 2, 1, 0 copies
-        os[q] = c == 1 ? 0 : 0x3C00;                        // observed
-      }
-      uint32_t* e = reinterpret_cast<uint32_t*>(smem + OFF_LUT + b * 16);
-      e[0] = xs[0] | (uint32_t(xs[1]) << 16);
-      e[1] = xs[2] | (uint32_t(xs[3]) << 16);
-      e[2] = os[0] | (uint32_t(os[1]) << 16);
-      e[3] = os[2] | (uint32_t(os[3]) << 16);
-    }
   }
   if (warp == 0) {
     tmem_alloc(&bars->tmem_base, 512);
@@ -232,7 +233,6 @@ __global__ void __launch_bounds__(THREADS, 1) k_grm_tc(Args args) {
   } else if (warp < 6) {
     // ---------------- producers: 2-bit codes -> f16 operand tiles ----------------
     const int pt = tid - 64;
-    const uint8_t* lut = smem + OFF_LUT;
     uint32_t g = 0;
     bool ok = true;
     const int br = pt & 31;   // B-side row
@@ -253,20 +253,20 @@ __global__ void __launch_bounds__(THREADS, 1) k_grm_tc(Args args) {
             const uint32_t word = kg < 2 ? w.x : w.y;
             const uint32_t b0 = (word >> (16 * (kg & 1))) & 0xFF;
             const uint32_t b1 = (word >> (16 * (kg & 1) + 8)) & 0xFF;
-            const uint4 e0 = *reinterpret_cast<const uint4*>(lut + b0 * 16);
-            const uint4 e1 = *reinterpret_cast<const uint4*>(lut + b1 * 16);
-            st_shared_v4(st + base + kg * 128, e0.x, e0.y, e1.x, e1.y);
-            st_shared_v4(st + A_TILE_BYTES + base + kg * 128, e0.z, e0.w, e1.z, e1.w);
+            uint32_t x0, x1, x2, x3, o0, o1, o2, o3;
+            decode_byte(b0, x0, x1, o0, o1);
+            decode_byte(b1, x2, x3, o2, o3);
+            st_shared_v4(st + base + kg * 128, x0, x1, x2, x3);
+            st_shared_v4(st + A_TILE_BYTES + base + kg * 128, o0, o1, o2, o3);
           }
         }
         // B side: row br, SNPs 8*bkg .. 8*bkg+7, 11 variants
         {
           const uint32_t b0 = raw[RAW_A + br * 8 + 2 * bkg];
           const uint32_t b1 = raw[RAW_A + br * 8 + 2 * bkg + 1];
-          const uint4 e0 = *reinterpret_cast<const uint4*>(lut + b0 * 16);
-          const uint4 e1 = *reinterpret_cast<const uint4*>(lut + b1 * 16);
-          const uint32_t X[4] = {e0.x, e0.y, e1.x, e1.y};
-          const uint32_t O[4] = {e0.z, e0.w, e1.z, e1.w};
+          uint32_t X[4], O[4];
+          decode_byte(b0, X[0], X[1], O[0], O[1]);
+          decode_byte(b1, X[2], X[3], O[2], O[3]);
           const uint8_t* dg = raw + RAW_A + RAW_B + bkg * 16;
           const uint32_t vbase = st + 2 * A_TILE_BYTES + (br >> 3) * 512 + (br & 7) * 16 + bkg * 128;
           st_shared_v4(vbase, X[0], X[1], X[2], X[3]);  // variant 0: X
