@@ -16,6 +16,7 @@
 #include "handle.h"
 #include "pcg.h"
 #include "solver.cuh"
+#include "pcg_fused.cuh"
 #include "dense_tc.h"
 #include "dense.h"
 #include <cstdlib>
@@ -226,10 +227,19 @@ constexpr int rpw() {
   return sizeof(T) == 8 ? (S <= 8 ? 8 : (S == 16 ? 4 : (S == 32 ? 2 : 1))) : (S <= 16 ? 8 : (S == 32 ? 4 : 2));
 }
 
+static int env_int(const char* name, int def) {
+  const char* e = std::getenv(name);
+  return (e && *e) ? std::atoi(e) : def;
+}
+
 template <typename T, int S>
 struct Workspace {
   DevBuf<T> R, Z, P, Q, Vt, Tout, X;
+  DevBuf<T> Pn;           // second direction buffer of the fused iteration
   DevBuf<double> part, pq_part, rz_fix, tol, colsum;
+  DevBuf<double> fpart;   // per-block partials of the fused iteration (nb_fused x 4 x S)
+  DevBuf<double> cpart;   // per-block column-sum partials of its direction (nb_fused x S)
+  int nb_fused = 0;       // co-resident grid of the fused iteration (0: not available)
   DevBuf<T> seg_part;
   DevBuf<sv::Col> col;
   DevBuf<int> active;
@@ -250,6 +260,19 @@ struct Workspace {
     active.resize(1);
     seg_part.resize((size_t)std::max<int32_t>(m.nseg, 1) * S);
     dim = m.dim;
+    nb_fused = 0;
+    if constexpr (sizeof(T) == 4) {
+      int per_sm = 0;
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sv::k_pcg_iter<T, S>, sv::NT, 0) == cudaSuccess &&
+          per_sm > 0) {
+        nb_fused = std::min(per_sm, 2) * num_sms;  // 2 per SM measured best (1, 3, 4 slower)
+        Pn.resize(n);
+        fpart.resize((size_t)nb_fused * 4 * S);
+        cpart.resize((size_t)nb_fused * S);
+      } else {
+        cudaGetLastError();
+      }
+    }
   }
 };
 
@@ -277,10 +300,6 @@ static bool use_resid_ff() {
 // Recursive-residual threshold of the mixed solver: a correction d updates
 // r -= A d in float-float when ||d|| <= 2^-recur_shift ||x|| in every column
 // (environment CBX_RECUR_SHIFT, default 4).
-static int env_int(const char* name, int def) {
-  const char* e = std::getenv(name);
-  return (e && *e) ? std::atoi(e) : def;
-}
 static int recur_shift() {
   static int v = env_int("CBX_RECUR_SHIFT", 4);
   return v;
@@ -296,6 +315,13 @@ static double inner_tol_min() {
   }();
   return v;
 }
+
+// The FP32 PCG iteration as one persistent cooperative kernel after the dense
+// product, when the environment sets CBX_FUSED=1 (read at every solve).  Off
+// by default: on GB300 its four grid-wide barriers and per-block redundant
+// reductions cost 1-10 % more per iteration than the separate kernels replayed
+// from a CUDA graph (measured at n = 2,000, 8,192 and 20,000).
+static bool use_fused() { return env_int("CBX_FUSED", 0) != 0; }
 
 // CUDA graphs for the PCG iteration body (environment CBX_GRAPHS=0 launches
 // every kernel from the host instead)
@@ -387,6 +413,45 @@ static void dense64(cbx_handle* h, const sv::OpView<double>& op, const double* X
   h->launched("cublas_dgemm<f64>");
 }
 
+// FP32 dense block product Tout = Qd Vt^T from the gathered operand w.Vt (the
+// tcgen05 3xTF32 kernel for 16, 32 or 64 columns, the HBM-streaming GEMV for
+// one, the CUDA-core kernel otherwise); returns the number of K-split partials.
+template <typename T, int S>
+int product_from_vt(cbx_handle* h, const sv::OpView<T>& op, Workspace<T, S>& w, const int* active) {
+  cudaStream_t s = h->stream;
+  int tsplit = 1;
+  cbx_handle::ProfRec pr{};
+  if (h->prof_on) {
+    CBX_CUDA(cudaEventCreate(&pr.a));
+    CBX_CUDA(cudaEventCreate(&pr.b));
+    CBX_CUDA(cudaEventRecord(pr.a, s));
+  }
+  if ((S == 16 || S == 32 || S == 64) && use_dense_tc()) {
+    tsplit = dense_tc_ksplit(op.ng, op.ld, h->num_sms);
+    dense_tc(h, reinterpret_cast<const float*>(op.Qd), op.ng, op.ld, reinterpret_cast<const float*>(w.Vt.p), S,
+             tsplit, reinterpret_cast<float*>(w.Tout.p), active);
+  } else if (S == 1) {
+    sv::k_gemv<T, 4, 4><<<(unsigned)((op.ng + 31) / 32), 256, 0, s>>>(op.Qd, op.ng, op.ld, w.Vt.p, w.Tout.p, active);
+    h->launched("k_gemv<f32>");
+  } else {
+    constexpr int R = rpw<T, S>();
+    constexpr int KT = 32 * sv::Vec16<T>::n * 4;
+    const int smem = S * KT * (int)sizeof(T);
+    ensure_smem((const void*)sv::k_dense<T, S, R>, smem, h->device);
+    sv::k_dense<T, S, R><<<(unsigned)((op.ng + 8 * R - 1) / (8 * R)), 256, smem, s>>>(op.Qd, op.ng, op.ld, w.Vt.p,
+                                                                                     w.Tout.p, active);
+    h->launched("k_dense<f32>");
+  }
+  if (h->prof_on) {
+    CBX_CUDA(cudaEventRecord(pr.b, s));
+    pr.bucket = 0;
+    // algorithmic bytes: the dense block once, the S gathered vectors, the outputs
+    pr.bytes = 4.0 * ((double)op.ng * op.ld + (double)S * op.ld + (double)op.ng * S * tsplit);
+    h->prof.push_back(pr);
+  }
+  return tsplit;
+}
+
 // Y = use_D * W'W X + lam [0; Qinv X_u] for an S-wide interleaved block whose
 // first ncols columns are populated (the rest are zero or ignored); optional
 // pq partials sum_i P[i] Y[i] for the PCG step.
@@ -420,73 +485,14 @@ void matvec(cbx_handle* h, const sv::OpView<T>& op, Workspace<T, S>& w, const T*
       pr.bytes = 8.0 * (double)op.ng * op.ld + 8.0 * ncols * ((double)op.ld + (double)op.ng);
       h->prof.push_back(pr);
     }
-  } else if ((S == 16 || S == 32 || S == 64) && use_dense_tc()) {
-    sv::k_gather_t<T, S><<<grid_for(S * op.ld, 256, 4 * h->num_sms), 256, 0, s>>>(X, w.Vt.p, op.p, op.ng, op.ld,
-                                                                               op.gmap, active);
-    h->launched("k_gather_t<f32>");
-    sv::k_colsum_vt<T><<<S, 256, 0, s>>>(w.Vt.p, op.ld, op.ng, w.colsum.p);
-    h->launched("k_colsum_vt<f32>");
-    tsplit = dense_tc_ksplit(op.ng, op.ld, h->num_sms);
-    cbx_handle::ProfRec pr{};
-    if (h->prof_on) {
-      CBX_CUDA(cudaEventCreate(&pr.a));
-      CBX_CUDA(cudaEventCreate(&pr.b));
-      CBX_CUDA(cudaEventRecord(pr.a, s));
-    }
-    dense_tc(h, reinterpret_cast<const float*>(op.Qd), op.ng, op.ld, reinterpret_cast<const float*>(w.Vt.p), S,
-             tsplit, reinterpret_cast<float*>(w.Tout.p), active);
-    if (h->prof_on) {
-      CBX_CUDA(cudaEventRecord(pr.b, s));
-      pr.bucket = 0;
-      pr.bytes = 4.0 * ((double)op.ng * op.ld + (double)S * op.ld + (double)op.ng * S * tsplit);
-      h->prof.push_back(pr);
-    }
-  } else if (S == 1) {
-    sv::k_gather_t<T, S><<<grid_for(S * op.ld, 256, 4 * h->num_sms), 256, 0, s>>>(X, w.Vt.p, op.p, op.ng, op.ld,
-                                                                               op.gmap, active);
-    h->launched("k_gather_t<f32>");
-    cbx_handle::ProfRec pr{};
-    if (h->prof_on) {
-      CBX_CUDA(cudaEventCreate(&pr.a));
-      CBX_CUDA(cudaEventCreate(&pr.b));
-      CBX_CUDA(cudaEventRecord(pr.a, s));
-    }
-    sv::k_colsum_vt<T><<<S, 256, 0, s>>>(w.Vt.p, op.ld, op.ng, w.colsum.p);
-    h->launched("k_colsum_vt<f32>");
-    sv::k_gemv<T, 4, 4><<<(unsigned)((op.ng + 31) / 32), 256, 0, s>>>(op.Qd, op.ng, op.ld, w.Vt.p, w.Tout.p, active);
-    h->launched("k_gemv<f32>");
-    if (h->prof_on) {
-      CBX_CUDA(cudaEventRecord(pr.b, s));
-      pr.bucket = 0;
-      pr.bytes = 4.0 * ((double)op.ng * op.ld + (double)op.ld + (double)op.ng);
-      h->prof.push_back(pr);
-    }
   } else {
+    // FP32: gather the dense-block rows, their FP64 column sums, the product
     sv::k_gather_t<T, S><<<grid_for(S * op.ld, 256, 4 * h->num_sms), 256, 0, s>>>(X, w.Vt.p, op.p, op.ng, op.ld,
                                                                                op.gmap, active);
     h->launched("k_gather_t<f32>");
-    constexpr int R = rpw<T, S>();
-    constexpr int KT = 32 * sv::Vec16<T>::n * 4;
-    const int smem = S * KT * (int)sizeof(T);
-    ensure_smem((const void*)sv::k_dense<T, S, R>, smem, h->device);
-    cbx_handle::ProfRec pr{};
-    if (h->prof_on) {
-      CBX_CUDA(cudaEventCreate(&pr.a));
-      CBX_CUDA(cudaEventCreate(&pr.b));
-      CBX_CUDA(cudaEventRecord(pr.a, s));
-    }
     sv::k_colsum_vt<T><<<S, 256, 0, s>>>(w.Vt.p, op.ld, op.ng, w.colsum.p);
     h->launched("k_colsum_vt<f32>");
-    sv::k_dense<T, S, R><<<(unsigned)((op.ng + 8 * R - 1) / (8 * R)), 256, smem, s>>>(op.Qd, op.ng, op.ld, w.Vt.p,
-                                                                                     w.Tout.p, active);
-    h->launched("k_dense<f32>");
-    if (h->prof_on) {
-      CBX_CUDA(cudaEventRecord(pr.b, s));
-      pr.bucket = 0;
-      // algorithmic bytes: the dense block once, the S gathered vectors, the S outputs
-      pr.bytes = 4.0 * ((double)op.ng * op.ld + (double)S * op.ld + (double)op.ng * S);
-      h->prof.push_back(pr);
-    }
+    tsplit = product_from_vt<T, S>(h, op, w, active);
   }
   if (use_D && h->mme->nseg > 0) {
     const Mme& mm = *h->mme;
@@ -531,7 +537,71 @@ void run_pcg(cbx_handle* h, Mme& m, const sv::OpView<T>& op, Workspace<T, S>& w,
   // block product is slow enough (and cannot skip finished blocks) to check
   // after every iteration
   const int CHECK = (sizeof(T) == 8 && op.Qd) ? 1 : 8;
-  auto iterations = [&]() {
+  // FP32: one persistent cooperative kernel per iteration after the dense
+  // product (pcg_fused.cuh); CHECK is even, so the direction is back in w.P
+  // after every block of CHECK iterations
+  const bool fused = sizeof(T) == 4 && w.nb_fused > 0 && use_fused() && CHECK % 2 == 0;
+  const Mme& mm = m;
+  if (fused && op.Qd) {
+    sv::k_gather_t<T, S><<<grid_for(S * op.ld, 256, 4 * h->num_sms), 256, 0, s>>>(w.P.p, w.Vt.p, op.p, op.ng, op.ld,
+                                                                               op.gmap, nullptr);
+    h->launched("k_gather_t<f32>");
+    sv::k_colsum_vt<T><<<S, 256, 0, s>>>(w.Vt.p, op.ld, op.ng, w.colsum.p);
+    h->launched("k_colsum_vt<f32>");
+  }
+  auto fused_step = [&](const T* P, T* Pn, bool first) {
+    int tsplit = 1;
+    if (op.Qd) tsplit = product_from_vt<T, S>(h, op, w, w.active.p);
+    sv::FusedArgs<T> a{};
+    a.op = op;
+    a.Tout = w.Tout.p;
+    a.tsplit = tsplit;
+    // the first step's direction sums come from k_colsum_vt, later ones from
+    // the previous step's per-block partials
+    a.colsum = (op.Qd && first) ? w.colsum.p : nullptr;
+    a.cpart_in = (op.Qd && !first) ? w.cpart.p : nullptr;
+    a.cpart_out = op.Qd ? w.cpart.p : nullptr;
+    a.tshift = mm.qshift;
+    a.lam = (T)lam;
+    a.seg_lo = mm.seg_lo.p;
+    a.seg_hi = mm.seg_hi.p;
+    a.nseg = mm.nseg;
+    a.fix_seg_ptr = mm.fix_seg_ptr.p;
+    a.seg_part = w.seg_part.p;
+    a.X = X;
+    a.R = w.R.p;
+    a.Z = w.Z.p;
+    a.P = P;
+    a.Pn = Pn;
+    a.Q = w.Q.p;
+    a.Vt = op.Qd ? w.Vt.p : nullptr;
+    a.col = w.col.p;
+    a.tol_col = w.tol.p;
+    a.abs_tol = abs_tol;
+    a.maxit = maxit;
+    a.active = w.active.p;
+    a.part = w.fpart.p;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)w.nb_fused);
+    cfg.blockDim = dim3(sv::NT);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    CBX_CUDA(cudaLaunchKernelEx(&cfg, sv::k_pcg_iter<T, S>, a));
+    h->launched("k_pcg_iter<f32>");
+  };
+  auto iterations = [&](bool first_block) {
+    if (fused) {
+      for (int j = 0; j < CHECK; j += 2) {
+        fused_step(w.P.p, w.Pn.p, first_block && j == 0);
+        fused_step(w.Pn.p, w.P.p, false);
+      }
+      return;
+    }
     for (int j = 0; j < CHECK; ++j) {
       matvec<T, S>(h, op, w, w.P.p, w.Q.p, lam, 1, w.P.p, w.pq_part.p, w.active.p, false, ncols);
       sv::k_scalar_alpha<S><<<1, sv::NTS, 0, s>>>(w.col.p, w.pq_part.p, w.nblk_spmv);
@@ -556,32 +626,39 @@ void run_pcg(cbx_handle* h, Mme& m, const sv::OpView<T>& op, Workspace<T, S>& w,
   // kernel in it still skips its work once no column is active.
   const bool graphs = CHECK > 1 && !h->prof_on && !h->trace_on && use_graphs();
   cudaGraphExec_t gexec = nullptr;
+  bool graph_failed = false;
   int64_t graph_launches = 0;
   try {
     for (int it = 0; it < maxit && host_active; it += CHECK) {
-      if (it > 0 && graphs && !gexec) {
+      if (it > 0 && graphs && !gexec && !graph_failed) {
+        // A body that cannot be captured (or instantiated) runs eagerly: the
+        // capture launched nothing, so nothing is lost.
         cudaGraph_t g = nullptr;
         const int64_t l0 = h->launches;
-        CBX_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-        try {
-          iterations();
-        } catch (...) {
-          cudaStreamEndCapture(s, &g);
-          if (g) cudaGraphDestroy(g);
-          throw;
+        bool ok = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+        if (ok) {
+          try {
+            iterations(false);
+          } catch (...) {
+            ok = false;
+          }
+          ok = (cudaStreamEndCapture(s, &g) == cudaSuccess) && ok && g;
         }
-        CBX_CUDA(cudaStreamEndCapture(s, &g));
+        if (ok) ok = cudaGraphInstantiate(&gexec, g, 0) == cudaSuccess;
+        if (g) cudaGraphDestroy(g);
         graph_launches = h->launches - l0;
         h->launches = l0;
-        const cudaError_t e = cudaGraphInstantiate(&gexec, g, 0);
-        cudaGraphDestroy(g);
-        CBX_CUDA(e);
+        if (!ok) {
+          gexec = nullptr;
+          graph_failed = true;
+          cudaGetLastError();
+        }
       }
       if (gexec) {
         CBX_CUDA(cudaGraphLaunch(gexec, s));
         h->launches += graph_launches;
       } else {
-        iterations();
+        iterations(it == 0);
       }
       matvecs += CHECK;
       CBX_CUDA(cudaMemcpyAsync(&host_active, w.active.p, sizeof(int), cudaMemcpyDeviceToHost, s));

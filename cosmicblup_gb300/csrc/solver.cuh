@@ -387,19 +387,20 @@ __device__ __forceinline__ double block_sum_cols(double v, double* red /*[NT]*/)
       for (int w = 0; w < (int)blockDim.x / S; ++w) t += red[w * S + tid];
     __syncthreads();
     return t;
-  }
+  } else {
 #pragma unroll
-  for (int off = 16; off >= S; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-  // now lanes < S of each warp hold that warp's per-column sums
-  const int warp = tid >> 5, lane = tid & 31;
-  if (lane < S) red[warp * S + lane] = v;
-  __syncthreads();
-  double t = 0.0;
-  if (tid < S) {
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w * S + tid];
+    for (int off = 16; off >= S; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    // now lanes < S of each warp hold that warp's per-column sums
+    const int warp = tid >> 5, lane = tid & 31;
+    if (lane < S) red[warp * S + lane] = v;
+    __syncthreads();
+    double t = 0.0;
+    if (tid < S) {
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w * S + tid];
+    }
+    __syncthreads();
+    return t;
   }
-  __syncthreads();
-  return t;
 }
 
 // Fixed-effect rows of W'W can hold one entry per record (the mean holds all of
@@ -434,6 +435,121 @@ __global__ void __launch_bounds__(NT) k_fix_seg(OpView<T> op, const int32_t* __r
     seg_part[(int64_t)sg * S + tid] = s;
   }
   (void)seg_row;
+}
+
+// Lanes of a warp over the S columns of one row: S <= 32 puts 32 / S lanes on
+// each column (c = lane % S); S > 32 gives each lane CPL = S / 32 columns
+// (c = lane + 32 j).
+template <int S>
+struct RowLayout {
+  static constexpr int CPL = S > 32 ? S / 32 : 1;
+};
+
+// Random-effect row i of Y = use_D W'W X + lam [Qs X_u + scatter(Tout) +
+// tshift colsum] (one warp); adds this lane's P[i] Y[i] terms to pq.
+template <typename T, int S>
+__device__ __forceinline__ void spmv_random_row(const OpView<T>& op, int64_t i, const T* __restrict__ X,
+                                                const T* __restrict__ Tout, int tsplit,
+                                                const double* __restrict__ colsum, double tshift, T lam,
+                                                int use_D, T* __restrict__ Y, const T* __restrict__ P,
+                                                double (&pq)[RowLayout<S>::CPL], int lane) {
+  const int64_t p = op.p, u = i - p;
+  if constexpr (S > 32) {
+    constexpr int CPL = S / 32;
+    T acc[CPL], qv[CPL];
+#pragma unroll
+    for (int j = 0; j < CPL; ++j) acc[j] = qv[j] = T(0);
+    if (use_D) {
+      for (int32_t e = op.Dptr[i]; e < op.Dptr[i + 1]; ++e) {
+        const T dv = op.Dval[e];
+        const T* xr = X + (int64_t)op.Dcol[e] * S + lane;
+#pragma unroll
+        for (int j = 0; j < CPL; ++j) acc[j] += dv * xr[32 * j];
+      }
+    }
+    if (op.Sptr) {
+      for (int32_t e = op.Sptr[u]; e < op.Sptr[u + 1]; ++e) {
+        const T sv = op.Sval[e];
+        const T* xr = X + (p + op.Scol[e]) * S + lane;
+#pragma unroll
+        for (int j = 0; j < CPL; ++j) qv[j] += sv * xr[32 * j];
+      }
+    }
+    if (op.Qd) {
+      const int32_t k = op.ginv[u];
+      if (k >= 0) {
+        for (int t = 0; t < tsplit; ++t) {
+          const T* tr = Tout + ((int64_t)t * op.ng + k) * S + lane;
+#pragma unroll
+          for (int j = 0; j < CPL; ++j) qv[j] += tr[32 * j];
+        }
+        if (colsum) {
+#pragma unroll
+          for (int j = 0; j < CPL; ++j) qv[j] += (T)(tshift * colsum[lane + 32 * j]);
+        }
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < CPL; ++j) {
+      const T yv = acc[j] + lam * qv[j];
+      Y[i * S + lane + 32 * j] = yv;
+      if (P) pq[j] += (double)P[i * S + lane + 32 * j] * (double)yv;
+    }
+  } else {
+    constexpr int G = 32 / S;
+    const int c = lane % S, g = lane / S;
+    T acc = T(0);
+    if (use_D) {
+      for (int32_t j = op.Dptr[i] + g; j < op.Dptr[i + 1]; j += G) acc += op.Dval[j] * X[(int64_t)op.Dcol[j] * S + c];
+    }
+    T qv = T(0);
+    if (op.Sptr) {
+      for (int32_t j = op.Sptr[u] + g; j < op.Sptr[u + 1]; j += G) qv += op.Sval[j] * X[(p + op.Scol[j]) * S + c];
+    }
+#pragma unroll
+    for (int off = 16; off >= S; off >>= 1) {
+      acc += __shfl_xor_sync(0xffffffffu, acc, off);
+      qv += __shfl_xor_sync(0xffffffffu, qv, off);
+    }
+    if (lane < S) {
+      if (op.Qd) {
+        const int32_t k = op.ginv[u];
+        if (k >= 0) {
+          // K-split partial sums of the dense block product, in a fixed order
+          for (int t = 0; t < tsplit; ++t) qv += Tout[((int64_t)t * op.ng + k) * S + c];
+          if (colsum) qv += (T)(tshift * colsum[c]);
+        }
+      }
+      const T yv = acc + lam * qv;
+      Y[i * S + c] = yv;
+      if (P) pq[0] += (double)P[i * S + c] * (double)yv;
+    }
+  }
+}
+
+// Block totals per column of the pq terms left by spmv_random_row: blk[c] for
+// every c < S (fixed order: lanes, then warps).
+template <int S>
+__device__ __forceinline__ void block_sum_row_pq(const double (&pq)[RowLayout<S>::CPL], double* red /*[NT]*/,
+                                                 double* blk /*[S]*/) {
+  const int tid = threadIdx.x, lane = tid & 31;
+  if constexpr (S > 32) {
+#pragma unroll
+    for (int j = 0; j < S / 32; ++j) {
+      red[tid] = pq[j];
+      __syncthreads();
+      if (tid < 32) {
+        double t = 0.0;
+        for (int w = 0; w < NT / 32; ++w) t += red[w * 32 + tid];
+        blk[32 * j + tid] = t;
+      }
+      __syncthreads();
+    }
+  } else {
+    const double t = block_sum_cols<S>(lane < S ? pq[0] : 0.0, red);
+    if (tid < S) blk[tid] = t;
+    __syncthreads();
+  }
 }
 
 // Y = use_D * D X + lam * [0; Qs X_u + scatter(Tout)]; optional pq partials sum_i P[i]Y[i].
@@ -475,116 +591,23 @@ __global__ void __launch_bounds__(NT) k_spmv(OpView<T> op, const T* __restrict__
       Y[i * S + tid] = t;
       if (P) pq = (double)P[i * S + tid] * (double)t;
     }
-  } else if constexpr (S > 32) {
-    // one warp per row, CPL columns per lane (c = lane + 32 j)
-    constexpr int CPL = S / 32;
-    double pqv[CPL];
+  } else {
+    // random-effect rows, one warp per row
+    double pqv[RowLayout<S>::CPL];
 #pragma unroll
-    for (int j = 0; j < CPL; ++j) pqv[j] = 0.0;
+    for (int j = 0; j < RowLayout<S>::CPL; ++j) pqv[j] = 0.0;
     const int64_t nwarps = (int64_t)(gridDim.x - nfix) * (NT / 32);
-    for (int64_t i = p + (int64_t)(blockIdx.x - nfix) * (NT / 32) + warp; i < op.dim; i += nwarps) {
-      T acc[CPL], qv[CPL];
-#pragma unroll
-      for (int j = 0; j < CPL; ++j) acc[j] = qv[j] = T(0);
-      if (use_D) {
-        for (int32_t e = op.Dptr[i]; e < op.Dptr[i + 1]; ++e) {
-          const T dv = op.Dval[e];
-          const T* xr = X + (int64_t)op.Dcol[e] * S + lane;
-#pragma unroll
-          for (int j = 0; j < CPL; ++j) acc[j] += dv * xr[32 * j];
-        }
-      }
-      const int64_t u = i - p;
-      if (op.Sptr) {
-        for (int32_t e = op.Sptr[u]; e < op.Sptr[u + 1]; ++e) {
-          const T sv = op.Sval[e];
-          const T* xr = X + (p + op.Scol[e]) * S + lane;
-#pragma unroll
-          for (int j = 0; j < CPL; ++j) qv[j] += sv * xr[32 * j];
-        }
-      }
-      if (op.Qd) {
-        const int32_t k = op.ginv[u];
-        if (k >= 0) {
-          for (int t = 0; t < tsplit; ++t) {
-            const T* tr = Tout + ((int64_t)t * op.ng + k) * S + lane;
-#pragma unroll
-            for (int j = 0; j < CPL; ++j) qv[j] += tr[32 * j];
-          }
-          if (colsum) {
-#pragma unroll
-            for (int j = 0; j < CPL; ++j) qv[j] += (T)(tshift * colsum[lane + 32 * j]);
-          }
-        }
-      }
-#pragma unroll
-      for (int j = 0; j < CPL; ++j) {
-        const T yv = acc[j] + lam * qv[j];
-        Y[i * S + lane + 32 * j] = yv;
-        if (P) pqv[j] += (double)P[i * S + lane + 32 * j] * (double)yv;
-      }
-    }
+    for (int64_t i = p + (int64_t)(blockIdx.x - nfix) * (NT / 32) + warp; i < op.dim; i += nwarps)
+      spmv_random_row<T, S>(op, i, X, Tout, tsplit, colsum, tshift, lam, use_D, Y, P, pqv, lane);
     if (pq_part) {
-      // per column: the 8 warps' sums in warp order
-#pragma unroll
-      for (int j = 0; j < CPL; ++j) {
-        red[tid] = pqv[j];
-        __syncthreads();
-        if (tid < 32) {
-          double t = 0.0;
-          for (int w = 0; w < NT / 32; ++w) t += red[w * 32 + tid];
-          pq_part[(int64_t)blockIdx.x * S + 32 * j + tid] = t;
-        }
-        __syncthreads();
-      }
+      __shared__ double blk[S];
+      block_sum_row_pq<S>(pqv, red, blk);
+      if (tid < S) pq_part[(int64_t)blockIdx.x * S + tid] = blk[tid];
     }
     return;
-  } else {
-    constexpr int G = 32 / S;
-    const int c = lane % S, g = lane / S;
-    const int64_t nwarps = (int64_t)(gridDim.x - nfix) * (NT / 32);
-    for (int64_t i = p + (int64_t)(blockIdx.x - nfix) * (NT / 32) + warp; i < op.dim; i += nwarps) {
-      T acc = T(0);
-      if (use_D) {
-        for (int32_t j = op.Dptr[i] + g; j < op.Dptr[i + 1]; j += G)
-          acc += op.Dval[j] * X[(int64_t)op.Dcol[j] * S + c];
-      }
-      T qv = T(0);
-      const int64_t u = i - p;
-      if (op.Sptr) {
-        for (int32_t j = op.Sptr[u] + g; j < op.Sptr[u + 1]; j += G)
-          qv += op.Sval[j] * X[(p + op.Scol[j]) * S + c];
-      }
-#pragma unroll
-      for (int off = 16; off >= S; off >>= 1) {
-        acc += __shfl_xor_sync(0xffffffffu, acc, off);
-        qv += __shfl_xor_sync(0xffffffffu, qv, off);
-      }
-      if (lane < S) {
-        if (op.Qd) {
-          const int32_t k = op.ginv[u];
-          if (k >= 0) {
-            // K-split partial sums of the dense block product, in a fixed order
-            for (int t = 0; t < tsplit; ++t) qv += Tout[((int64_t)t * op.ng + k) * S + c];
-            if (colsum) qv += (T)(tshift * colsum[c]);
-          }
-        }
-        const T yv = acc + lam * qv;
-        Y[i * S + c] = yv;
-        if (P) pq += (double)P[i * S + c] * (double)yv;
-      }
-    }
   }
-  if (pq_part) {
-    // threads tid < S hold pq for column tid in the fixed branch; lanes < S per warp otherwise
-    double v = pq;
-    if ((int)blockIdx.x < nfix) {
-      if (tid < S) pq_part[(int64_t)blockIdx.x * S + tid] = v;
-    } else {
-      const double t = block_sum_cols<S>(lane < S ? v : 0.0, red);
-      if (tid < S) pq_part[(int64_t)blockIdx.x * S + tid] = t;
-    }
-  }
+  // fixed-row block: thread tid < S holds p'q of its row for column tid
+  if (pq_part && tid < S) pq_part[(int64_t)blockIdx.x * S + tid] = pq;
 }
 
 // r = b - Y, z = M^-1 r on random rows, partial sums of r'r, r'z (random rows) and b'b.

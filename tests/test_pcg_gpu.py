@@ -235,3 +235,26 @@ def test_dense_ff_product_accuracy(handle, S, rpw):
         for c in range(S):
             err = abs(Y[i, c] - xdot(Q[i], V[c])) / scale[i, c]
             assert err < 6e-14, (i, c, err)
+
+
+def test_fused_iteration_matches_separate_kernels(handle, gblup, monkeypatch):
+    """The persistent cooperative PCG iteration (CBX_FUSED=1) runs the same
+    per-column recurrences as the separate kernels (its sums are ordered
+    differently): solutions agree to 1e-8, true relres < 1e-10."""
+    om, lam = gblup["mme"], 2.0
+    A = om.lhs(gblup["Gi"], lam)
+    rng = np.random.default_rng(91)
+    k = 33
+    B = np.zeros((om.dim, k))
+    B[om.p:, :] = rng.choice([-1.0, 1.0], size=(om.q, k))
+    B[:, 0] = om.rhs()
+    dm = dev_mme(handle, gblup)
+    X0, it0, rr0 = dm.pcg_solve(lam, B, precision=MIXED)
+    monkeypatch.setenv("CBX_FUSED", "1")
+    dm1 = dev_mme(handle, gblup)
+    X1, it1, rr1 = dm1.pcg_solve(lam, B, precision=MIXED)
+    monkeypatch.delenv("CBX_FUSED")
+    for c in range(k):
+        assert true_relres(A, X1[:, c], B[:, c]) < 1e-10, c
+        assert rel(X1[:, c], X0[:, c]) < 1e-8, c
+
