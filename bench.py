@@ -52,6 +52,11 @@ CONFIGS = {
     # single-step GBLUP: 10 generations x 20,000 animals (500 sires x 10,000 dams
     # per generation, 5 % unknown parents), the last 20,000 genotyped at m =
     # 50,000; H^-1 = A^-1 + [0; (0.95 G + 0.05 A22)^-1 - A22^-1]; 500 herd-years
+    # 96 independent GBLUPs, n ~ log-uniform [500, 8000], m ~ log-uniform
+    # [5000, 40000], h2 ~ U(0.1, 0.6), mean + 10-level group; each one GRM +
+    # eigen-bent G^-1 + REML (3 EM iterations), the batch sharing the GPU
+    "c5": dict(name="batch96_gblup_n500-8000_m5000-40000", kind="batch", nprob=96, n_lo=500, n_hi=8000,
+               m_lo=5000, m_hi=40000, levels=10, max_iter=3, workers=16, seed=5000),
     "c3": dict(name="ssgblup_ped200000_geno20000_m50000_hy500", kind="ssgblup", n_gen=10, per_gen=20000,
                n_sires=500, n_dams=10000, p_unknown=0.05, n=20000, m=50000, p_lo=0.01, miss=0.02,
                var_a=0.35, var_e=0.65, levels=500, seed=3000),
@@ -198,6 +203,10 @@ def run_reference(args, cfg):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
+    if cfg.get("kind") in ("batch", "ssgblup"):
+        print(json.dumps({"impl": "reference", "unavailable":
+                          f"the CPU port is timed on the GBLUP workloads only, not {cfg['name']}"}))
+        return
     import scipy.sparse as sp  # noqa: F401
     from cosmicblup_gb300.synth import simulate_gblup_records
     from oracle.mme import build_fixed_design, sparse_data_part
@@ -238,6 +247,50 @@ def run_reference(args, cfg):
 
 
 # ---------------------------------------------------------------------------
+def run_batch(args, cfg):
+    """Batched uneven GBLUPs (cbx_batch_reml): wall time of the whole batch,
+    mixed precision and the plain FP64 path, many workers and one."""
+    from cosmicblup_gb300 import BatchProblem, RemlConfig, batch_reml
+    from cosmicblup_gb300.design import fixed_design
+    from cosmicblup_gb300.mme import FP64, MIXED
+    from cosmicblup_gb300.synth import genetic_values, simulate_bed, simulate_gblup_records
+    from cosmicblup_gb300.vce import MODE_EM
+    rng = np.random.default_rng(cfg["seed"])
+    t0 = time.perf_counter()
+    probs = []
+    for i in range(cfg["nprob"]):
+        n = int(round(np.exp(rng.uniform(np.log(cfg["n_lo"]), np.log(cfg["n_hi"])))))
+        m = int(round(np.exp(rng.uniform(np.log(cfg["m_lo"]), np.log(cfg["m_hi"])))))
+        h2 = rng.uniform(0.1, 0.6)
+        bed, _ = simulate_bed(n, m, seed=cfg["seed"] + 10 * i, p_lo=0.01, miss=0.02)
+        g = genetic_values(bed, n, m, seed=cfg["seed"] + 10 * i + 1, var_a=h2)
+        rec = simulate_gblup_records(n, cfg["levels"], g, seed=cfg["seed"] + 10 * i + 2, var_e=1.0 - h2)
+        d = fixed_design(rec["cats"])
+        probs.append(BatchProblem(bed=bed, n=n, m=m, y=rec["y"], aid=rec["aid"], rows=d.csr(), p=d.p))
+    gen_s = time.perf_counter() - t0
+    out = {}
+    for label, prec, workers in [("mixed", MIXED, cfg["workers"]), ("fp64", FP64, cfg["workers"]),
+                                 ("mixed_1worker", MIXED, 1)]:
+        rc = RemlConfig.default(mode=MODE_EM, precision=prec, max_iter=cfg["max_iter"])
+        t0 = time.perf_counter()
+        res = batch_reml(probs, rc, workers=workers)
+        wall = time.perf_counter() - t0
+        iters = sum(r.iterations for r in res)
+        out[label] = {"wall_s": wall, "problems_per_s": len(probs) / wall, "reml_iterations": iters,
+                      "reml_iter_per_s_incl_setup": iters / wall, "workers": workers,
+                      "sum_problem_s": sum(r.seconds for r in res)}
+    line = {"metric": METRIC, "value": out["mixed"]["reml_iter_per_s_incl_setup"],
+            "unit": "REML iter/s (batch, GRM + G^-1 + REML per problem)", "n_gpus": 1,
+            "higher_is_better": True, "dtype": "f32+f64", "data": "synthetic (seeded generator)",
+            "config": {"workload": cfg["name"], "problems": cfg["nprob"], "max_iter": cfg["max_iter"],
+                       "n_range": [min(p.n for p in probs), max(p.n for p in probs)],
+                       "m_range": [min(p.m for p in probs), max(p.m for p in probs)]},
+            "batch": out, "mixed_vs_fp64": out["fp64"]["wall_s"] / out["mixed"]["wall_s"],
+            "workers_speedup": out["mixed_1worker"]["wall_s"] / out["mixed"]["wall_s"],
+            "setup": {"synthetic_data_s": gen_s}}
+    print(json.dumps(line))
+
+
 def run_gpu(args, cfg):
     import ctypes as C
     from cosmicblup_gb300 import AIREML, DeviceMME, Handle, RemlConfig, invert_psd
@@ -447,6 +500,8 @@ def main():
     cfg = CONFIGS[args.config]
     if args.impl == "reference":
         run_reference(args, cfg)
+    elif cfg.get("kind") == "batch":
+        run_batch(args, cfg)
     else:
         run_gpu(args, cfg)
 

@@ -77,6 +77,7 @@ SIGNATURES = [
     ("cbx_mt_solve", C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
                                C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("cbx_dense_apply_noalloc", C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
+    ("cbx_batch_reml", C.c_int, [C.c_int, C.c_int32, C.c_void_p, C.c_float, C.c_void_p, C.c_int32, C.c_void_p]),
     # diagnostics and self-test exports (not in the public header)
     ("cbx_trace_enable", C.c_int, [C.c_void_p, C.c_int32]),
     ("cbx_trace_read", C.c_int, [C.c_void_p, C.c_char_p, C.c_int64]),

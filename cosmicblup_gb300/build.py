@@ -20,7 +20,7 @@ LIB = os.path.join(HERE, "libcbx.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "--expt-relaxed-constexpr", "-Xptxas", "-v"]
-LIBS = ["-lcublas", "-lcusolver"]
+LIBS = ["-lcublas", "-lcusolver", "-lpthread"]
 
 
 def nvcc() -> str:

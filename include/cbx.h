@@ -214,6 +214,40 @@ int cbx_reml_solve(cbx_handle* h, const cbx_reml_config* cfg, double* var_u, dou
                    int32_t* iterations, int32_t* converged, double* solution,
                    cbx_reml_iter_info* history);
 
+/* ---- Batched independent GBLUP problems ----------------------------------
+ * Many uneven GBLUP problems -- each one GrmBuilder::compute + the eigen-bent
+ * invert_psd_matrix + AI_REML::solve, i.e. one reference run (the reference
+ * runs them one after the other) -- share one GPU: nworkers host threads each
+ * own a handle (one stream, its own library handles and buffers, reused from
+ * problem to problem) and take problems largest first, so the streams of
+ * small problems overlap on the GPU.  Every problem gets exactly the
+ * single-problem path (results equal the per-problem calls).  Each problem's
+ * status code lands in its result; the call returns the first non-zero one
+ * (CBX_OK when all succeeded). */
+typedef struct cbx_batch_problem {
+  const uint8_t* bed;        /* PLINK BED (with its 3-byte header), bed_bytes long */
+  int64_t bed_bytes, n, m;   /* n animals = q, m SNPs */
+  int64_t n_rec, p;          /* records, fixed-effect columns */
+  const double* y;           /* n_rec */
+  const int32_t* aid;        /* n_rec, 1-based row of G^-1 (0 = none) */
+  const int64_t* fx_ptr;     /* fixed-effect design CSR (as cbx_mme_create) */
+  const int32_t* fx_col;
+  const double* fx_val;
+  double var_u, var_e;       /* starting variances */
+} cbx_batch_problem;
+
+typedef struct cbx_batch_result {
+  int32_t status;            /* CBX_OK or the failing call's code */
+  int32_t iterations, converged;
+  double var_u, var_e;
+  int64_t pcg_iters;         /* CG iterations over the whole REML run */
+  double seconds;            /* wall time of this problem on its worker */
+  double* solution;          /* caller-owned, length p + n, or NULL */
+} cbx_batch_result;
+
+int cbx_batch_reml(int device, int32_t nprob, const cbx_batch_problem* probs, float min_maf,
+                   const cbx_reml_config* cfg, int32_t nworkers, cbx_batch_result* results);
+
 /* ---- Final MME solve and fixed-effect standard errors ---------------------
  * Replaces GSSolve::solve (src/solve/mixed_model_solver.cpp:37-420) for one
  * random component: lambda = var_e / var_u (0 if var_u <= 1e-9), sol (dim) =
