@@ -330,9 +330,11 @@ static bool use_graphs() {
   return v != 0;
 }
 
+// rows per warp of the float-float product (measured on GB300 at n = 16,384:
+// 16 columns x 2 rows runs at ~58 % of FP32 issue, 32 columns at <= 40 %)
 template <int S>
 constexpr int rpw_ff() {
-  return S >= 64 ? 1 : (S >= 32 ? 2 : (S >= 8 ? 4 : 8));
+  return S >= 64 ? 1 : (S >= 16 ? 2 : (S >= 8 ? 4 : 8));
 }
 
 // Vt[c * ld + k] = X[(p + gmap[k]) * xs + c] for c < ncols, k < ng (the gathered
@@ -349,7 +351,7 @@ __global__ void k_gather_cols(const double* __restrict__ X, int xs, int ncols, d
 }
 
 // Float-float block products are FP32-issue-bound, so they run on the
-// populated columns only, in power-of-two pieces of at most 32 columns written
+// populated columns only, in power-of-two pieces of at most 16 columns written
 // into the S-wide output.
 template <int W>
 static void ff_piece(cbx_handle* h, const sv::OpView<double>& op, const double* X, int xs, double* Vt,
@@ -379,8 +381,10 @@ static void dense64(cbx_handle* h, const sv::OpView<double>& op, const double* X
     // the compensated FP64 column sums that restore the block's shift
     sv::k_colsum_x<<<ncols, 256, 0, h->stream>>>(X, S, op.p, op.ng, op.gmap, colsum);
     h->launched("k_colsum_x<f64>");
+    // pieces of at most 16 columns (two 16-column passes beat one 32-column
+    // pass: register pressure, not the second read of the block, limits it)
     for (int c0 = 0; c0 < ncols;) {
-      const int left = std::min(ncols - c0, 32);
+      const int left = std::min(ncols - c0, 16);
       int w = 1;
       while (2 * w <= left) w <<= 1;
       switch (w) {
