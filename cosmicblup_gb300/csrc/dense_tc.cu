@@ -109,7 +109,7 @@ template <int S>
 __global__ void __launch_bounds__(THREADS, 1)
     k_dense_tf32(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int ng,
                  int ksteps, int ksplit, int kps, int nunits, float* __restrict__ Tpart, const int* active,
-                 int* status) {
+                 int* status, int nc) {
   if (active && *active == 0) return;
   using LY = Layout<S>;
   extern __shared__ uint8_t dsm_raw[];
@@ -155,7 +155,7 @@ __global__ void __launch_bounds__(THREADS, 1)
           const uint32_t s = g % NSTAGE;
           if (!mbar_wait(&bars->empty[s], ((g / NSTAGE) & 1) ^ 1, abort_flag)) { ok = false; break; }
           uint8_t* st = smem + s * LY::STAGE;
-          mbar_expect_tx(&bars->full[s], A_BYTES + LY::B_BYTES);
+          mbar_expect_tx(&bars->full[s], A_BYTES + nc * KB * 4);
           tma_load_2d(smem_addr(st), &tmA, k * KB, mt * 128, &bars->full[s]);
           tma_load_2d(smem_addr(st + LY::OFF_B), &tmB, k * KB, 0, &bars->full[s]);
         }
@@ -165,7 +165,8 @@ __global__ void __launch_bounds__(THREADS, 1)
     __syncwarp();
   } else if (warp == 1) {
     if (lane == 0) {
-      constexpr uint32_t ID2 = idesc_tf32(128, 2 * S), ID1 = idesc_tf32(128, S);
+      // N = 2 nc for [B_hi; B_lo] and nc for B_hi (nc populated columns, a multiple of 16)
+      const uint32_t ID2 = idesc_tf32(128, 2 * nc), ID1 = idesc_tf32(128, nc);
       uint32_t g = 0, c = 0;
       bool ok = true;
       for (int u = blockIdx.x; u < nunits && ok; u += gridDim.x, ++c) {
@@ -181,12 +182,12 @@ __global__ void __launch_bounds__(THREADS, 1)
           tc_fence_after();
           const uint32_t st = smem_addr(smem + s * LY::STAGE);
           const uint64_t dA = sdesc_sw128(st), dAl = sdesc_sw128(st + A_BYTES);
-          const uint64_t dB = sdesc_sw128(st + LY::OFF_B);  // N = 2S rows: B_hi then B_lo
+          const uint64_t dB = sdesc_sw128(st + LY::OFF_B);  // N = 2 nc rows: B_hi then B_lo
 #pragma unroll
           for (int j = 0; j < 4; ++j) {  // four K slices of 8 tf32 (32 bytes) per 128-byte row
             const uint32_t first = (k == k0 && j == 0) ? 0u : 1u;
             umma_tf32(d, dA + 2 * j, dB + 2 * j, ID2, first);      // [A B_hi | A B_lo]
-            umma_tf32(d + S, dAl + 2 * j, dB + 2 * j, ID1, 1u);    // upper half += A_lo B_hi
+            umma_tf32(d + nc, dAl + 2 * j, dB + 2 * j, ID1, 1u);   // upper half += A_lo B_hi
           }
           umma_commit(&bars->empty[s]);
         }
@@ -216,8 +217,8 @@ __global__ void __launch_bounds__(THREADS, 1)
 #pragma unroll 8
         for (int i = t; i < A_BYTES / 16; i += 128) Al[i] = lo4(A[i]);
         const float4* B = reinterpret_cast<const float4*>(st + LY::OFF_B);
-        float4* Bl = reinterpret_cast<float4*>(st + LY::OFF_BL);
-        for (int i = t; i < LY::B_BYTES / 16; i += 128) Bl[i] = lo4(B[i]);
+        float4* Bl = reinterpret_cast<float4*>(st + LY::OFF_B + nc * KB * 4);
+        for (int i = t; i < nc * KB / 4; i += 128) Bl[i] = lo4(B[i]);
         fence_async_smem();
         mbar_arrive(&bars->conv[s]);
       }
@@ -233,25 +234,22 @@ __global__ void __launch_bounds__(THREADS, 1)
       const uint32_t b = c & 1;
       if (!mbar_wait(&bars->acc_full[b], (c >> 1) & 1, abort_flag)) { ok = false; break; }
       tc_fence_after();
-      // columns [0, S): A B_hi; [S, 2S): A B_lo + A_lo B_hi
-      uint32_t r[32];
+      // columns [0, nc): A B_hi; [nc, 2 nc): A B_lo + A_lo B_hi; nc <= S
       float out[S];
       const uint32_t ta = tmem + (uint32_t(q * 32) << 16) + b * 2 * S;
-      if constexpr (S >= 32) {
 #pragma unroll
-        for (int j0 = 0; j0 < S; j0 += 32) {
-          uint32_t r2[32];
-          tmem_ld32(ta + j0, r);
-          tmem_ld32(ta + S + j0, r2);
+      for (int j0 = 0; j0 < S; j0 += 16) {
+        if (j0 < nc) {
+          uint32_t r1[16], r2[16];
+          tmem_ld16(ta + j0, r1);
+          tmem_ld16(ta + nc + j0, r2);
           tmem_ld_wait();
 #pragma unroll
-          for (int j = 0; j < 32; ++j) out[j0 + j] = __uint_as_float(r[j]) + __uint_as_float(r2[j]);
-        }
-      } else {
-        tmem_ld32(ta, r);  // 16 + 16 columns
-        tmem_ld_wait();
+          for (int j = 0; j < 16; ++j) out[j0 + j] = __uint_as_float(r1[j]) + __uint_as_float(r2[j]);
+        } else {
 #pragma unroll
-        for (int j = 0; j < 16; ++j) out[j] = __uint_as_float(r[j]) + __uint_as_float(r[16 + j]);
+          for (int j = 0; j < 16; ++j) out[j0 + j] = 0.0f;
+        }
       }
       tc_fence_before();
       __syncwarp();
@@ -324,11 +322,14 @@ int dense_tc_ksplit(int64_t ng, int64_t ld, int num_sms) {
 }
 
 void dense_tc(cbx_handle* h, const float* Qd, int64_t ng, int64_t ld, const float* Vt, int S, int ksplit, float* Tpart,
-              const int* active) {
+              const int* active, int ncols) {
   CBX_REQUIRE(S == 16 || S == 32 || S == 64, CBX_ERR_ARG, "dense_tc supports 16, 32 or 64 columns");
+  // the MMAs and the lo conversion run on the populated columns, rounded up
+  // to the MMA granularity of 16; the output's other columns are written as 0
+  const int nc = std::min(S, std::max(16, (ncols + 15) / 16 * 16));
   CBX_REQUIRE(ld % 4 == 0, CBX_ERR_ARG, "row pitch must be a multiple of 4");
   const CUtensorMap ma = dtc::make_map(Qd, ld, ng, 128);
-  const CUtensorMap mb = dtc::make_map(Vt, ld, S, S);
+  const CUtensorMap mb = dtc::make_map(Vt, ld, S, nc);
   const int ksteps = (int)((ld + dtc::KB - 1) / dtc::KB);
   const int kps = (ksteps + ksplit - 1) / ksplit;
   CBX_REQUIRE((int64_t)(ksplit - 1) * kps < ksteps, CBX_ERR_ARG, "K split leaves an empty split");
@@ -339,17 +340,17 @@ void dense_tc(cbx_handle* h, const float* Qd, int64_t ng, int64_t ld, const floa
     constexpr int SM = dtc::Layout<64>::SMEM;
     ensure_smem((const void*)dtc::k_dense_tf32<64>, SM, h->device);
     dtc::k_dense_tf32<64><<<grid, dtc::THREADS, SM, h->stream>>>(ma, mb, (int)ng, ksteps, ksplit, kps, nunits, Tpart,
-                                                                 active, h->status.p);
+                                                                 active, h->status.p, nc);
   } else if (S == 32) {
     constexpr int SM = dtc::Layout<32>::SMEM;
     ensure_smem((const void*)dtc::k_dense_tf32<32>, SM, h->device);
     dtc::k_dense_tf32<32><<<grid, dtc::THREADS, SM, h->stream>>>(ma, mb, (int)ng, ksteps, ksplit, kps, nunits, Tpart,
-                                                                 active, h->status.p);
+                                                                 active, h->status.p, nc);
   } else {
     constexpr int SM = dtc::Layout<16>::SMEM;
     ensure_smem((const void*)dtc::k_dense_tf32<16>, SM, h->device);
     dtc::k_dense_tf32<16><<<grid, dtc::THREADS, SM, h->stream>>>(ma, mb, (int)ng, ksteps, ksplit, kps, nunits, Tpart,
-                                                                 active, h->status.p);
+                                                                 active, h->status.p, nc);
   }
   h->launched("k_dense_tf32");
 }

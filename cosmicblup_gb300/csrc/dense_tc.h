@@ -7,5 +7,5 @@ namespace cbx {
 int dense_tc_ksplit(int64_t ng, int64_t ld, int num_sms);
 // Tpart[ks][i][c] = sum over split ks of Qd[i][k] Vt[c][k]; S = 16 or 32.
 void dense_tc(cbx_handle* h, const float* Qd, int64_t ng, int64_t ld, const float* Vt, int S, int ksplit,
-              float* Tpart, const int* active);
+              float* Tpart, const int* active, int ncols);
 }  // namespace cbx

@@ -421,7 +421,8 @@ static void dense64(cbx_handle* h, const sv::OpView<double>& op, const double* X
 // tcgen05 3xTF32 kernel for 16, 32 or 64 columns, the HBM-streaming GEMV for
 // one, the CUDA-core kernel otherwise); returns the number of K-split partials.
 template <typename T, int S>
-int product_from_vt(cbx_handle* h, const sv::OpView<T>& op, Workspace<T, S>& w, const int* active) {
+int product_from_vt(cbx_handle* h, const sv::OpView<T>& op, Workspace<T, S>& w, const int* active,
+                    int ncols = S) {
   cudaStream_t s = h->stream;
   int tsplit = 1;
   cbx_handle::ProfRec pr{};
@@ -433,7 +434,7 @@ int product_from_vt(cbx_handle* h, const sv::OpView<T>& op, Workspace<T, S>& w, 
   if ((S == 16 || S == 32 || S == 64) && use_dense_tc()) {
     tsplit = dense_tc_ksplit(op.ng, op.ld, h->num_sms);
     dense_tc(h, reinterpret_cast<const float*>(op.Qd), op.ng, op.ld, reinterpret_cast<const float*>(w.Vt.p), S,
-             tsplit, reinterpret_cast<float*>(w.Tout.p), active);
+             tsplit, reinterpret_cast<float*>(w.Tout.p), active, ncols);
   } else if (S == 1) {
     sv::k_gemv<T, 4, 4><<<(unsigned)((op.ng + 31) / 32), 256, 0, s>>>(op.Qd, op.ng, op.ld, w.Vt.p, w.Tout.p, active);
     h->launched("k_gemv<f32>");
@@ -496,7 +497,7 @@ void matvec(cbx_handle* h, const sv::OpView<T>& op, Workspace<T, S>& w, const T*
     h->launched("k_gather_t<f32>");
     sv::k_colsum_vt<T><<<S, 256, 0, s>>>(w.Vt.p, op.ld, op.ng, w.colsum.p);
     h->launched("k_colsum_vt<f32>");
-    tsplit = product_from_vt<T, S>(h, op, w, active);
+    tsplit = product_from_vt<T, S>(h, op, w, active, ncols);
   }
   if (use_D && h->mme->nseg > 0) {
     const Mme& mm = *h->mme;
@@ -555,7 +556,7 @@ void run_pcg(cbx_handle* h, Mme& m, const sv::OpView<T>& op, Workspace<T, S>& w,
   }
   auto fused_step = [&](const T* P, T* Pn, bool first) {
     int tsplit = 1;
-    if (op.Qd) tsplit = product_from_vt<T, S>(h, op, w, w.active.p);
+    if (op.Qd) tsplit = product_from_vt<T, S>(h, op, w, w.active.p, ncols);
     sv::FusedArgs<T> a{};
     a.op = op;
     a.Tout = w.Tout.p;

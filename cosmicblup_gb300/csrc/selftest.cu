@@ -107,7 +107,7 @@ extern "C" int cbx_selftest_dense_tc(cbx_handle* h, const float* Q, int64_t ng, 
     dT.resize((size_t)ks * ng * S);
     CBX_CUDA(cudaMemcpyAsync(dQ.p, Q, (size_t)ng * ld * 4, cudaMemcpyHostToDevice, h->stream));
     CBX_CUDA(cudaMemcpyAsync(dV.p, V, (size_t)S * ld * 4, cudaMemcpyHostToDevice, h->stream));
-    cbx::dense_tc(h, dQ.p, ng, ld, dV.p, S, ks, dT.p, nullptr);
+    cbx::dense_tc(h, dQ.p, ng, ld, dV.p, S, ks, dT.p, nullptr, S);
     h->check_status("cbx_selftest_dense_tc");
     std::vector<float> T((size_t)ks * ng * S);
     CBX_CUDA(cudaMemcpyAsync(T.data(), dT.p, T.size() * 4, cudaMemcpyDeviceToHost, h->stream));
