@@ -28,24 +28,30 @@ namespace cbx {
 namespace dtc {
 
 constexpr int KB = 32;                 // FP32 elements per 128-byte row of a tile
-constexpr int NSTAGE = 4;
 constexpr int A_BYTES = 128 * KB * 4;  // 16 KB
 constexpr int THREADS = 320;
+constexpr uint32_t TMEM_ALLOC = 512;
 
 template <int S>
 struct Layout {
-  static constexpr uint32_t TMEM_COLS = 4 * S;         // two accumulator buffers of 2S columns
   static constexpr int B_BYTES = S * KB * 4;             // S rows of 128 bytes
-  static constexpr int OFF_B = 2 * A_BYTES;              // A, A_lo, then B and B_lo back to back
-  static constexpr int OFF_BL = OFF_B + B_BYTES;         // (B_lo rows continue B's 1024-byte groups)
-  static constexpr int STAGE = 2 * A_BYTES + 2 * B_BYTES;
+  // stage: the Qd tile (its tf32 lo part goes to TMEM), then the vector tile
+  // as B_hi rows followed by B_lo rows (one N = 2 nc descriptor covers both)
+  static constexpr int OFF_B = A_BYTES;
+  static constexpr int STAGE = A_BYTES + 2 * B_BYTES;
+  static constexpr int NSTAGE = (227 * 1024 - 1280) / STAGE;  // as deep as shared memory allows
   static_assert(STAGE % 1024 == 0, "stages must stay 1024-byte aligned for SWIZZLE_128B");
   static constexpr int OFF_BAR = NSTAGE * STAGE;
   static constexpr int SMEM = OFF_BAR + 256 + 1024;     // + alignment slack
+  // TMEM: two accumulator buffers of 2S columns, then 32 columns (one K step
+  // of tf32 lo values) per stage
+  static constexpr uint32_t ALO_COL = 4 * S;
+  static_assert(ALO_COL + 32 * NSTAGE <= TMEM_ALLOC, "tensor memory budget");
+  static_assert(NSTAGE <= 12, "barrier arrays");
 };
 
 struct Bars {
-  uint64_t full[NSTAGE], conv[NSTAGE], empty[NSTAGE];
+  uint64_t full[12], conv[12], empty[12];
   uint64_t acc_full[2], acc_empty[2], drain;
   uint32_t tmem;
   int abort;
@@ -94,6 +100,29 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
       : "memory");
 }
 
+// D[tmem] (+)= A[tmem] * B[smem]^T, kind::tf32 (A: 128 lanes = rows, one
+// column per K element)
+__device__ __forceinline__ void umma_tf32_ts(uint32_t d, uint32_t a_tmem, uint64_t b, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n\t}" ::"r"(d),
+      "r"(a_tmem), "l"(b), "r"(idesc), "r"(acc)
+      : "memory");
+}
+// 32 consecutive 32-bit TMEM columns of this thread's lane
+__device__ __forceinline__ void tmem_st32(uint32_t taddr, const uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], "
+      "{%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,"
+      "%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32};" ::"r"(taddr),
+      "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(r[8]),
+      "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15]), "r"(r[16]),
+      "r"(r[17]), "r"(r[18]), "r"(r[19]), "r"(r[20]), "r"(r[21]), "r"(r[22]), "r"(r[23]), "r"(r[24]),
+      "r"(r[25]), "r"(r[26]), "r"(r[27]), "r"(r[28]), "r"(r[29]), "r"(r[30]), "r"(r[31])
+      : "memory");
+}
+__device__ __forceinline__ void tmem_st_wait() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
+
 // lo = a - hi with hi = a's 13 low mantissa bits cleared (the tf32 value the
 // MMA reads); exact in FP32
 __device__ __forceinline__ float4 lo4(const float4& v) {
@@ -112,6 +141,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                  int* status, int nc) {
   if (active && *active == 0) return;
   using LY = Layout<S>;
+  constexpr int NSTAGE = LY::NSTAGE;
   extern __shared__ uint8_t dsm_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(dsm_raw) + 1023) & ~uintptr_t(1023));
   Bars* bars = reinterpret_cast<Bars*>(smem + LY::OFF_BAR);
@@ -131,7 +161,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 1) {
-    tmem_alloc(&bars->tmem, LY::TMEM_COLS);
+    tmem_alloc(&bars->tmem, TMEM_ALLOC);
     tmem_relinquish();
   }
   tc_fence_before();
@@ -181,13 +211,14 @@ __global__ void __launch_bounds__(THREADS, 1)
           if (!mbar_wait(&bars->conv[s], (g / NSTAGE) & 1, abort_flag)) { ok = false; break; }
           tc_fence_after();
           const uint32_t st = smem_addr(smem + s * LY::STAGE);
-          const uint64_t dA = sdesc_sw128(st), dAl = sdesc_sw128(st + A_BYTES);
+          const uint64_t dA = sdesc_sw128(st);
+          const uint32_t aLo = tmem + LY::ALO_COL + 32 * s;   // A_lo of this stage in TMEM
           const uint64_t dB = sdesc_sw128(st + LY::OFF_B);  // N = 2 nc rows: B_hi then B_lo
 #pragma unroll
           for (int j = 0; j < 4; ++j) {  // four K slices of 8 tf32 (32 bytes) per 128-byte row
             const uint32_t first = (k == k0 && j == 0) ? 0u : 1u;
-            umma_tf32(d, dA + 2 * j, dB + 2 * j, ID2, first);      // [A B_hi | A B_lo]
-            umma_tf32(d + nc, dAl + 2 * j, dB + 2 * j, ID1, 1u);   // upper half += A_lo B_hi
+            umma_tf32(d, dA + 2 * j, dB + 2 * j, ID2, first);        // [A B_hi | A B_lo]
+            umma_tf32_ts(d + nc, aLo + 8 * j, dB + 2 * j, ID1, 1u);  // upper half += A_lo B_hi
           }
           umma_commit(&bars->empty[s]);
         }
@@ -201,8 +232,11 @@ __global__ void __launch_bounds__(THREADS, 1)
     }
     __syncwarp();
   } else if (warp < 6) {
-    // converters: the tf32 lo parts of the staged tiles
+    // converters: the tf32 lo part of the Qd tile into TMEM (each warp its
+    // lane quadrant: thread = one row of 32 K elements), the lo part of the
+    // vector tile into shared memory after its hi rows
     const int t = tid - 64;
+    const int row = (warp & 3) * 32 + lane;
     uint32_t g = 0;
     bool ok = true;
     for (int u = blockIdx.x; u < nunits && ok; u += gridDim.x) {
@@ -212,14 +246,25 @@ __global__ void __launch_bounds__(THREADS, 1)
         const uint32_t s = g % NSTAGE;
         if (!mbar_wait(&bars->full[s], (g / NSTAGE) & 1, abort_flag)) { ok = false; break; }
         uint8_t* st = smem + s * LY::STAGE;
-        const float4* A = reinterpret_cast<const float4*>(st);
-        float4* Al = reinterpret_cast<float4*>(st + A_BYTES);
-#pragma unroll 8
-        for (int i = t; i < A_BYTES / 16; i += 128) Al[i] = lo4(A[i]);
+        // row `row` of the SWIZZLE_128B tile: 16-byte chunk c at (c ^ (row & 7)) * 16
+        const uint8_t* arow = st + row * 128;
+        uint32_t lo[32];
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+          const float4 v = *reinterpret_cast<const float4*>(arow + ((c ^ (row & 7)) << 4));
+          const float4 l = lo4(v);
+          lo[4 * c] = __float_as_uint(l.x);
+          lo[4 * c + 1] = __float_as_uint(l.y);
+          lo[4 * c + 2] = __float_as_uint(l.z);
+          lo[4 * c + 3] = __float_as_uint(l.w);
+        }
+        tmem_st32(tmem + (uint32_t((warp & 3) * 32) << 16) + LY::ALO_COL + 32 * s, lo);
         const float4* B = reinterpret_cast<const float4*>(st + LY::OFF_B);
         float4* Bl = reinterpret_cast<float4*>(st + LY::OFF_B + nc * KB * 4);
         for (int i = t; i < nc * KB / 4; i += 128) Bl[i] = lo4(B[i]);
+        tmem_st_wait();
         fence_async_smem();
+        tc_fence_before();
         mbar_arrive(&bars->conv[s]);
       }
     }
@@ -267,7 +312,7 @@ __global__ void __launch_bounds__(THREADS, 1)
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
-  if (warp == 1) tmem_dealloc(tmem, LY::TMEM_COLS);
+  if (warp == 1) tmem_dealloc(tmem, TMEM_ALLOC);
 }
 
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
