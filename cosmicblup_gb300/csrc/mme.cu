@@ -251,7 +251,7 @@ struct Workspace {
     R.resize(n); Z.resize(n); P.resize(n); Q.resize(n); X.resize(n);
     if (m.has_dense) { Vt.resize((size_t)S * m.ld); Tout.resize((size_t)m.ng * S * 8); colsum.resize(S); }
     nblk_vec = (int)grid_for(n, sv::NT, 2 * num_sms);
-    nblk_spmv = (int)m.p + (int)grid_for(m.dim - m.p, 8, 2 * num_sms);
+    nblk_spmv = (int)m.p + (int)grid_for(m.dim - m.p, 8, 4 * num_sms);
     part.resize((size_t)nblk_vec * 3 * S);
     pq_part.resize((size_t)nblk_spmv * S);
     rz_fix.resize((size_t)std::max<int64_t>(m.p, 1) * S);
@@ -492,10 +492,10 @@ void matvec(cbx_handle* h, const sv::OpView<T>& op, Workspace<T, S>& w, const T*
     }
   } else {
     // FP32: gather the dense-block rows, their FP64 column sums, the product
-    sv::k_gather_t<T, S><<<grid_for(S * op.ld, 256, 4 * h->num_sms), 256, 0, s>>>(X, w.Vt.p, op.p, op.ng, op.ld,
+    sv::k_gather_t<T, S><<<grid_for(S * op.ld, 256, 16 * h->num_sms), 256, 0, s>>>(X, w.Vt.p, op.p, op.ng, op.ld,
                                                                                op.gmap, active);
     h->launched("k_gather_t<f32>");
-    sv::k_colsum_vt<T><<<S, 256, 0, s>>>(w.Vt.p, op.ld, op.ng, w.colsum.p);
+    sv::k_colsum_vt<T><<<S, 1024, 0, s>>>(w.Vt.p, op.ld, op.ng, w.colsum.p);
     h->launched("k_colsum_vt<f32>");
     tsplit = product_from_vt<T, S>(h, op, w, active, ncols);
   }
@@ -551,7 +551,7 @@ void run_pcg(cbx_handle* h, Mme& m, const sv::OpView<T>& op, Workspace<T, S>& w,
     sv::k_gather_t<T, S><<<grid_for(S * op.ld, 256, 4 * h->num_sms), 256, 0, s>>>(w.P.p, w.Vt.p, op.p, op.ng, op.ld,
                                                                                op.gmap, nullptr);
     h->launched("k_gather_t<f32>");
-    sv::k_colsum_vt<T><<<S, 256, 0, s>>>(w.Vt.p, op.ld, op.ng, w.colsum.p);
+    sv::k_colsum_vt<T><<<S, 1024, 0, s>>>(w.Vt.p, op.ld, op.ng, w.colsum.p);
     h->launched("k_colsum_vt<f32>");
   }
   auto fused_step = [&](const T* P, T* Pn, bool first) {
@@ -620,7 +620,8 @@ void run_pcg(cbx_handle* h, Mme& m, const sv::OpView<T>& op, Workspace<T, S>& w,
       sv::k_scalar_beta<S><<<1, sv::NTS, 0, s>>>(w.col.p, w.part.p, w.nblk_vec, w.rz_fix.p, m.p, w.tol.p, abs_tol,
                                                  maxit, w.active.p);
       h->launched(sizeof(T) == 4 ? "k_scalar_beta<f32>" : "k_scalar_beta<f64>");
-      sv::k_pupdate<T, S><<<w.nblk_vec, sv::NT, 0, s>>>(m.dim, w.col.p, w.Z.p, w.P.p);
+      sv::k_pupdate<T, S><<<grid_for(m.dim * S, sv::NT, 16 * h->num_sms), sv::NT, 0, s>>>(m.dim, w.col.p, w.Z.p,
+                                                                                           w.P.p);
       h->launched(sizeof(T) == 4 ? "k_pupdate<f32>" : "k_pupdate<f64>");
     }
   };

@@ -78,6 +78,13 @@ struct Mme {
   std::vector<double> probe_lam;   // per stored column
   std::vector<char> probe_r_ok;    // residual column valid (mixed-precision solve)
   int probe_seed = -1;
+  // right-hand sides of the EM iteration, column-major dim x (1 + max probes):
+  // column 0 = W'y, column 1 + j = [0; z_j] for Rademacher probe j.  The
+  // probe stream restarts at the same seed every iteration, so each batch of
+  // probes is generated on the host and uploaded once (probe_have[j]).
+  DevBuf<double> em_B;
+  std::vector<char> probe_have;
+  int em_B_seed = -1;
   void drop_carry() {
     has_last = has_last_resid = false;
     probe_lam.clear();

@@ -209,6 +209,40 @@ static double y_variance(const Mme& m) {
   return std::max(1e-12, m.yty);
 }
 
+// out[c] = sum_i A[c * lda + i] * B[c * ldb + i] for i < n, one block per
+// column, summed in a fixed order.
+__global__ void __launch_bounds__(256) k_coldot(const double* __restrict__ A, int64_t lda,
+                                                const double* __restrict__ B, int64_t ldb, int64_t n,
+                                                double* __restrict__ out) {
+  __shared__ double red[256];
+  const int c = blockIdx.x, tid = threadIdx.x;
+  const double* a = A + (int64_t)c * lda;
+  const double* b = B + (int64_t)c * ldb;
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  int64_t i = tid;
+  for (; i + 3 * 256 < n; i += 4 * 256) {
+#pragma unroll
+    for (int u = 0; u < 4; ++u) acc[u] += a[i + u * 256] * b[i + u * 256];
+  }
+  for (; i < n; i += 256) acc[0] += a[i] * b[i];
+  red[tid] = (acc[0] + acc[1]) + (acc[2] + acc[3]);
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (tid < o) red[tid] += red[tid + o];
+    __syncthreads();
+  }
+  if (tid == 0) out[c] = red[0];
+}
+
+static std::vector<double> coldots(cbx_handle* h, const double* A, int64_t lda, const double* B, int64_t ldb,
+                                   int64_t n, int ncols) {
+  DevBuf<double> out;
+  out.resize(ncols);
+  k_coldot<<<ncols, 256, 0, h->stream>>>(A, lda, B, ldb, n, out.p);
+  h->launched("k_coldot");
+  return d2h(h, out.p, ncols);
+}
+
 // One EM iteration (vce.cpp:1490-1574).
 //
 // The reference solves the data system, then the probe batches of the
@@ -250,11 +284,32 @@ static void em_iteration(cbx_handle* h, const RemlConfigI& cfg, double& vu, doub
     m.probe_r_ok.clear();
   }
 
+  // right-hand sides: W'y and the probe columns, generated once per seed
+  if (m.em_B_seed != cfg.seed || m.em_B.n < (size_t)dim * (1 + max_s)) {
+    m.em_B.resize((size_t)dim * (1 + max_s));
+    m.em_B.zero(s);
+    m.probe_have.assign(max_s, 0);
+    m.em_B_seed = cfg.seed;
+  }
+  CBX_CUDA(cudaMemcpyAsync(m.em_B.p, m.rhs.p, dim * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  auto ensure_batch = [&](int start, int size) {
+    if (m.probe_have[start]) return;
+    std::vector<double> Zb((size_t)q * size);
+    std::mt19937_64 gen((unsigned long)(cfg.seed + start));
+    std::uniform_int_distribution<int> dist(0, 1);
+    for (int j = 0; j < size; ++j)
+      for (int64_t i = 0; i < q; ++i) Zb[(size_t)j * q + i] = dist(gen) == 0 ? -1.0 : 1.0;
+    // the u rows of columns 1 + start .. (the fixed rows stay zero)
+    CBX_CUDA(cudaMemcpy2DAsync(m.em_B.p + (size_t)(1 + start) * dim + p, dim * sizeof(double), Zb.data(),
+                               q * sizeof(double), q * sizeof(double), size, cudaMemcpyHostToDevice, s));
+    CBX_CUDA(cudaStreamSynchronize(s));
+    for (int j = 0; j < size; ++j) m.probe_have[start + j] = 1;
+  };
+
   // the probe group starting at `done`: batches solved before the next check
   struct Group {
     std::vector<std::pair<int, int>> batches;  // (start, size)
     int k = 0;
-    std::vector<double> Z;                     // q x k
   };
   auto make_group = [&](int done) {
     Group g;
@@ -265,14 +320,7 @@ static void em_iteration(cbx_handle* h, const RemlConfigI& cfg, double& vu, doub
       next += sz;
     } while (next < min_s && next < max_s);
     g.k = next - done;
-    g.Z.resize((size_t)q * g.k);
-    int col = 0;
-    for (auto& bt : g.batches) {
-      std::mt19937_64 gen((unsigned long)(cfg.seed + bt.first));
-      std::uniform_int_distribution<int> dist(0, 1);
-      for (int j = 0; j < bt.second; ++j, ++col)
-        for (int64_t i = 0; i < q; ++i) g.Z[(size_t)col * q + i] = dist(gen) == 0 ? -1.0 : 1.0;
-    }
+    for (auto& bt : g.batches) ensure_batch(bt.first, bt.second);
     return g;
   };
   // The probe stream restarts at the same seed every REML iteration, so the
@@ -304,22 +352,15 @@ static void em_iteration(cbx_handle* h, const RemlConfigI& cfg, double& vu, doub
 
   int done = 0;
   Group g0 = make_group(0);
-  DevBuf<double> B, X, QW;
+  DevBuf<double> X, QW;
   // --- 1. the data solve (with the first probe group in mixed precision)
   const bool data_warm = m.has_last;
   const bool merge = mixed && data_warm == probes_warm(0, g0.k);
   if (merge) {
     const int k = g0.k, nc = 1 + k;
-    std::vector<double> Bh((size_t)dim * nc, 0.0);
-    CBX_CUDA(cudaMemcpyAsync(Bh.data(), m.rhs.p, dim * sizeof(double), cudaMemcpyDeviceToHost, s));
-    CBX_CUDA(cudaStreamSynchronize(s));
-    for (int c = 0; c < k; ++c)
-      for (int64_t i = 0; i < q; ++i) Bh[(size_t)(1 + c) * dim + p + i] = g0.Z[(size_t)c * q + i];
-    B.resize((size_t)dim * nc);
     X.resize((size_t)dim * nc);
     DevBuf<double> R;
     R.resize((size_t)dim * nc);
-    CBX_CUDA(cudaMemcpyAsync(B.p, Bh.data(), Bh.size() * sizeof(double), cudaMemcpyHostToDevice, s));
     const bool carry = data_warm && m.has_last_resid && probes_carry(0, k) && m.last_lam == m.probe_lam[0];
     if (data_warm) {
       CBX_CUDA(cudaMemcpyAsync(X.p, m.last_solution.p, dim * sizeof(double), cudaMemcpyDeviceToDevice, s));
@@ -336,7 +377,7 @@ static void em_iteration(cbx_handle* h, const RemlConfigI& cfg, double& vu, doub
     rc.dlam = carry ? lam - m.last_lam : 0.0;
     rc.r_out = R.p;
     PcgResult pr;
-    pcg_solve(h, lam, nc, B.p, X.p, data_warm, cfg.pcg_tol, cfg.pcg_max_iter, 0, cfg.precision, pr, &rc);
+    pcg_solve(h, lam, nc, m.em_B.p, X.p, data_warm, cfg.pcg_tol, cfg.pcg_max_iter, 0, cfg.precision, pr, &rc);
     if (h->trace_on) h->trace_mark("#em: data + probe solve");
     info.matvecs += pr.matvecs;
     count(pr, 0, 1, "non-finite data solve");
@@ -372,9 +413,7 @@ static void em_iteration(cbx_handle* h, const RemlConfigI& cfg, double& vu, doub
     qinv_from_solution(h, lam, 1, m.rhs.p, m.last_solution.p, m.last_resid.p, Qu.p);
   else
     qinv_apply(h, 1, m.last_solution.p + p, Qu.p);
-  const auto u_h = d2h(h, m.last_solution.p + p, q);
-  const auto Qu_h = d2h(h, Qu.p, q);
-  const double uQu = dot_h(u_h, Qu_h);
+  const double uQu = coldots(h, m.last_solution.p + p, q, Qu.p, q, q, 1)[0];
   if (h->trace_on) h->trace_mark("#em: e'e and u'Qinv u");
   // --- 4. Hutchinson trace of Qinv C^uu
   double tsum = 0, tsq = 0;
@@ -385,18 +424,13 @@ static void em_iteration(cbx_handle* h, const RemlConfigI& cfg, double& vu, doub
     const int k = g.k;
     // B / X / residual columns of this group (dim x k each)
     const double *Bg, *Xg, *Rg;
-    DevBuf<double> Bp, Xp;
+    DevBuf<double> Xp;
     if (first && merge) {
-      Bg = B.p + dim;
+      Bg = m.em_B.p + dim;
       Xg = m.probe_x.p;
       Rg = m.probe_r.p;
     } else {
-      std::vector<double> Bh((size_t)dim * k, 0.0);
-      for (int c = 0; c < k; ++c)
-        for (int64_t i = 0; i < q; ++i) Bh[(size_t)c * dim + p + i] = g.Z[(size_t)c * q + i];
-      Bp.resize((size_t)dim * k);
       Xp.resize((size_t)dim * k);
-      CBX_CUDA(cudaMemcpyAsync(Bp.p, Bh.data(), Bh.size() * sizeof(double), cudaMemcpyHostToDevice, s));
       const bool warm = probes_warm(done, k), carry = probes_carry(done, k);
       if (warm)
         CBX_CUDA(cudaMemcpyAsync(Xp.p, m.probe_x.p + (size_t)done * dim, (size_t)dim * k * sizeof(double),
@@ -406,14 +440,15 @@ static void em_iteration(cbx_handle* h, const RemlConfigI& cfg, double& vu, doub
       pc.dlam = carry ? lam - m.probe_lam[done] : 0.0;
       pc.r_out = m.probe_r.p + (size_t)done * dim;
       PcgResult pr;
-      pcg_solve(h, lam, k, Bp.p, Xp.p, warm, cfg.pcg_tol, cfg.pcg_max_iter, 0, cfg.precision, pr, &pc);
+      pcg_solve(h, lam, k, m.em_B.p + (size_t)(1 + done) * dim, Xp.p, warm, cfg.pcg_tol, cfg.pcg_max_iter, 0,
+                cfg.precision, pr, &pc);
       if (h->trace_on) h->trace_mark("#em: probe solve");
       CBX_CUDA(cudaMemcpyAsync(m.probe_x.p + (size_t)done * dim, Xp.p, (size_t)dim * k * sizeof(double),
                                cudaMemcpyDeviceToDevice, s));
       record_probes(done, k);
       count(pr, 0, k, "non-finite probe solve");
       info.matvecs += pr.matvecs;
-      Bg = Bp.p;
+      Bg = m.em_B.p + (size_t)(1 + done) * dim;
       Xg = Xp.p;
       Rg = m.probe_r.p + (size_t)done * dim;
     }
@@ -430,13 +465,13 @@ static void em_iteration(cbx_handle* h, const RemlConfigI& cfg, double& vu, doub
                                  cudaMemcpyDeviceToDevice, s));
       qinv_apply(h, k, Wu.p, QW.p);
     }
-    const auto QWh = d2h(h, QW.p, (size_t)q * k);
+    // z' Qinv C^uu z per probe (the u rows of the probe columns are z)
+    const std::vector<double> zv = coldots(h, Bg + p, dim, QW.p, q, q, k);
     int col = 0;
     for (auto& bt : g.batches) {
       double bs = 0, bq = 0;
       for (int j = 0; j < bt.second; ++j, ++col) {
-        double v = 0;
-        for (int64_t i = 0; i < q; ++i) v += g.Z[(size_t)col * q + i] * QWh[(size_t)col * q + i];
+        const double v = zv[col];
         bs += v;
         bq += v * v;
       }

@@ -276,15 +276,21 @@ static __global__ void __launch_bounds__(256) k_colsum_x(const double* __restric
 // sum of FP32 values with 29 spare bits, so cancellation costs nothing that
 // the FP32 solve can see).  One block of 256 threads per column, fixed order.
 template <typename T>
-__global__ void __launch_bounds__(256) k_colsum_vt(const T* __restrict__ Vt, int64_t ld, int64_t ng,
-                                                   double* __restrict__ out) {
-  __shared__ double red[256];
+__global__ void __launch_bounds__(1024) k_colsum_vt(const T* __restrict__ Vt, int64_t ld, int64_t ng,
+                                                    double* __restrict__ out) {
+  __shared__ double red[1024];
   const int c = blockIdx.x, tid = threadIdx.x;
-  double acc = 0.0;
-  for (int64_t k = tid; k < ng; k += 256) acc += (double)Vt[(int64_t)c * ld + k];
-  red[tid] = acc;
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  const T* col = Vt + (int64_t)c * ld;
+  int64_t k = tid;
+  for (; k + 3 * 1024 < ng; k += 4 * 1024) {
+#pragma unroll
+    for (int u = 0; u < 4; ++u) acc[u] += (double)col[k + u * 1024];
+  }
+  for (; k < ng; k += 1024) acc[0] += (double)col[k];
+  red[tid] = (acc[0] + acc[1]) + (acc[2] + acc[3]);
   __syncthreads();
-  for (int o = 128; o > 0; o >>= 1) {
+  for (int o = 512; o > 0; o >>= 1) {
     if (tid < o) red[tid] += red[tid + o];
     __syncthreads();
   }
@@ -727,18 +733,25 @@ __device__ __forceinline__ void col_sums(const double* __restrict__ part, int nb
   const int t = threadIdx.x;
   const int G = blockDim.x / S;
   const int c = t % S, g = t / S;
-  // 8 independent partial sums per thread keep 8 loads in flight; they are
+  // 16 independent partial sums per thread keep 16 loads in flight; they are
   // combined in a fixed order, so the total does not depend on timing
-  double v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  constexpr int U = 16;
+  double v[U];
+#pragma unroll
+  for (int u = 0; u < U; ++u) v[u] = 0.0;
   if (g < G) {
     int b = g;
-    for (; b + 7 * G < nblk; b += 8 * G) {
+    for (; b + (U - 1) * G < nblk; b += U * G) {
 #pragma unroll
-      for (int u = 0; u < 8; ++u) v[u] += part[(int64_t)(b + u * G) * stride + c];
+      for (int u = 0; u < U; ++u) v[u] += part[(int64_t)(b + u * G) * stride + c];
     }
     for (; b < nblk; b += G) v[0] += part[(int64_t)b * stride + c];
   }
-  red[t] = ((v[0] + v[1]) + (v[2] + v[3])) + ((v[4] + v[5]) + (v[6] + v[7]));
+#pragma unroll
+  for (int w = U / 2; w > 0; w >>= 1)
+#pragma unroll
+    for (int u = 0; u < w; ++u) v[u] += v[u + w];
+  red[t] = v[0];
   __syncthreads();
   if (t < S) {
     double a = 0.0;
@@ -761,6 +774,7 @@ __global__ void k_scalar_init(Col* col, int ncols, const double* part, int nblk,
   }
   col_sums<S>(rz_fix, (int)p, S, red);
   const int c = threadIdx.x;
+  int act = 0;
   if (c < S) {
     const double rr = sums[0][c], rz = sums[1][c] + (p > 0 ? red[c] : 0.0), bb = sums[2][c];
     Col s{};
@@ -773,13 +787,10 @@ __global__ void k_scalar_init(Col* col, int ncols, const double* part, int nblk,
     // MatrixFreePCG returns at once when ||r0|| < 1e-20 (matrix_free_pcg.h:31)
     if (c < ncols && abs_tol && sqrt(rr) < 1e-20) { s.active = 0; s.status = COL_CONVERGED; }
     col[c] = s;
+    act = s.active;
   }
-  __syncthreads();
-  if (c == 0) {
-    int a = 0;
-    for (int k = 0; k < S; ++k) a += col[k].active;
-    *active_count = a;
-  }
+  const int n_act = __syncthreads_count(act);
+  if (c == 0) *active_count = n_act;
 }
 
 // alpha = rz / p'Ap, breakdown handling (pcg_solver.h:482-498).
@@ -823,6 +834,7 @@ __global__ void k_scalar_beta(Col* col, const double* part, int nblk, const doub
   }
   col_sums<S>(rz_fix, (int)p, S, red);
   const int c = threadIdx.x;
+  int act = 0;
   if (c < S) {
     Col s = col[c];
     if (s.active) {
@@ -854,13 +866,10 @@ __global__ void k_scalar_beta(Col* col, const double* part, int nblk, const doub
       }
     }
     col[c] = s;
+    act = s.active;
   }
-  __syncthreads();
-  if (c == 0) {
-    int a = 0;
-    for (int k = 0; k < S; ++k) a += col[k].active;
-    *active_count = a;
-  }
+  const int n_act = __syncthreads_count(act);
+  if (c == 0) *active_count = n_act;
 }
 
 // Partial sums of squares per column (interleaved layout).
