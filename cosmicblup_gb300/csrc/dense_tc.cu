@@ -11,13 +11,17 @@
 // This replaces, for probe blocks, the CUDA-core product of DenseMatrixAdapter /
 // SplitMatrixAdapter (reference src/core/matrix_adapter.h:125-127, 252-278)
 // applied to every probe of AdaptiveTraceEstimator.  One persistent CTA per SM
-// walks (128-row tile, K split) work units:
+// takes an equal contiguous share of the (128-row tile, K step) space (a
+// stream-K split: a tile is cut where a CTA's share ends, so every SM gets the
+// same number of K steps and a tile has at most a few partial sums):
 //   warp 0  TMA producer (SWIZZLE_128B tiles of Qd and Vt),
 //   warp 1  TMEM owner and MMA issuer (kind::tf32, M = 128, N = 2S and S),
 //   warps 2-5 write the tf32 lo parts of each staged tile to shared memory,
 //   warps 6-9 epilogue (TMEM -> partial sums in global memory).
-// The K splits are summed in a fixed order by the consumer (k_spmv), so the
-// result is deterministic.
+// Each tile's partial sums go to fixed slots (the CTA's rank among those
+// covering the tile; the CTA finishing a tile zeroes its unused slots) and are
+// summed in slot order by the consumer (k_spmv), so the result is
+// deterministic.
 #include <cuda.h>
 #include <algorithm>
 #include <vector>
@@ -137,7 +141,7 @@ __device__ __forceinline__ float4 lo4(const float4& v) {
 template <int S>
 __global__ void __launch_bounds__(THREADS, 1)
     k_dense_tf32(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int ng,
-                 int ksteps, int ksplit, int kps, int nunits, float* __restrict__ Tpart, const int* active,
+                 int ksteps, int total, int per, int nslot, float* __restrict__ Tpart, const int* active,
                  int* status, int nc) {
   if (active && *active == 0) return;
   using LY = Layout<S>;
@@ -178,9 +182,10 @@ __global__ void __launch_bounds__(THREADS, 1)
     if (lane == 0) {
       uint32_t g = 0;
       bool ok = true;
-      for (int u = blockIdx.x; u < nunits && ok; u += gridDim.x) {
-        const int mt = u / ksplit, ks = u % ksplit;
-        const int k0 = ks * kps, k1 = min(ksteps, k0 + kps);
+      const int seg_end = min(total, (int)blockIdx.x * per + per);
+      for (int pos = blockIdx.x * per; pos < seg_end && ok;) {
+        const int mt = pos / ksteps, k0 = pos - mt * ksteps, k1 = min(ksteps, k0 + (seg_end - pos));
+        pos += k1 - k0;
         for (int k = k0; k < k1; ++k, ++g) {
           const uint32_t s = g % NSTAGE;
           if (!mbar_wait(&bars->empty[s], ((g / NSTAGE) & 1) ^ 1, abort_flag)) { ok = false; break; }
@@ -199,9 +204,10 @@ __global__ void __launch_bounds__(THREADS, 1)
       const uint32_t ID2 = idesc_tf32(128, 2 * nc), ID1 = idesc_tf32(128, nc);
       uint32_t g = 0, c = 0;
       bool ok = true;
-      for (int u = blockIdx.x; u < nunits && ok; u += gridDim.x, ++c) {
-        const int ks = u % ksplit;
-        const int k0 = ks * kps, k1 = min(ksteps, k0 + kps);
+      const int seg_end = min(total, (int)blockIdx.x * per + per);
+      for (int pos = blockIdx.x * per; pos < seg_end && ok; ++c) {
+        const int mt = pos / ksteps, k0 = pos - mt * ksteps, k1 = min(ksteps, k0 + (seg_end - pos));
+        pos += k1 - k0;
         const uint32_t b = c & 1;
         if (!mbar_wait(&bars->acc_empty[b], ((c >> 1) & 1) ^ 1, abort_flag)) { ok = false; break; }
         tc_fence_after();
@@ -239,9 +245,10 @@ __global__ void __launch_bounds__(THREADS, 1)
     const int row = (warp & 3) * 32 + lane;
     uint32_t g = 0;
     bool ok = true;
-    for (int u = blockIdx.x; u < nunits && ok; u += gridDim.x) {
-      const int ks = u % ksplit;
-      const int k0 = ks * kps, k1 = min(ksteps, k0 + kps);
+    const int seg_end = min(total, (int)blockIdx.x * per + per);
+    for (int pos = blockIdx.x * per; pos < seg_end && ok;) {
+      const int mt = pos / ksteps, k0 = pos - mt * ksteps, k1 = min(ksteps, k0 + (seg_end - pos));
+      pos += k1 - k0;
       for (int k = k0; k < k1; ++k, ++g) {
         const uint32_t s = g % NSTAGE;
         if (!mbar_wait(&bars->full[s], (g / NSTAGE) & 1, abort_flag)) { ok = false; break; }
@@ -274,8 +281,12 @@ __global__ void __launch_bounds__(THREADS, 1)
     const int q = warp & 3;
     uint32_t c = 0;
     bool ok = true;
-    for (int u = blockIdx.x; u < nunits && ok; u += gridDim.x, ++c) {
-      const int mt = u / ksplit, ks = u % ksplit;
+    const int seg_end = min(total, (int)blockIdx.x * per + per);
+    for (int pos = blockIdx.x * per; pos < seg_end && ok; ++c) {
+      const int mt = pos / ksteps, k0 = pos - mt * ksteps, k1 = min(ksteps, k0 + (seg_end - pos));
+      pos += k1 - k0;
+      // slot: this CTA's rank among the CTAs that cover the tile
+      const int ks = (int)blockIdx.x - (mt * ksteps) / per;
       const uint32_t b = c & 1;
       if (!mbar_wait(&bars->acc_full[b], (c >> 1) & 1, abort_flag)) { ok = false; break; }
       tc_fence_after();
@@ -305,6 +316,14 @@ __global__ void __launch_bounds__(THREADS, 1)
 #pragma unroll
         for (int j = 0; j < S / 4; ++j)
           dst[j] = make_float4(out[4 * j], out[4 * j + 1], out[4 * j + 2], out[4 * j + 3]);
+        if (k1 == ksteps) {
+          // the tile ends here: its slots after this one hold nothing
+          for (int z = ks + 1; z < nslot; ++z) {
+            float4* zd = reinterpret_cast<float4*>(Tpart + ((int64_t)z * ng + row) * S);
+#pragma unroll
+            for (int j = 0; j < S / 4; ++j) zd[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+          }
+        }
       }
     }
     if (!ok) fail();
@@ -346,25 +365,28 @@ static CUtensorMap make_map(const float* base, int64_t cols, int64_t rows, int b
 
 }  // namespace dtc
 
-int dense_tc_ksplit(int64_t ng, int64_t ld, int num_sms) {
+// Stream-K split of the (tile, K step) space: CTA b takes steps [b per,
+// (b + 1) per).  Returns the number of partial slots a tile can need (the
+// consumer's split count); per and grid are chosen so that it stays <= 8.
+static int stream_k(int64_t ng, int64_t ld, int num_sms, int* grid_out, int* per_out) {
   const int mtiles = (int)((ng + 127) / 128);
   const int ksteps = (int)((ld + dtc::KB - 1) / dtc::KB);
-  int best = 1;
-  double best_eff = -1;
-  for (int ks = 1; ks <= 8 && ks <= ksteps; ++ks) {
-    // every split must own at least one K step: use the effective split count
-    const int kps = (ksteps + ks - 1) / ks;
-    const int eff_ks = (ksteps + kps - 1) / kps;
-    const int units = mtiles * eff_ks;
-    const int waves = (units + num_sms - 1) / num_sms;
-    const double eff = (double)units / ((double)waves * num_sms);
-    if (eff > best_eff + 0.02) {
-      best_eff = eff;
-      best = eff_ks;
-    }
+  const int total = mtiles * ksteps;
+  int grid = std::max(1, std::min(num_sms, total));
+  int per = (total + grid - 1) / grid;
+  per = std::max(per, (ksteps + 6) / 7);   // at most 8 CTAs on any tile
+  grid = (total + per - 1) / per;
+  int nslot = 1;
+  for (int t = 0; t < mtiles; ++t) {
+    const int first = (t * ksteps) / per, last = ((t + 1) * ksteps - 1) / per;
+    nslot = std::max(nslot, last - first + 1);
   }
-  return best;
+  if (grid_out) *grid_out = grid;
+  if (per_out) *per_out = per;
+  return nslot;
 }
+
+int dense_tc_ksplit(int64_t ng, int64_t ld, int num_sms) { return stream_k(ng, ld, num_sms, nullptr, nullptr); }
 
 void dense_tc(cbx_handle* h, const float* Qd, int64_t ng, int64_t ld, const float* Vt, int S, int ksplit, float* Tpart,
               const int* active, int ncols) {
@@ -376,25 +398,25 @@ void dense_tc(cbx_handle* h, const float* Qd, int64_t ng, int64_t ld, const floa
   const CUtensorMap ma = dtc::make_map(Qd, ld, ng, 128);
   const CUtensorMap mb = dtc::make_map(Vt, ld, S, nc);
   const int ksteps = (int)((ld + dtc::KB - 1) / dtc::KB);
-  const int kps = (ksteps + ksplit - 1) / ksplit;
-  CBX_REQUIRE((int64_t)(ksplit - 1) * kps < ksteps, CBX_ERR_ARG, "K split leaves an empty split");
   const int mtiles = (int)((ng + 127) / 128);
-  const int nunits = mtiles * ksplit;
-  const int grid = std::min(nunits, h->num_sms);
+  const int total = mtiles * ksteps;
+  int grid = 0, per = 0;
+  const int nslot = stream_k(ng, ld, h->num_sms, &grid, &per);
+  CBX_REQUIRE(nslot == ksplit, CBX_ERR_ARG, "partial slot count does not match dense_tc_ksplit");
   if (S == 64) {
     constexpr int SM = dtc::Layout<64>::SMEM;
     ensure_smem((const void*)dtc::k_dense_tf32<64>, SM, h->device);
-    dtc::k_dense_tf32<64><<<grid, dtc::THREADS, SM, h->stream>>>(ma, mb, (int)ng, ksteps, ksplit, kps, nunits, Tpart,
+    dtc::k_dense_tf32<64><<<grid, dtc::THREADS, SM, h->stream>>>(ma, mb, (int)ng, ksteps, total, per, nslot, Tpart,
                                                                  active, h->status.p, nc);
   } else if (S == 32) {
     constexpr int SM = dtc::Layout<32>::SMEM;
     ensure_smem((const void*)dtc::k_dense_tf32<32>, SM, h->device);
-    dtc::k_dense_tf32<32><<<grid, dtc::THREADS, SM, h->stream>>>(ma, mb, (int)ng, ksteps, ksplit, kps, nunits, Tpart,
+    dtc::k_dense_tf32<32><<<grid, dtc::THREADS, SM, h->stream>>>(ma, mb, (int)ng, ksteps, total, per, nslot, Tpart,
                                                                  active, h->status.p, nc);
   } else {
     constexpr int SM = dtc::Layout<16>::SMEM;
     ensure_smem((const void*)dtc::k_dense_tf32<16>, SM, h->device);
-    dtc::k_dense_tf32<16><<<grid, dtc::THREADS, SM, h->stream>>>(ma, mb, (int)ng, ksteps, ksplit, kps, nunits, Tpart,
+    dtc::k_dense_tf32<16><<<grid, dtc::THREADS, SM, h->stream>>>(ma, mb, (int)ng, ksteps, total, per, nslot, Tpart,
                                                                  active, h->status.p, nc);
   }
   h->launched("k_dense_tf32");
