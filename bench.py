@@ -291,6 +291,53 @@ def run_batch(args, cfg):
     print(json.dumps(line))
 
 
+def run_geno(h, bed, n, m, seed, hbm_peak, want_host, reps: int = 5) -> dict:
+    """SNP-effect back-solve and the genotype products on the resident BED payload.
+
+    snp_effects_ms is end to end (u_g up, G^-1 u on the device, Z^T q, effects down);
+    the kernel figures come from CUDA events around each k_geno_zt / k_geno_z launch.
+    """
+    from cosmicblup_gb300 import DeviceGenotypes
+    t0 = time.perf_counter()
+    dg = DeviceGenotypes(bed, n, m, h)
+    attach_s = time.perf_counter() - t0
+    rng = np.random.default_rng(seed + 11)
+    u = rng.standard_normal(n)
+    w = rng.standard_normal(m)
+    dg.snp_effects(u)
+    dg.multiply_Z_v(w)
+    h.profile(True)
+    h.timer_start()
+    for _ in range(reps):
+        dg.snp_effects(u)
+    ms_eff = h.timer_stop() / reps
+    zl, zms, zbytes = h.profile_read(3)
+    h.profile(True)
+    for _ in range(reps):
+        dg.multiply_Z_v(w)
+    yl, yms, ybytes = h.profile_read(4)
+    h.profile(False)
+    out = {"workload": f"n={n} samples, m={m} SNPs, one vector", "attach_s": attach_s,
+           "snp_effects_ms": ms_eff,
+           "k_geno_zt_ms": zms / zl, "k_geno_zt_GBps": zbytes / (zms * 1e-3) / 1e9,
+           "k_geno_zt_frac_hbm": zbytes / (zms * 1e-3) / 1e9 / hbm_peak,
+           "k_geno_z_ms": yms / yl, "k_geno_z_GBps": ybytes / (yms * 1e-3) / 1e9,
+           "elements_per_s_zt": n * m / (zms / zl * 1e-3),
+           "note": "exact 64-bit fixed-point sums; integer-issue bound (3 masked 64-bit adds per code)"}
+    if want_host:
+        # the oracle's Z^T v (numpy, all threads) on a bounded SNP sample, scaled to m
+        from oracle.geno import compute_stats, multiply_zt_v
+        from oracle.plink import decode_bed
+        ms_ = min(m, 2000)
+        g = decode_bed(bed[:3 + ms_ * ((n + 3) // 4)], n, ms_)
+        mean, inv = compute_stats(g)
+        t0 = time.perf_counter()
+        multiply_zt_v(g, mean, inv, u)
+        out["cpu_port_zt_ms"] = (time.perf_counter() - t0) * 1e3 * m / ms_
+        out["cpu_port_sample"] = f"oracle multiply_zt_v on {ms_} of {m} SNPs, scaled"
+    return out
+
+
 def run_gpu(args, cfg):
     import ctypes as C
     from cosmicblup_gb300 import AIREML, DeviceMME, Handle, RemlConfig, invert_psd
@@ -425,6 +472,11 @@ def run_gpu(args, cfg):
     e2e = {"value": world * e2e_steps / (ms_e2e * 1e-3), "unit": UNIT,
            "h2d_bytes_per_step": int(h2d_bytes), "d2h_bytes_per_step": int(d2h_bytes)}
 
+    # ---- genotype products: SNP-effect back-solve effect = Z^T G^-1 u / total 2pq ----
+    geno = None
+    if not ss:
+        geno = run_geno(h, bed, n, m, cfg["seed"], hbm_peak, want_host)
+
     # ---- CPU baseline: the oracle's FP64 PCG on this operator, bounded sample ----
     cpu = None
     if want_host and fp64 is not None:
@@ -472,6 +524,7 @@ def run_gpu(args, cfg):
         "fp64": fp64,
         "mixed_vs_fp64": (value / world) / fp64["reml_iter_per_s"] if fp64 else None,
         "grm": grm,
+        "snp_backsolve": geno,
         "setup": phases,
         "clocks": clk,
         "e2e": e2e,

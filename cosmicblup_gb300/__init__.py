@@ -11,9 +11,10 @@ from .vce import AIREML, RemlConfig, final_solve, invert_psd, reml_gradient, rem
 from .ped import ainv_henderson, ssgblup_qinv  # noqa: F401
 from .mt import MvEigenVce, MvOptions, solve_multi_trait  # noqa: F401
 from .batch import BatchProblem, BatchResult, batch_reml  # noqa: F401
+from .geno import DeviceGenotypes  # noqa: F401
 
 __all__ = ["CbxError", "Handle", "lib", "GrmBuilder", "GrmOptions", "PlinkReader",
            "bed_snp_counts", "DeviceMME", "AIREML", "RemlConfig", "final_solve", "invert_psd",
            "reml_gradient", "reml_logl_dense",
            "ainv_henderson", "ssgblup_qinv", "MvEigenVce", "MvOptions", "solve_multi_trait",
-           "BatchProblem", "BatchResult", "batch_reml"]
+           "BatchProblem", "BatchResult", "batch_reml", "DeviceGenotypes"]

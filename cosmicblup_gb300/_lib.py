@@ -38,6 +38,12 @@ SIGNATURES = [
     ("cbx_sync", C.c_int, [C.c_void_p]),
     ("cbx_bed_snp_counts", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_int64,
                                      C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("cbx_geno_attach", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.c_void_p,
+                                  C.c_void_p]),
+    ("cbx_geno_zt_v", C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
+    ("cbx_geno_z_v", C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
+    ("cbx_snp_effects", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
+                                  C.POINTER(C.c_double)]),
     ("cbx_grm_bed", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.c_float,
                               C.c_int, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
                               C.POINTER(C.c_double), C.POINTER(C.c_int64)]),

@@ -32,6 +32,8 @@ struct cbx_handle {
   // library handles (cuSOLVER / cuBLAS) and dense exact AI state, owned here
   std::shared_ptr<void> libs_slot;
   std::shared_ptr<void> dense_slot;
+  // genotypes kept on the device by cbx_geno_attach (matrix-free Z / Z^T products)
+  std::shared_ptr<void> geno_slot;
 
   // optional per-launch timing of the dense block product (bench roofline):
   // bucket 0 = FP32 launches, bucket 1 = FP64 launches

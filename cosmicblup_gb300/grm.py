@@ -55,6 +55,29 @@ class PlinkReader:
     def getBytesPerSnp(self) -> int:
         return (self.num_samples + 3) // 4
 
+    # RHE / PCG support (src/core/plink_reader.h:100-125): the payload moves to
+    # the device on the first call and the products run there.
+    def computeStats(self, handle: Handle | None = None) -> None:
+        from .geno import DeviceGenotypes
+        if getattr(self, "_dev", None) is None:
+            self._dev = DeviceGenotypes(self.bed, self.num_samples, self.num_snps, handle)
+
+    def getMeans(self) -> np.ndarray:
+        self.computeStats()
+        return self._dev.getMeans()
+
+    def getInvStds(self) -> np.ndarray:
+        self.computeStats()
+        return self._dev.getInvStds()
+
+    def multiply_Z_v(self, v: np.ndarray) -> np.ndarray:
+        self.computeStats()
+        return self._dev.multiply_Z_v(v)
+
+    def multiply_Zt_v(self, v: np.ndarray) -> np.ndarray:
+        self.computeStats()
+        return self._dev.multiply_Zt_v(v)
+
 
 @dataclass
 class GrmOptions:

@@ -61,6 +61,35 @@ int cbx_bed_snp_counts(cbx_handle* h, const uint8_t* bed, int64_t bed_bytes,
                        int64_t n, int64_t m, int32_t* n_obs, int32_t* sum_x,
                        int32_t* n_hom1, int32_t* n_het, int32_t* n_hom2);
 
+/* ---- Genotype matrix-free products ---------------------------------------
+ * cbx_geno_attach replaces PlinkReader::openBed + computeStats
+ * (src/core/plink_reader.cpp:66-91, 186-237): the payload of the whole .bed file
+ * (bed_bytes, magic included) is copied to the device once and kept in the handle
+ * for the products below.  Per SNP: mean = sum of the observed codes' allele-1
+ * counts / observed calls, p = mean / 2, var = 2p(1-p), inv_std = 1 / sqrt(var),
+ * or 0 when var < 1e-9 or nothing is observed (bit-identical to the reference's
+ * FP64 arithmetic).  means / inv_stds (length m) may be NULL. */
+int cbx_geno_attach(cbx_handle* h, const uint8_t* bed, int64_t bed_bytes, int64_t n, int64_t m,
+                    double* means, double* inv_stds);
+/* Y (m x nvec, column-major) = Z^T V (V: n x nvec), Z_ij = (x_ij - mean_j) inv_std_j
+ * for an observed call and 0 for a missing one: PlinkReader::multiply_Zt_v
+ * (src/core/plink_reader.cpp:341-392).  Sums are exact in 64-bit fixed point (one
+ * rounding of each input below 2^-62 of sum|v|); CBX_ERR_NONFINITE for NaN / Inf. */
+int cbx_geno_zt_v(cbx_handle* h, int32_t nvec, const double* V, double* Y);
+/* Y (n x nvec) = Z V (V: m x nvec), each term first rounded to float as the
+ * reference's per-SNP val_map is: PlinkReader::multiply_Z_v
+ * (src/core/plink_reader.cpp:239-293).  SNPs with inv_std = 0 are skipped. */
+int cbx_geno_z_v(cbx_handle* h, int32_t nvec, const double* V, double* Y);
+/* SNP-effect back-solve of the result writer (src/solve/result_writer.cpp:565-623,
+ * the --bfile branch): q = G^-1 u_g, effect_j = ((Z^T q)_j / inv_std_j) / total_2pq
+ * (0 when inv_std_j = 0), freq_j = mean_j / 2, total_2pq = sum of var_j >= 1e-9.
+ * G^-1 is Ginv (host, n_g x n_g) when given, else the handle's device inverse
+ * (cbx_invert_psd) or its dense Q^-1 (cbx_mme_set_qinv_dense) of order n_g;
+ * otherwise CBX_ERR_STATE ("Could not locate Ginv for back-solving").
+ * n_g must equal the attached sample count.  freq / total_2pq may be NULL. */
+int cbx_snp_effects(cbx_handle* h, const double* u_g, int64_t n_g, const double* Ginv,
+                    double* effect, double* freq, double* total_2pq);
+
 /* ---- Genomic relationship matrix -----------------------------------------
  * Replaces GrmBuilder::compute(const PlinkReader&) for algorithm 1 (VanRaden)
  * with one population, no SNP weights and no HWE filter
