@@ -323,7 +323,7 @@ def run_geno(h, bed, n, m, seed, hbm_peak, want_host, reps: int = 5) -> dict:
            "k_geno_zt_frac_hbm": zbytes / (zms * 1e-3) / 1e9 / hbm_peak,
            "k_geno_z_ms": yms / yl, "k_geno_z_GBps": ybytes / (yms * 1e-3) / 1e9,
            "elements_per_s_zt": n * m / (zms / zl * 1e-3),
-           "note": "exact 64-bit fixed-point sums; integer-issue bound (3 masked 64-bit adds per code)"}
+           "note": "exact 64-bit fixed-point sums; integer multiply-issue bound (two 32-bit multiply-adds per code)"}
     if want_host:
         # the oracle's Z^T v (numpy, all threads) on a bounded SNP sample, scaled to m
         from oracle.geno import compute_stats, multiply_zt_v

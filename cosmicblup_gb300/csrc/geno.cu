@@ -20,17 +20,31 @@
 // below that of the reference's sequential FP64 sums.
 //
 // Codes (2 bits, first sample in the low bits): 00 -> x = 2, 01 -> missing,
-// 10 -> x = 1, 11 -> x = 0.  With lo / hi the two bits, x = (1 - lo)(2 - hi) and
-// missing = lo (1 - hi), so one SNP needs three masked sums, S_lo = sum_{lo} v,
-// S_hi = sum_{hi} v and S_both = sum_{lo and hi} v:
-//   sum_obs x v = 2T - 2 S_lo - S_hi + S_both,   sum_obs v = T - S_lo + S_both,
-// with T the sum of v over all samples.  In the same way Z v adds, for SNP j, w0_j to
-// every sample, plus -w0_j where lo is set, w2_j - w0_j where hi is set and
-// w0_j - w2_j + w3_j where both are set (w_c = the float term of code c).
+// 10 -> x = 1, 11 -> x = 0.  With lo / hi the two bits and k = lo + hi, every
+// observed call has x = 2 - k (a missing call has k = 1).  So one SNP needs a single
+// dense sum S = sum_i k_i v_i plus M = the sum of v over its missing calls, taken
+// from a sparse list built once:
+//   sum_obs x v = 2T - S - M,   sum_obs v = T - M,
+// with T the sum of v over all samples.  Z v needs, per SNP j, w0_j for every
+// sample, k (w2_j - w0_j) and, where both bits are set, w3_j - 2 w2_j + w0_j (w_c =
+// the float term of code c, which is not linear in x); a missing call then receives
+// w2_j, which the sample-major missing list takes back out.  Missing calls are rare
+// in genotype data: the dense passes cost a few integer operations per code, the
+// sparse ones one gather per missing call.
+//
+// The k-weighted sums run on the integer multiply path instead of as masked adds.
+// For one 32-bit word of 16 codes, kw = (w & 0x55..) + ((w >> 1) & 0x55..) holds the
+// k_t in 2-bit fields, and with a_t = kw >> 2t (so that k_t = a_t - 4 a_{t+1}, a_16 = 0)
+//   sum_t k_t v_t = sum_t a_t (v_t - 4 v_{t-1})      (v_{-1} = 0),
+// one 32 x 64-bit multiply-add per code against u_t = v_t - 4 v_{t-1}, precomputed per
+// 16-sample word; modulo 2^64 it is two multiply-adds (the low word widening, the high
+// word 32-bit).  Z v telescopes over the accumulators instead: P_t = sum_j a_t(j) d_j
+// gives sum_j k_t(j) d_j = P_t - 4 P_{t+1}.
 //
 // Layout: the payload is copied once into rows of `pitch` bytes (a multiple of 16,
 // the padding bytes zero).  Samples at or beyond n get v = 0 (Z^T v) or are dropped
-// (Z v), so the padding codes never reach a result.
+// (Z v), so the padding codes never reach a result; the missing lists hold calls of
+// samples below n only.
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -86,14 +100,15 @@ __device__ int fix_exponent(double S) {
 }
 
 // computeStats for one SNP row per block (plink_reader.cpp:192-236).
+// Also counts the SNP's missing calls (miss_cnt) for the sparse missing lists.
 __global__ void k_geno_stats(const uint8_t* __restrict__ bed, int64_t pitch, int64_t n, int64_t m,
                              double* __restrict__ mean, double* __restrict__ inv_std,
-                             double* __restrict__ var2pq) {
+                             double* __restrict__ var2pq, int32_t* __restrict__ miss_cnt) {
   const int64_t j = blockIdx.x;
   if (j >= m) return;
   const uint32_t* row = reinterpret_cast<const uint32_t*>(bed + j * pitch);
   const int64_t nw = (n + 15) / 16;
-  int hom1 = 0, het = 0, hom2 = 0;
+  int hom1 = 0, het = 0, hom2 = 0, miss = 0;
   for (int64_t t = threadIdx.x; t < nw; t += blockDim.x) {
     const uint32_t v = row[t];
     const int64_t valid = n - 16 * t;  // >= 1
@@ -102,19 +117,24 @@ __global__ void k_geno_stats(const uint8_t* __restrict__ bed, int64_t pitch, int
     hom1 += __popc(~lo & ~hi & mask);
     het += __popc(~lo & hi & mask);
     hom2 += __popc(lo & hi & mask);
+    miss += __popc(lo & ~hi & mask);
   }
   for (int o = 16; o > 0; o >>= 1) {
     hom1 += __shfl_down_sync(0xffffffffu, hom1, o);
     het += __shfl_down_sync(0xffffffffu, het, o);
     hom2 += __shfl_down_sync(0xffffffffu, hom2, o);
+    miss += __shfl_down_sync(0xffffffffu, miss, o);
   }
-  __shared__ int red[3][32];
+  __shared__ int red[4][32];
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-  if (l == 0) { red[0][w] = hom1; red[1][w] = het; red[2][w] = hom2; }
+  if (l == 0) { red[0][w] = hom1; red[1][w] = het; red[2][w] = hom2; red[3][w] = miss; }
   __syncthreads();
   if (threadIdx.x != 0) return;
-  int a = 0, b = 0, c = 0;
-  for (int i = 0; i < (int)(blockDim.x >> 5); ++i) { a += red[0][i]; b += red[1][i]; c += red[2][i]; }
+  int a = 0, b = 0, c = 0, d = 0;
+  for (int i = 0; i < (int)(blockDim.x >> 5); ++i) {
+    a += red[0][i]; b += red[1][i]; c += red[2][i]; d += red[3][i];
+  }
+  miss_cnt[j] = d;
   const int count = a + b + c;
   double mu = 0.0, is = 0.0, v2 = 0.0;
   if (count > 0) {
@@ -142,9 +162,118 @@ __global__ void __launch_bounds__(PREP_THREADS) k_geno_total(const double* __res
   if (threadIdx.x == 0) *out = a;
 }
 
-// v (n, FP64) -> V (n_pad, int64 at scale 2^s); meta[0] = s, meta[1] = T = sum V.
+// Exclusive prefix sum of len int32 counts into ptr[0..len] (one block, fixed order).
+__global__ void __launch_bounds__(PREP_THREADS) k_geno_scan(const int32_t* __restrict__ cnt, int64_t len,
+                                                           int64_t* __restrict__ ptr) {
+  __shared__ long long part[PREP_THREADS];
+  const int t = threadIdx.x;
+  const int64_t seg = (len + PREP_THREADS - 1) / PREP_THREADS;
+  const int64_t lo = std::min<int64_t>(len, t * seg), hi = std::min<int64_t>(len, lo + seg);
+  long long sum = 0;
+  for (int64_t i = lo; i < hi; ++i) sum += cnt[i];
+  part[t] = sum;
+  __syncthreads();
+  if (t == 0) {
+    long long run = 0;
+    for (int i = 0; i < PREP_THREADS; ++i) {
+      const long long x = part[i];
+      part[i] = run;
+      run += x;
+    }
+    ptr[len] = run;
+  }
+  __syncthreads();
+  long long run = part[t];
+  for (int64_t i = lo; i < hi; ++i) {
+    ptr[i] = run;
+    run += cnt[i];
+  }
+}
+
+// SNP-major missing list: one warp per SNP writes the sample indices of its missing
+// calls (increasing) at snp_list[ptr[j]..] and counts them per sample.
+__global__ void k_geno_miss_fill(const uint8_t* __restrict__ bed, int64_t pitch, int64_t n, int64_t m,
+                                 const int64_t* __restrict__ ptr, int32_t* __restrict__ snp_list,
+                                 int32_t* __restrict__ samp_cnt) {
+  const int lane = threadIdx.x & 31;
+  const int64_t j = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (j >= m) return;
+  const uint32_t* row = reinterpret_cast<const uint32_t*>(bed + j * pitch);
+  const int64_t nw = (n + 15) / 16;
+  int64_t base = ptr[j];
+  for (int64_t w0 = 0; w0 < nw; w0 += 32) {
+    const int64_t t = w0 + lane;
+    uint32_t bits = 0;
+    if (t < nw) {
+      const uint32_t v = row[t];
+      const int64_t valid = n - 16 * t;
+      const uint32_t mask = valid >= 16 ? 0x55555555u : (0x55555555u >> (2 * (16 - valid)));
+      bits = v & ~(v >> 1) & mask;  // code 01
+    }
+    const int c = __popc(bits);
+    int incl = c;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    int64_t pos = base + incl - c;
+    while (bits) {
+      const int b = __ffs(bits) - 1;
+      const int32_t i = (int32_t)(16 * t + (b >> 1));
+      snp_list[pos++] = i;
+      atomicAdd(samp_cnt + i, 1);
+      bits &= bits - 1;
+    }
+    base += __shfl_sync(0xffffffffu, incl, 31);
+  }
+}
+
+// Sample-major copy of the missing list (the order within a sample is free: the
+// corrections it feeds are exact integer sums).
+__global__ void k_geno_miss_transpose(const int64_t* __restrict__ ptr, const int32_t* __restrict__ snp_list,
+                                      int64_t m, const int64_t* __restrict__ samp_ptr,
+                                      int32_t* __restrict__ samp_fill, int32_t* __restrict__ samp_list) {
+  const int lane = threadIdx.x & 31;
+  const int64_t j = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (j >= m) return;
+  for (int64_t k = ptr[j] + lane; k < ptr[j + 1]; k += 32) {
+    const int32_t i = snp_list[k];
+    const int pos = atomicAdd(samp_fill + i, 1);
+    samp_list[samp_ptr[i] + pos] = (int32_t)j;
+  }
+}
+
+// M_j = sum of V over SNP j's missing calls, into acc[m + j] (one warp per SNP).
+__global__ void k_geno_miss_zt(const int64_t* __restrict__ ptr, const int32_t* __restrict__ snp_list, int64_t m,
+                               const long long* __restrict__ V, unsigned long long* __restrict__ acc) {
+  const int lane = threadIdx.x & 31;
+  const int64_t j = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (j >= m) return;
+  unsigned long long s = 0;
+  for (int64_t k = ptr[j] + lane; k < ptr[j + 1]; k += 32) s += (unsigned long long)V[snp_list[k]];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if (lane == 0) acc[m + j] = s;
+}
+
+// Takes the missing calls' spurious terms back out of Z v: acc[i] -= sum of D[3j + 2]
+// over the SNPs j where sample i is missing (one warp per sample).
+__global__ void k_geno_miss_z(const int64_t* __restrict__ samp_ptr, const int32_t* __restrict__ samp_list,
+                              int64_t n, const long long* __restrict__ D, unsigned long long* __restrict__ acc) {
+  const int lane = threadIdx.x & 31;
+  const int64_t i = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (i >= n) return;
+  unsigned long long s = 0;
+  for (int64_t k = samp_ptr[i] + lane; k < samp_ptr[i + 1]; k += 32)
+    s += (unsigned long long)D[3 * (int64_t)samp_list[k] + 2];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if (lane == 0) acc[i] -= s;
+}
+
+// v (n, FP64) -> V (n_pad, int64 at scale 2^s) and U_i = V_i - 4 V_{i-1} within each
+// 16-sample word (V_{i-1} = 0 at a word's first sample); meta[0] = s, meta[1] = T = sum V.
 __global__ void __launch_bounds__(PREP_THREADS) k_geno_vprep(const double* __restrict__ v, int64_t n,
                                                             int64_t n_pad, long long* __restrict__ V,
+                                                            long long* __restrict__ U,
                                                             long long* __restrict__ meta, int* status) {
   __shared__ double red[32];
   __shared__ unsigned long long redu[32];
@@ -164,15 +293,18 @@ __global__ void __launch_bounds__(PREP_THREADS) k_geno_vprep(const double* __res
   unsigned long long t = 0;
   for (int64_t i = threadIdx.x; i < n_pad; i += blockDim.x) {
     const long long x = i < n ? __double2ll_rn(ldexp(v[i], s)) : 0ll;
+    const long long xp = (i % 16) && i - 1 < n ? __double2ll_rn(ldexp(v[i - 1], s)) : 0ll;
     V[i] = x;
+    U[i] = (long long)((unsigned long long)x - 4ull * (unsigned long long)xp);
     t += (unsigned long long)x;
   }
   t = block_sum_u64(t, redu);
   if (threadIdx.x == 0) meta[1] = (long long)t;
 }
 
-// Per-SNP float terms of multiply_Z_v (plink_reader.cpp:258-270) -> int64 deltas
-// D[3j..3j+2] = (-W0, W2 - W0, W0 - W2 + W3) at scale 2^s; meta[0] = s, meta[1] =
+// Per-SNP float terms of multiply_Z_v (plink_reader.cpp:258-270) -> int64 values
+// at scale 2^s: D[3j..3j+2] = (W2 - W0 per unit of k, W3 - 2 W2 + W0 where both bits
+// are set, W2 = the spurious term of a missing call); meta[0] = s, meta[1] =
 // C = sum_j W0_j (added to every sample).  w (3m floats) is scratch.
 __global__ void __launch_bounds__(PREP_THREADS) k_geno_zprep(const double* __restrict__ v,
                                                             const double* __restrict__ mean,
@@ -213,79 +345,63 @@ __global__ void __launch_bounds__(PREP_THREADS) k_geno_zprep(const double* __res
     const long long W0 = __double2ll_rn(ldexp((double)w[3 * j], s));
     const long long W2 = __double2ll_rn(ldexp((double)w[3 * j + 1], s));
     const long long W3 = __double2ll_rn(ldexp((double)w[3 * j + 2], s));
-    D[3 * j] = -W0;
-    D[3 * j + 1] = W2 - W0;
-    D[3 * j + 2] = W0 - W2 + W3;
+    D[3 * j] = W2 - W0;
+    D[3 * j + 1] = W3 - 2 * W2 + W0;
+    D[3 * j + 2] = W2;
     c += (unsigned long long)W0;
   }
   c = block_sum_u64(c, redu);
   if (threadIdx.x == 0) meta[1] = (long long)c;
 }
 
-// Masked sums of one 32-bit word (16 codes) against 16 fixed-point values.
-__device__ __forceinline__ void masked16(uint32_t w, const long long* __restrict__ v,
-                                         unsigned long long& s_lo, unsigned long long& s_hi,
-                                         unsigned long long& s_both) {
-  const uint32_t both = w & (w >> 1);
+// sum_t k_t V_t for one 32-bit word of 16 codes against u = U of its 16 samples
+// (the telescoped form above): lo accumulates the low words' 64-bit products, hi
+// the high words' products modulo 2^32.
+__device__ __forceinline__ void kdot16(uint32_t w, const uint2* __restrict__ u, unsigned long long& lo,
+                                       uint32_t& hi) {
+  const uint32_t kw = (w & 0x55555555u) + ((w >> 1) & 0x55555555u);
 #pragma unroll
-  for (int t = 0; t < 16; t += 2) {
-    const longlong2 x = *reinterpret_cast<const longlong2*>(v + t);
-    if ((w >> (2 * t)) & 1u) s_lo += (unsigned long long)x.x;
-    if ((w >> (2 * t + 1)) & 1u) s_hi += (unsigned long long)x.x;
-    if ((both >> (2 * t)) & 1u) s_both += (unsigned long long)x.x;
-    if ((w >> (2 * t + 2)) & 1u) s_lo += (unsigned long long)x.y;
-    if ((w >> (2 * t + 3)) & 1u) s_hi += (unsigned long long)x.y;
-    if ((both >> (2 * t + 2)) & 1u) s_both += (unsigned long long)x.y;
+  for (int t = 0; t < 16; ++t) {
+    const uint32_t at = kw >> (2 * t);
+    const uint2 x = u[t];
+    lo += (unsigned long long)at * x.x;
+    hi += at * x.y;
   }
 }
 
-// Z^T v: one SNP row per thread over a chunk of ZT_CHUNK samples.  The chunk's
-// fixed-point v sits in shared memory and is read as broadcasts; each thread
-// streams its own row 32 bytes (128 samples) at a time.  acc = (S_lo, S_hi,
-// S_both) per row, 3m words, added with 64-bit atomics.
+// Z^T v: one SNP row per thread over a chunk of ZT_CHUNK samples.  The chunk's U
+// sits in shared memory and is read as broadcasts; each thread streams its own row
+// 16 bytes (64 samples) at a time.  acc[row] += S (64-bit atomics).
 __global__ void __launch_bounds__(ZT_THREADS) k_geno_zt(const uint8_t* __restrict__ bed, int64_t pitch,
-                                                       int64_t m, const long long* __restrict__ V,
+                                                       int64_t m, const long long* __restrict__ U,
                                                        unsigned long long* __restrict__ acc) {
-  __shared__ __align__(16) long long sv[ZT_CHUNK];
+  __shared__ __align__(16) long long su[ZT_CHUNK];
   const int64_t c0 = (int64_t)blockIdx.y * ZT_CHUNK;
   const int len = (int)std::min<int64_t>(ZT_CHUNK, 4 * pitch - c0);  // multiple of 64
-  for (int i = threadIdx.x; i < len; i += ZT_THREADS) sv[i] = V[c0 + i];
+  for (int i = threadIdx.x; i < len; i += ZT_THREADS) su[i] = U[c0 + i];
   __syncthreads();
   const int64_t row = (int64_t)blockIdx.x * ZT_THREADS + threadIdx.x;
   if (row >= m) return;
   const uint4* p = reinterpret_cast<const uint4*>(bed + row * pitch + c0 / 4);
-  unsigned long long s_lo = 0, s_hi = 0, s_both = 0;
+  const uint2* u = reinterpret_cast<const uint2*>(su);
+  unsigned long long lo = 0;
+  uint32_t hi = 0;
   const int nv = len / 64;  // 16-byte words of this row in the chunk
-  int k = 0;
-  for (; k + 1 < nv; k += 2) {
+  for (int k = 0; k < nv; ++k) {
     const uint4 a = __ldg(p + k);
-    const uint4 b = __ldg(p + k + 1);
-    const long long* v = sv + 64 * k;
-    masked16(a.x, v, s_lo, s_hi, s_both);
-    masked16(a.y, v + 16, s_lo, s_hi, s_both);
-    masked16(a.z, v + 32, s_lo, s_hi, s_both);
-    masked16(a.w, v + 48, s_lo, s_hi, s_both);
-    masked16(b.x, v + 64, s_lo, s_hi, s_both);
-    masked16(b.y, v + 80, s_lo, s_hi, s_both);
-    masked16(b.z, v + 96, s_lo, s_hi, s_both);
-    masked16(b.w, v + 112, s_lo, s_hi, s_both);
+    kdot16(a.x, u + 64 * k, lo, hi);
+    kdot16(a.y, u + 64 * k + 16, lo, hi);
+    kdot16(a.z, u + 64 * k + 32, lo, hi);
+    kdot16(a.w, u + 64 * k + 48, lo, hi);
   }
-  if (k < nv) {
-    const uint4 a = __ldg(p + k);
-    const long long* v = sv + 64 * k;
-    masked16(a.x, v, s_lo, s_hi, s_both);
-    masked16(a.y, v + 16, s_lo, s_hi, s_both);
-    masked16(a.z, v + 32, s_lo, s_hi, s_both);
-    masked16(a.w, v + 48, s_lo, s_hi, s_both);
-  }
-  atomicAdd(acc + row, s_lo);
-  atomicAdd(acc + m + row, s_hi);
-  atomicAdd(acc + 2 * m + row, s_both);
+  atomicAdd(acc + row, lo + ((unsigned long long)hi << 32));
 }
 
 // Z v: 16 samples per thread (one 32-bit word per row, 128 coalesced bytes per
-// warp), looping over a chunk of SNP rows whose deltas sit in shared memory.
-// acc: one word per sample (n_pad), added with 64-bit atomics.
+// warp), looping over a chunk of SNP rows whose values sit in shared memory.
+// Per sample t: P_t = sum_j (kw_j >> 2t) D[3j] (telescoped, split into a 64-bit low
+// and a 32-bit high accumulator) and Q_t = sum of D[3j+1] where both bits are set;
+// acc[t] += P_t - 4 P_{t+1} + Q_t (64-bit atomics, one word per sample of n_pad).
 __global__ void __launch_bounds__(Z_THREADS) k_geno_z(const uint8_t* __restrict__ bed, int64_t pitch,
                                                      int64_t m, int rows_per_cta,
                                                      const long long* __restrict__ D,
@@ -298,26 +414,33 @@ __global__ void __launch_bounds__(Z_THREADS) k_geno_z(const uint8_t* __restrict_
   const int64_t byte_off = ((int64_t)blockIdx.x * Z_THREADS + threadIdx.x) * 4;
   if (byte_off >= pitch) return;
   const uint8_t* p = bed + r0 * pitch + byte_off;
-  unsigned long long a[16];
+  unsigned long long P[16], Q[16];
+  uint32_t H[16];
 #pragma unroll
-  for (int t = 0; t < 16; ++t) a[t] = 0;
+  for (int t = 0; t < 16; ++t) { P[t] = 0; Q[t] = 0; H[t] = 0; }
 #pragma unroll 2
   for (int r = 0; r < nr; ++r) {
     const uint32_t w = __ldg(reinterpret_cast<const uint32_t*>(p + (int64_t)r * pitch));
-    const unsigned long long d_lo = (unsigned long long)sd[3 * r];
-    const unsigned long long d_hi = (unsigned long long)sd[3 * r + 1];
-    const unsigned long long d_both = (unsigned long long)sd[3 * r + 2];
+    const unsigned long long d1 = (unsigned long long)sd[3 * r];
+    const unsigned long long d2 = (unsigned long long)sd[3 * r + 1];
+    const uint32_t d1l = (uint32_t)d1, d1h = (uint32_t)(d1 >> 32);
+    const uint32_t kw = (w & 0x55555555u) + ((w >> 1) & 0x55555555u);
     const uint32_t both = w & (w >> 1);
 #pragma unroll
     for (int t = 0; t < 16; ++t) {
-      if ((w >> (2 * t)) & 1u) a[t] += d_lo;
-      if ((w >> (2 * t + 1)) & 1u) a[t] += d_hi;
-      if ((both >> (2 * t)) & 1u) a[t] += d_both;
+      const uint32_t at = kw >> (2 * t);
+      P[t] += (unsigned long long)at * d1l;
+      H[t] += at * d1h;
+      if (both & (1u << (2 * t))) Q[t] += d2;
     }
   }
   const int64_t i0 = byte_off * 4;
 #pragma unroll
-  for (int t = 0; t < 16; ++t) atomicAdd(acc + i0 + t, a[t]);
+  for (int t = 0; t < 16; ++t) {
+    const unsigned long long pt = P[t] + ((unsigned long long)H[t] << 32);
+    const unsigned long long pn = t < 15 ? P[t + 1] + ((unsigned long long)H[t + 1] << 32) : 0ull;
+    atomicAdd(acc + i0 + t, pt - 4ull * pn + Q[t]);
+  }
 }
 
 // multiply_Zt_v's last step (plink_reader.cpp:387) and, when effect != null, the
@@ -330,9 +453,9 @@ __global__ void k_geno_zt_fin(const unsigned long long* __restrict__ acc, const 
   const unsigned long long T = (unsigned long long)meta[1];
   for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < m;
        j += (int64_t)gridDim.x * blockDim.x) {
-    const unsigned long long slo = acc[j], shi = acc[m + j], sboth = acc[2 * m + j];
-    const long long A = (long long)(2ull * T - 2ull * slo - shi + sboth);
-    const long long B = (long long)(T - slo + sboth);
+    const unsigned long long S = acc[j], miss = acc[m + j];
+    const long long A = (long long)(2ull * T - S - miss);
+    const long long B = (long long)(T - miss);
     const double is = inv_std[j];
     double r = 0.0;
     if (is != 0.0) {
@@ -362,11 +485,16 @@ struct State {
   DevBuf<uint8_t> bed;      // m x pitch
   int64_t n = 0, m = 0, pitch = 0;
   DevBuf<double> stats;     // mean (m), inv_std (m), var2pq (m), total_2pq (1)
-  DevBuf<long long> fixv;   // fixed-point v (n_pad) or deltas (3m)
+  DevBuf<long long> fixv;   // fixed-point V and U (2 n_pad) or per-SNP values (3m)
   DevBuf<float> wterm;      // float terms of Z v (3m)
   DevBuf<long long> meta;   // s, T or C
   DevBuf<unsigned long long> acc;
   DevBuf<double> vin, vout, q;
+  // missing calls: SNP-major (miss_ptr m + 1, miss_snp) and sample-major (samp_ptr
+  // n + 1, miss_samp) lists of the other index
+  int64_t nmiss = 0;
+  DevBuf<int64_t> miss_ptr, samp_ptr;
+  DevBuf<int32_t> miss_snp, miss_samp;
   double* mean() const { return stats.p; }
   double* inv_std() const { return stats.p + m; }
   double* var2pq() const { return stats.p + 2 * m; }
@@ -401,19 +529,25 @@ void timed(cbx_handle* h, int bucket, double bytes, F&& launch) {
 void zt_device(cbx_handle* h, State& g, const double* v, double* y, double* effect, double* freq) {
   cudaStream_t s = h->stream;
   const int64_t n_pad = g.n_pad();
-  g.fixv.resize(std::max<int64_t>(n_pad, 3 * g.m));
+  g.fixv.resize(std::max<int64_t>(2 * n_pad, 3 * g.m));
   g.meta.resize(2);
-  g.acc.resize(3 * g.m);
-  g.acc.zero(s);
-  k_geno_vprep<<<1, PREP_THREADS, 0, s>>>(v, g.n, n_pad, g.fixv.p, g.meta.p, h->status.p);
+  g.acc.resize(std::max<int64_t>(2 * g.m, n_pad));
+  CBX_CUDA(cudaMemsetAsync(g.acc.p, 0, 2 * g.m * sizeof(unsigned long long), s));
+  long long* V = g.fixv.p;
+  long long* U = g.fixv.p + n_pad;
+  k_geno_vprep<<<1, PREP_THREADS, 0, s>>>(v, g.n, n_pad, V, U, g.meta.p, h->status.p);
   h->launched("k_geno_vprep");
   const dim3 grid((unsigned)((g.m + ZT_THREADS - 1) / ZT_THREADS), (unsigned)((n_pad + ZT_CHUNK - 1) / ZT_CHUNK));
   // algorithmic bytes: the payload once, v once per SNP block of the grid, one row result
   const double bytes = (double)g.m * (double)((g.n + 3) / 4) + 8.0 * (double)g.n + 8.0 * (double)g.m;
   timed(h, 3, bytes, [&] {
-    k_geno_zt<<<grid, ZT_THREADS, 0, s>>>(g.bed.p, g.pitch, g.m, g.fixv.p, g.acc.p);
+    k_geno_zt<<<grid, ZT_THREADS, 0, s>>>(g.bed.p, g.pitch, g.m, U, g.acc.p);
     h->launched("k_geno_zt");
   });
+  if (g.nmiss > 0) {
+    k_geno_miss_zt<<<(unsigned)((g.m + 7) / 8), 256, 0, s>>>(g.miss_ptr.p, g.miss_snp.p, g.m, V, g.acc.p);
+    h->launched("k_geno_miss_zt");
+  }
   k_geno_zt_fin<<<gridn(g.m, 256, 4 * h->num_sms), 256, 0, s>>>(g.acc.p, g.meta.p, g.mean(), g.inv_std(), g.m,
                                                                 g.total(), y, effect, freq);
   h->launched("k_geno_zt_fin");
@@ -423,11 +557,11 @@ void zt_device(cbx_handle* h, State& g, const double* v, double* y, double* effe
 void z_device(cbx_handle* h, State& g, const double* v, double* y) {
   cudaStream_t s = h->stream;
   const int64_t n_pad = g.n_pad();
-  g.fixv.resize(std::max<int64_t>(n_pad, 3 * g.m));
+  g.fixv.resize(std::max<int64_t>(2 * n_pad, 3 * g.m));
   g.wterm.resize(3 * g.m);
   g.meta.resize(2);
-  g.acc.resize(n_pad);
-  g.acc.zero(s);
+  g.acc.resize(std::max<int64_t>(2 * g.m, n_pad));
+  CBX_CUDA(cudaMemsetAsync(g.acc.p, 0, n_pad * sizeof(unsigned long long), s));
   k_geno_zprep<<<1, PREP_THREADS, 0, s>>>(v, g.mean(), g.inv_std(), g.m, g.wterm.p, g.fixv.p, g.meta.p,
                                           h->status.p);
   h->launched("k_geno_zprep");
@@ -444,6 +578,10 @@ void z_device(cbx_handle* h, State& g, const double* v, double* y) {
                                                                       g.fixv.p, g.acc.p);
     h->launched("k_geno_z");
   });
+  if (g.nmiss > 0) {
+    k_geno_miss_z<<<(unsigned)((g.n + 7) / 8), 256, 0, s>>>(g.samp_ptr.p, g.miss_samp.p, g.n, g.fixv.p, g.acc.p);
+    h->launched("k_geno_miss_z");
+  }
   k_geno_z_fin<<<gridn(g.n, 256, 4 * h->num_sms), 256, 0, s>>>(g.acc.p, g.meta.p, g.n, y);
   h->launched("k_geno_z_fin");
 }
@@ -476,11 +614,34 @@ extern "C" int cbx_geno_attach(cbx_handle* h, const uint8_t* bed, int64_t bed_by
     g->bed.zero(s);
     CBX_CUDA(cudaMemcpy2DAsync(g->bed.p, g->pitch, bed + 3, bps, bps, m, cudaMemcpyHostToDevice, s));
     g->stats.resize(3 * m + 1);
+    DevBuf<int32_t> cnt;
+    cnt.resize(std::max(m, n));
     geno::k_geno_stats<<<(unsigned)m, 128, 0, s>>>(g->bed.p, g->pitch, n, m, g->mean(), g->inv_std(),
-                                                    g->var2pq());
+                                                    g->var2pq(), cnt.p);
     h->launched("k_geno_stats");
     geno::k_geno_total<<<1, geno::PREP_THREADS, 0, s>>>(g->var2pq(), m, g->total());
     h->launched("k_geno_total");
+    // sparse missing lists
+    g->miss_ptr.resize(m + 1);
+    geno::k_geno_scan<<<1, geno::PREP_THREADS, 0, s>>>(cnt.p, m, g->miss_ptr.p);
+    h->launched("k_geno_scan");
+    CBX_CUDA(cudaMemcpyAsync(&g->nmiss, g->miss_ptr.p + m, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    CBX_CUDA(cudaStreamSynchronize(s));
+    if (g->nmiss > 0) {
+      g->miss_snp.resize(g->nmiss);
+      g->miss_samp.resize(g->nmiss);
+      g->samp_ptr.resize(n + 1);
+      CBX_CUDA(cudaMemsetAsync(cnt.p, 0, n * sizeof(int32_t), s));
+      geno::k_geno_miss_fill<<<(unsigned)((m + 7) / 8), 256, 0, s>>>(g->bed.p, g->pitch, n, m, g->miss_ptr.p,
+                                                                     g->miss_snp.p, cnt.p);
+      h->launched("k_geno_miss_fill");
+      geno::k_geno_scan<<<1, geno::PREP_THREADS, 0, s>>>(cnt.p, n, g->samp_ptr.p);
+      h->launched("k_geno_scan");
+      CBX_CUDA(cudaMemsetAsync(cnt.p, 0, n * sizeof(int32_t), s));
+      geno::k_geno_miss_transpose<<<(unsigned)((m + 7) / 8), 256, 0, s>>>(g->miss_ptr.p, g->miss_snp.p, m,
+                                                                          g->samp_ptr.p, cnt.p, g->miss_samp.p);
+      h->launched("k_geno_miss_transpose");
+    }
     if (means) CBX_CUDA(cudaMemcpyAsync(means, g->mean(), m * sizeof(double), cudaMemcpyDeviceToHost, s));
     if (inv_stds)
       CBX_CUDA(cudaMemcpyAsync(inv_stds, g->inv_std(), m * sizeof(double), cudaMemcpyDeviceToHost, s));
