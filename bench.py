@@ -341,7 +341,7 @@ def run_geno(h, bed, n, m, seed, hbm_peak, want_host, reps: int = 5) -> dict:
 def run_gpu(args, cfg):
     import ctypes as C
     from cosmicblup_gb300 import AIREML, DeviceMME, Handle, RemlConfig, invert_psd
-    from cosmicblup_gb300._lib import lib, ptr
+    from cosmicblup_gb300._lib import lib, ptr, tune_report
     from cosmicblup_gb300.mme import FP64, MIXED
     from cosmicblup_gb300.synth import simulate_bed
     from cosmicblup_gb300.vce import MODE_EM
@@ -536,6 +536,7 @@ def run_gpu(args, cfg):
                      "peak_source": peak_src, "launches": dl, "avg_launch_ms": dms / dl if dl else None},
         "cpu_baseline": cpu,
         "variances": {"var_u": r.var_u, "var_e": r.var_e},
+        "autotune": tune_report(),
     }
     print(json.dumps(line))
 

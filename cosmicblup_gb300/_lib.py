@@ -82,6 +82,9 @@ SIGNATURES = [
                              C.POINTER(C.c_int32)]),
     ("cbx_mt_solve", C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
                                C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("cbx_tune_enable", C.c_int, [C.c_int32]),
+    ("cbx_tune_reset", C.c_int, []),
+    ("cbx_tune_report", C.c_int, [C.c_char_p, C.c_int64]),
     ("cbx_dense_apply_noalloc", C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
     ("cbx_batch_reml", C.c_int, [C.c_int, C.c_int32, C.c_void_p, C.c_float, C.c_void_p, C.c_int32, C.c_void_p]),
     # diagnostics and self-test exports (not in the public header)
@@ -199,3 +202,19 @@ class Handle:
             self.close()
         except Exception:
             pass
+
+
+def tune_enable(on: bool) -> None:
+    """Switch the launch-shape autotuner on or off for the whole process."""
+    lib().cbx_tune_enable(1 if on else 0)
+
+
+def tune_reset() -> None:
+    lib().cbx_tune_reset()
+
+
+def tune_report() -> list[str]:
+    """One line per autotuner decision (kernel, device, size classes, width, choice, ms)."""
+    buf = C.create_string_buffer(1 << 16)
+    lib().cbx_tune_report(buf, len(buf))
+    return [ln for ln in buf.value.decode().splitlines() if ln]

@@ -4,6 +4,7 @@
 #include <cstring>
 #include <map>
 #include "handle.h"
+#include "tune.h"
 
 void cbx_handle::check_status(const char* what) {
   int st = 0;
@@ -165,6 +166,25 @@ int cbx_trace_read(cbx_handle* h, char* buf, int64_t cap) {
     h->trace.clear();
     if (h->trace_on) CBX_CUDA(cudaEventRecord(h->trace_start, h->stream));
   });
+}
+
+int cbx_tune_enable(int32_t on) {
+  cbx::tune::enabled_flag().store(on ? 1 : 0);
+  return CBX_OK;
+}
+
+int cbx_tune_reset(void) {
+  cbx::tune::reset();
+  return CBX_OK;
+}
+
+int cbx_tune_report(char* buf, int64_t cap) {
+  if (!buf || cap <= 0) return CBX_ERR_ARG;
+  const std::string out = cbx::tune::report();
+  const size_t n = std::min<size_t>(out.size(), (size_t)cap - 1);
+  memcpy(buf, out.data(), n);
+  buf[n] = 0;
+  return CBX_OK;
 }
 
 }  // extern "C"

@@ -52,12 +52,12 @@
 #include "dense.h"
 #include "handle.h"
 #include "pcg.h"
+#include "tune.h"
 
 namespace cbx {
 namespace geno {
 
 constexpr int ZT_THREADS = 256;   // one SNP row per thread
-constexpr int ZT_CHUNK = 4096;    // samples per CTA (32 KB of fixed-point v in shared memory)
 constexpr int Z_THREADS = 256;    // 16 samples (one 32-bit word) per thread
 constexpr int Z_MAX_ROWS = 2048;  // SNP rows per CTA (48 KB of deltas in shared memory)
 constexpr int PREP_THREADS = 1024;
@@ -369,15 +369,17 @@ __device__ __forceinline__ void kdot16(uint32_t w, const uint2* __restrict__ u, 
   }
 }
 
-// Z^T v: one SNP row per thread over a chunk of ZT_CHUNK samples.  The chunk's U
-// sits in shared memory and is read as broadcasts; each thread streams its own row
-// 16 bytes (64 samples) at a time.  acc[row] += S (64-bit atomics).
+// Z^T v: one SNP row per thread over a chunk of CHUNK samples (2,048 to 8,192, a
+// tuned launch shape).  The chunk's U sits in shared memory and is read as
+// broadcasts; each thread streams its own row 16 bytes (64 samples) at a time.
+// acc[row] += S (64-bit atomics).
+template <int CHUNK>
 __global__ void __launch_bounds__(ZT_THREADS) k_geno_zt(const uint8_t* __restrict__ bed, int64_t pitch,
                                                        int64_t m, const long long* __restrict__ U,
                                                        unsigned long long* __restrict__ acc) {
-  __shared__ __align__(16) long long su[ZT_CHUNK];
-  const int64_t c0 = (int64_t)blockIdx.y * ZT_CHUNK;
-  const int len = (int)std::min<int64_t>(ZT_CHUNK, 4 * pitch - c0);  // multiple of 64
+  __shared__ __align__(16) long long su[CHUNK];
+  const int64_t c0 = (int64_t)blockIdx.y * CHUNK;
+  const int len = (int)std::min<int64_t>(CHUNK, 4 * pitch - c0);  // multiple of 64
   for (int i = threadIdx.x; i < len; i += ZT_THREADS) su[i] = U[c0 + i];
   __syncthreads();
   const int64_t row = (int64_t)blockIdx.x * ZT_THREADS + threadIdx.x;
@@ -532,18 +534,27 @@ void zt_device(cbx_handle* h, State& g, const double* v, double* y, double* effe
   g.fixv.resize(std::max<int64_t>(2 * n_pad, 3 * g.m));
   g.meta.resize(2);
   g.acc.resize(std::max<int64_t>(2 * g.m, n_pad));
-  CBX_CUDA(cudaMemsetAsync(g.acc.p, 0, 2 * g.m * sizeof(unsigned long long), s));
+  CBX_CUDA(cudaMemsetAsync(g.acc.p + g.m, 0, g.m * sizeof(unsigned long long), s));
   long long* V = g.fixv.p;
   long long* U = g.fixv.p + n_pad;
   k_geno_vprep<<<1, PREP_THREADS, 0, s>>>(v, g.n, n_pad, V, U, g.meta.p, h->status.p);
   h->launched("k_geno_vprep");
-  const dim3 grid((unsigned)((g.m + ZT_THREADS - 1) / ZT_THREADS), (unsigned)((n_pad + ZT_CHUNK - 1) / ZT_CHUNK));
   // algorithmic bytes: the payload once, v once per SNP block of the grid, one row result
   const double bytes = (double)g.m * (double)((g.n + 3) / 4) + 8.0 * (double)g.n + 8.0 * (double)g.m;
-  timed(h, 3, bytes, [&] {
-    k_geno_zt<<<grid, ZT_THREADS, 0, s>>>(g.bed.p, g.pitch, g.m, U, g.acc.p);
+  const unsigned gx = (unsigned)((g.m + ZT_THREADS - 1) / ZT_THREADS);
+  // samples per CTA: 4,096 (default), 2,048 or 8,192; exact integer sums, so every
+  // shape gives the same bits (the accumulator is zeroed before each run)
+  auto zt = [&](int c) {
+    CBX_CUDA(cudaMemsetAsync(g.acc.p, 0, g.m * sizeof(unsigned long long), s));
+    const int chunk = c == 1 ? 2048 : (c == 2 ? 8192 : 4096);
+    const dim3 grid(gx, (unsigned)((n_pad + chunk - 1) / chunk));
+    if (c == 1) k_geno_zt<2048><<<grid, ZT_THREADS, 0, s>>>(g.bed.p, g.pitch, g.m, U, g.acc.p);
+    else if (c == 2) k_geno_zt<8192><<<grid, ZT_THREADS, 0, s>>>(g.bed.p, g.pitch, g.m, U, g.acc.p);
+    else k_geno_zt<4096><<<grid, ZT_THREADS, 0, s>>>(g.bed.p, g.pitch, g.m, U, g.acc.p);
     h->launched("k_geno_zt");
-  });
+  };
+  const int choice = tune::choose(h, tune::GENO_ZT, tune::size_class(g.n), tune::size_class(g.m), 1, 3, zt);
+  timed(h, 3, bytes, [&] { zt(choice); });
   if (g.nmiss > 0) {
     k_geno_miss_zt<<<(unsigned)((g.m + 7) / 8), 256, 0, s>>>(g.miss_ptr.p, g.miss_snp.p, g.m, V, g.acc.p);
     h->launched("k_geno_miss_zt");
@@ -561,23 +572,28 @@ void z_device(cbx_handle* h, State& g, const double* v, double* y) {
   g.wterm.resize(3 * g.m);
   g.meta.resize(2);
   g.acc.resize(std::max<int64_t>(2 * g.m, n_pad));
-  CBX_CUDA(cudaMemsetAsync(g.acc.p, 0, n_pad * sizeof(unsigned long long), s));
   k_geno_zprep<<<1, PREP_THREADS, 0, s>>>(v, g.mean(), g.inv_std(), g.m, g.wterm.p, g.fixv.p, g.meta.p,
                                           h->status.p);
   h->launched("k_geno_zprep");
   const int gx = (int)((g.pitch + 4 * Z_THREADS - 1) / (4 * Z_THREADS));
-  // about four CTAs per SM, at most Z_MAX_ROWS rows each
-  int64_t gy = std::max<int64_t>(1, (4 * (int64_t)h->num_sms + gx - 1) / gx);
-  int64_t rows = (g.m + gy - 1) / gy;
-  rows = std::min<int64_t>(rows, Z_MAX_ROWS);
-  gy = (g.m + rows - 1) / rows;
-  const int smem = (int)(3 * rows * sizeof(long long));
   const double bytes = (double)g.m * (double)((g.n + 3) / 4) + 8.0 * (double)g.m + 8.0 * (double)g.n;
-  timed(h, 4, bytes, [&] {
-    k_geno_z<<<dim3((unsigned)gx, (unsigned)gy), Z_THREADS, smem, s>>>(g.bed.p, g.pitch, g.m, (int)rows,
-                                                                      g.fixv.p, g.acc.p);
+  // about 4 (default), 2 or 8 CTAs per SM, at most Z_MAX_ROWS SNP rows each; exact
+  // integer sums, so every shape gives the same bits (the accumulator is zeroed
+  // before each run)
+  auto zk = [&](int c) {
+    CBX_CUDA(cudaMemsetAsync(g.acc.p, 0, n_pad * sizeof(unsigned long long), s));
+    const int per_sm = c == 1 ? 2 : (c == 2 ? 8 : 4);
+    int64_t gy = std::max<int64_t>(1, (per_sm * (int64_t)h->num_sms + gx - 1) / gx);
+    int64_t rows = std::min<int64_t>((g.m + gy - 1) / gy, Z_MAX_ROWS);
+    gy = (g.m + rows - 1) / rows;
+    CBX_REQUIRE(gy <= 65535, CBX_ERR_ARG, "too many SNPs for the Z v grid");
+    const int smem = (int)(3 * rows * sizeof(long long));
+    k_geno_z<<<dim3((unsigned)gx, (unsigned)gy), Z_THREADS, smem, s>>>(g.bed.p, g.pitch, g.m, (int)rows, g.fixv.p,
+                                                                      g.acc.p);
     h->launched("k_geno_z");
-  });
+  };
+  const int choice = tune::choose(h, tune::GENO_Z, tune::size_class(g.n), tune::size_class(g.m), 1, 3, zk);
+  timed(h, 4, bytes, [&] { zk(choice); });
   if (g.nmiss > 0) {
     k_geno_miss_z<<<(unsigned)((g.n + 7) / 8), 256, 0, s>>>(g.samp_ptr.p, g.miss_samp.p, g.n, g.fixv.p, g.acc.p);
     h->launched("k_geno_miss_z");

@@ -15,6 +15,7 @@
 #include <vector>
 #include "handle.h"
 #include "pcg.h"
+#include "tune.h"
 #include "solver.cuh"
 #include "pcg_fused.cuh"
 #include "dense_tc.h"
@@ -368,9 +369,9 @@ __global__ void k_gather_cols(const double* __restrict__ X, int xs, int ncols, d
 }
 
 // Float-float block products are FP32-issue-bound, so they run on the
-// populated columns only, in power-of-two pieces of at most 16 columns written
-// into the S-wide output.
-template <int W>
+// populated columns only, in power-of-two pieces written into the S-wide output;
+// R rows per warp.
+template <int W, int R = rpw_ff<W>()>
 static void ff_piece(cbx_handle* h, const sv::OpView<double>& op, const double* X, int xs, double* Vt,
                      double* Tout, const int* active) {
   cudaStream_t s = h->stream;
@@ -380,12 +381,41 @@ static void ff_piece(cbx_handle* h, const sv::OpView<double>& op, const double* 
   sv::k_gather_hl<W><<<grid_for(W * op.ld, 256, 4 * h->num_sms), 256, 0, s>>>(X, vhl, op.p, op.ng, op.ld, op.gmap,
                                                                             xs);
   h->launched("k_gather_hl<f64>");
-  constexpr int R = rpw_ff<W>();
   const int smem = W * 256 * (int)sizeof(float2);
   ensure_smem((const void*)sv::k_dense_ff<W, R>, smem, h->device);
   sv::k_dense_ff<W, R><<<(unsigned)((op.ng + 8 * R - 1) / (8 * R)), 256, smem, s>>>(mm.Qd32.p, mm.Qlo32.p, op.ng,
                                                                                    op.ld, vhl, Tout, active, xs);
   h->launched("k_dense_ff<f64>");
+}
+
+// The float-float product of ncols populated columns under one launch-shape plan
+// (the autotuner's candidates; every plan gives the same bits, since each output's
+// accumulation order depends only on the K tiling):
+//   0: pieces of at most 16 columns, rows per warp by width (16 -> 2)
+//   1: pieces of at most 16 columns, one row per warp at width 16
+//   2: pieces of at most 8 columns (4 rows per warp)
+//   3: pieces of at most 32 columns, one row per warp at width 32
+constexpr int FF_PLANS = 4;
+static void ff_plan(cbx_handle* h, const sv::OpView<double>& op, const double* X, int S, int ncols, double* Vt,
+                    double* Tout, const int* active, int plan) {
+  const int cap = plan == 2 ? 8 : (plan == 3 ? 32 : 16);
+  for (int c0 = 0; c0 < ncols;) {
+    const int left = std::min(ncols - c0, cap);
+    int w = 1;
+    while (2 * w <= left) w <<= 1;
+    switch (w) {
+      case 1: ff_piece<1>(h, op, X + c0, S, Vt, Tout + c0, active); break;
+      case 2: ff_piece<2>(h, op, X + c0, S, Vt, Tout + c0, active); break;
+      case 4: ff_piece<4>(h, op, X + c0, S, Vt, Tout + c0, active); break;
+      case 8: ff_piece<8>(h, op, X + c0, S, Vt, Tout + c0, active); break;
+      case 16:
+        if (plan == 1) ff_piece<16, 1>(h, op, X + c0, S, Vt, Tout + c0, active);
+        else ff_piece<16>(h, op, X + c0, S, Vt, Tout + c0, active);
+        break;
+      default: ff_piece<32, 1>(h, op, X + c0, S, Vt, Tout + c0, active); break;
+    }
+    c0 += w;
+  }
 }
 
 // Tout[:, 0:ncols] (rows S apart) of the dense block product in FP64
@@ -398,22 +428,13 @@ static void dense64(cbx_handle* h, const sv::OpView<double>& op, const double* X
     // the compensated FP64 column sums that restore the block's shift
     sv::k_colsum_x<<<ncols, 256, 0, h->stream>>>(X, S, op.p, op.ng, op.gmap, colsum);
     h->launched("k_colsum_x<f64>");
-    // pieces of at most 16 columns (two 16-column passes beat one 32-column
-    // pass: register pressure, not the second read of the block, limits it)
-    for (int c0 = 0; c0 < ncols;) {
-      const int left = std::min(ncols - c0, 16);
-      int w = 1;
-      while (2 * w <= left) w <<= 1;
-      switch (w) {
-        case 1: ff_piece<1>(h, op, X + c0, S, Vt, Tout + c0, active); break;
-        case 2: ff_piece<2>(h, op, X + c0, S, Vt, Tout + c0, active); break;
-        case 4: ff_piece<4>(h, op, X + c0, S, Vt, Tout + c0, active); break;
-        case 8: ff_piece<8>(h, op, X + c0, S, Vt, Tout + c0, active); break;
-        case 16: ff_piece<16>(h, op, X + c0, S, Vt, Tout + c0, active); break;
-        default: ff_piece<32>(h, op, X + c0, S, Vt, Tout + c0, active); break;
-      }
-      c0 += w;
-    }
+    // the launch shape is tuned per block order and column count (two 16-column
+    // passes with 2 rows per warp measured best at n = 20,000: register pressure,
+    // not the second read of the block, limits the wider pieces)
+    const int plan = tune::choose(h, tune::FF, tune::size_class(op.ng), 0, ncols, FF_PLANS, [&](int c) {
+      ff_plan(h, op, X, S, ncols, Vt, Tout, active, c);
+    });
+    ff_plan(h, op, X, S, ncols, Vt, Tout, active, plan);
     return;
   }
   cudaStream_t s = h->stream;
@@ -453,8 +474,22 @@ int product_from_vt(cbx_handle* h, const sv::OpView<T>& op, Workspace<T, S>& w, 
     dense_tc(h, reinterpret_cast<const float*>(op.Qd), op.ng, op.ld, reinterpret_cast<const float*>(w.Vt.p), S,
              tsplit, reinterpret_cast<float*>(w.Tout.p), active, ncols);
   } else if (S == 1) {
-    sv::k_gemv<T, 4, 4><<<(unsigned)((op.ng + 31) / 32), 256, 0, s>>>(op.Qd, op.ng, op.ld, w.Vt.p, w.Tout.p, active);
-    h->launched("k_gemv<f32>");
+    // rows per warp x loads in flight per lane, tuned per block order (all shapes
+    // accumulate each row in the same order)
+    auto gemv = [&](int c) {
+      switch (c) {
+        case 1: sv::k_gemv<T, 2, 4><<<(unsigned)((op.ng + 15) / 16), 256, 0, s>>>(op.Qd, op.ng, op.ld, w.Vt.p,
+                                                                               w.Tout.p, active); break;
+        case 2: sv::k_gemv<T, 8, 2><<<(unsigned)((op.ng + 63) / 64), 256, 0, s>>>(op.Qd, op.ng, op.ld, w.Vt.p,
+                                                                               w.Tout.p, active); break;
+        case 3: sv::k_gemv<T, 2, 8><<<(unsigned)((op.ng + 15) / 16), 256, 0, s>>>(op.Qd, op.ng, op.ld, w.Vt.p,
+                                                                               w.Tout.p, active); break;
+        default: sv::k_gemv<T, 4, 4><<<(unsigned)((op.ng + 31) / 32), 256, 0, s>>>(op.Qd, op.ng, op.ld, w.Vt.p,
+                                                                                w.Tout.p, active); break;
+      }
+      h->launched("k_gemv<f32>");
+    };
+    gemv(tune::choose(h, tune::GEMV, tune::size_class(op.ng), (int)sizeof(T), 1, 4, gemv));
   } else {
     constexpr int R = rpw<T, S>();
     constexpr int KT = 32 * sv::Vec16<T>::n * 4;

@@ -170,6 +170,20 @@ int cbx_profile_read(cbx_handle* h, int32_t bucket, int64_t* launches, double* t
 int cbx_timer_start(cbx_handle* h);
 int cbx_timer_stop(cbx_handle* h, double* ms);
 
+/* ---- Launch-shape autotuner (no reference counterpart) ---------------------
+ * Kernels with several launch shapes that give bit-identical results (the
+ * float-float block product's piece width and rows per warp, the single-RHS GEMV's
+ * rows per warp and loads in flight, the genotype products' chunking) time each
+ * shape once per (kernel, device, size class, width) on the live operands and keep
+ * the fastest (a shape must beat the default by 3 %).  Tuning never changes a
+ * result.  It is on unless the environment sets CBX_TUNE=0; cbx_tune_enable
+ * switches it process-wide, cbx_tune_reset forgets every decision, and
+ * cbx_tune_report writes one line per decision (kernel, device, size classes,
+ * width, chosen shape, measured ms per shape) into buf (cap bytes, NUL-ended). */
+int cbx_tune_enable(int32_t on);
+int cbx_tune_reset(void);
+int cbx_tune_report(char* buf, int64_t cap);
+
 /* ---- G inverse with eigen-bending -----------------------------------------
  * Replaces invert_psd_matrix (src/core/matrix_io.cpp:488-501): eigenvalues
  * below max(1e-12 lambda_max, 1e-6) are raised to that bound, then
