@@ -428,12 +428,14 @@ static void dense64(cbx_handle* h, const sv::OpView<double>& op, const double* X
     // the compensated FP64 column sums that restore the block's shift
     sv::k_colsum_x<<<ncols, 256, 0, h->stream>>>(X, S, op.p, op.ng, op.gmap, colsum);
     h->launched("k_colsum_x<f64>");
-    // the launch shape is tuned per block order and column count (two 16-column
-    // passes with 2 rows per warp measured best at n = 20,000: register pressure,
-    // not the second read of the block, limits the wider pieces)
-    const int plan = tune::choose(h, tune::FF, tune::size_class(op.ng), 0, ncols, FF_PLANS, [&](int c) {
-      ff_plan(h, op, X, S, ncols, Vt, Tout, active, c);
-    });
+    // the launch shape is tuned per block order (two 16-column passes with 2 rows
+    // per warp measured best at n = 20,000: register pressure, not the second read
+    // of the block, limits the wider pieces)
+    // one decision per block order, taken at the first product with at least 16
+    // columns (narrower ones run the same pieces under every plan but the last)
+    const int plan = tune::choose(
+        h, tune::FF, tune::size_class(op.ng), 0, 16, FF_PLANS,
+        [&](int c) { ff_plan(h, op, X, S, ncols, Vt, Tout, active, c); }, ncols >= 16);
     ff_plan(h, op, X, S, ncols, Vt, Tout, active, plan);
     return;
   }

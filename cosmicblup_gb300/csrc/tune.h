@@ -68,8 +68,11 @@ inline std::atomic<int>& enabled_flag() {
 inline bool enabled() { return enabled_flag().load() == 1; }
 
 // Candidate index for the key; run(c) launches candidate c on the handle's stream.
+// may_time = false only looks the key up (a call whose operands cannot tell the
+// candidates apart).
 template <typename F>
-int choose(cbx_handle* h, int family, int class_a, int class_b, int width, int ncand, F&& run) {
+int choose(cbx_handle* h, int family, int class_a, int class_b, int width, int ncand, F&& run,
+           bool may_time = true) {
   if (!enabled() || ncand <= 1) return 0;
   const Key key{family, h->device, class_a, class_b, width};
   {
@@ -77,6 +80,7 @@ int choose(cbx_handle* h, int family, int class_a, int class_b, int width, int n
     auto it = table().find(key);
     if (it != table().end()) return it->second.choice;
   }
+  if (!may_time) return 0;
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
   if (cudaStreamIsCapturing(h->stream, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return 0;
   Decision d;
