@@ -388,6 +388,23 @@ static void ff_piece(cbx_handle* h, const sv::OpView<double>& op, const double* 
   h->launched("k_dense_ff<f64>");
 }
 
+// The same with the packed (f32x2) kernel, for an even width W.
+template <int W, int R = rpw_ff<W>()>
+static void ff_piece2(cbx_handle* h, const sv::OpView<double>& op, const double* X, int xs, double* Vt,
+                      double* Tout, const int* active) {
+  cudaStream_t s = h->stream;
+  const Mme& mm = *h->mme;
+  float2* vhl = reinterpret_cast<float2*>(Vt);
+  sv::k_gather_hl<W><<<grid_for(W * op.ld, 256, 4 * h->num_sms), 256, 0, s>>>(X, vhl, op.p, op.ng, op.ld, op.gmap,
+                                                                            xs);
+  h->launched("k_gather_hl<f64>");
+  const int smem = W * 256 * (int)sizeof(float2);
+  ensure_smem((const void*)sv::k_dense_ff2<W, R>, smem, h->device);
+  sv::k_dense_ff2<W, R><<<(unsigned)((op.ng + 8 * R - 1) / (8 * R)), 256, smem, s>>>(mm.Qd32.p, mm.Qlo32.p, op.ng,
+                                                                                    op.ld, vhl, Tout, active, xs);
+  h->launched("k_dense_ff2<f64>");
+}
+
 // The float-float product of ncols populated columns under one launch-shape plan
 // (the autotuner's candidates; every plan gives the same bits, since each output's
 // accumulation order depends only on the K tiling):
@@ -395,24 +412,31 @@ static void ff_piece(cbx_handle* h, const sv::OpView<double>& op, const double* 
 //   1: pieces of at most 16 columns, one row per warp at width 16
 //   2: pieces of at most 8 columns (4 rows per warp)
 //   3: pieces of at most 32 columns, one row per warp at width 32
-constexpr int FF_PLANS = 4;
+//   4-7: plans 0-3 with the packed f32x2 kernel for pieces of 2 or more columns
+constexpr int FF_PLANS = 8;
 static void ff_plan(cbx_handle* h, const sv::OpView<double>& op, const double* X, int S, int ncols, double* Vt,
                     double* Tout, const int* active, int plan) {
-  const int cap = plan == 2 ? 8 : (plan == 3 ? 32 : 16);
+  const bool packed = plan >= 4;
+  const int base = plan & 3;
+  const int cap = base == 2 ? 8 : (base == 3 ? 32 : 16);
   for (int c0 = 0; c0 < ncols;) {
     const int left = std::min(ncols - c0, cap);
     int w = 1;
     while (2 * w <= left) w <<= 1;
+    const double* x = X + c0;
+    double* t = Tout + c0;
     switch (w) {
-      case 1: ff_piece<1>(h, op, X + c0, S, Vt, Tout + c0, active); break;
-      case 2: ff_piece<2>(h, op, X + c0, S, Vt, Tout + c0, active); break;
-      case 4: ff_piece<4>(h, op, X + c0, S, Vt, Tout + c0, active); break;
-      case 8: ff_piece<8>(h, op, X + c0, S, Vt, Tout + c0, active); break;
+      case 1: ff_piece<1>(h, op, x, S, Vt, t, active); break;
+      case 2: packed ? ff_piece2<2>(h, op, x, S, Vt, t, active) : ff_piece<2>(h, op, x, S, Vt, t, active); break;
+      case 4: packed ? ff_piece2<4>(h, op, x, S, Vt, t, active) : ff_piece<4>(h, op, x, S, Vt, t, active); break;
+      case 8: packed ? ff_piece2<8>(h, op, x, S, Vt, t, active) : ff_piece<8>(h, op, x, S, Vt, t, active); break;
       case 16:
-        if (plan == 1) ff_piece<16, 1>(h, op, X + c0, S, Vt, Tout + c0, active);
-        else ff_piece<16>(h, op, X + c0, S, Vt, Tout + c0, active);
+        if (base == 1) packed ? ff_piece2<16, 1>(h, op, x, S, Vt, t, active) : ff_piece<16, 1>(h, op, x, S, Vt, t, active);
+        else packed ? ff_piece2<16>(h, op, x, S, Vt, t, active) : ff_piece<16>(h, op, x, S, Vt, t, active);
         break;
-      default: ff_piece<32, 1>(h, op, X + c0, S, Vt, Tout + c0, active); break;
+      default:
+        packed ? ff_piece2<32, 1>(h, op, x, S, Vt, t, active) : ff_piece<32, 1>(h, op, x, S, Vt, t, active);
+        break;
     }
     c0 += w;
   }

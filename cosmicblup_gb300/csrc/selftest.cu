@@ -147,6 +147,14 @@ void launch_ff(cbx_handle* h, const float* qh, const float* ql, int64_t ng, int6
                                                                                              nullptr);
   h->launched("k_dense_ff");
 }
+template <int S, int R>
+void launch_ff2(cbx_handle* h, const float* qh, const float* ql, int64_t ng, int64_t ld, const float2* v, double* y) {
+  const int smem = S * 256 * (int)sizeof(float2);
+  CBX_CUDA(cudaFuncSetAttribute(cbx::sv::k_dense_ff2<S, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  cbx::sv::k_dense_ff2<S, R><<<(unsigned)((ng + 8 * R - 1) / (8 * R)), 256, smem, h->stream>>>(qh, ql, ng, ld, v, y,
+                                                                                              nullptr);
+  h->launched("k_dense_ff2");
+}
 }  // namespace
 
 extern "C" int cbx_selftest_dense_ff(cbx_handle* h, const double* Q, int64_t ng, int64_t ld, const double* V,
@@ -175,6 +183,10 @@ extern "C" int cbx_selftest_dense_ff(cbx_handle* h, const double* Q, int64_t ng,
       else if (S == 16 && rpw == 2) launch_ff<16, 2>(h, qh.p, ql.p, ng, ld, vhl.p, dY.p);
       else if (S == 16 && rpw == 4) launch_ff<16, 4>(h, qh.p, ql.p, ng, ld, vhl.p, dY.p);
       else if (S == 1 && rpw == 8) launch_ff<1, 8>(h, qh.p, ql.p, ng, ld, vhl.p, dY.p);
+      // negative rpw: the packed (f32x2) kernel with |rpw| rows per warp
+      else if (S == 16 && rpw == -2) launch_ff2<16, 2>(h, qh.p, ql.p, ng, ld, vhl.p, dY.p);
+      else if (S == 16 && rpw == -1) launch_ff2<16, 1>(h, qh.p, ql.p, ng, ld, vhl.p, dY.p);
+      else if (S == 32 && rpw == -1) launch_ff2<32, 1>(h, qh.p, ql.p, ng, ld, vhl.p, dY.p);
       else throw cbx::Error(CBX_ERR_ARG, "unsupported (S, rpw)");
     };
     run();

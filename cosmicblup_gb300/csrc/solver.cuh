@@ -379,6 +379,164 @@ __global__ void __launch_bounds__(256) k_dense_ff(const float* __restrict__ Qh, 
   }
 }
 
+// ---- packed (f32x2) float-float product -----------------------------------
+// The same float-float accumulation as k_dense_ff for two columns per instruction
+// with the sm_100-family packed FP32 operations (fma/add/sub/mul .rn.f32x2).  Each
+// lane of a packed operation rounds exactly as the scalar operation does, and the
+// order of every accumulation is unchanged, so the results are bit-identical to
+// k_dense_ff's; only the instruction count per column halves.
+typedef unsigned long long f32x2_t;
+__device__ __forceinline__ f32x2_t f2_pack(float a, float b) {
+  f32x2_t r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ void f2_unpack(f32x2_t v, float& a, float& b) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+}
+__device__ __forceinline__ f32x2_t f2_add(f32x2_t a, f32x2_t b) {
+  f32x2_t d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f32x2_t f2_sub(f32x2_t a, f32x2_t b) {
+  f32x2_t d;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f32x2_t f2_mul(f32x2_t a, f32x2_t b) {
+  f32x2_t d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f32x2_t f2_fma(f32x2_t a, f32x2_t b, f32x2_t c) {
+  f32x2_t d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+// ff_acc on a column pair.  With na = -ah, np = na bh = -fl(ah bh) exactly, so every
+// step below is the scalar step with a sign moved into an exact negation:
+//   e = fma(ah, bh, -p), t = hi + p, err = (hi - (t - z)) + (p - z) = (hi - (t - z)) - (np + z).
+__device__ __forceinline__ void ff_acc2(f32x2_t& hi, f32x2_t& lo, f32x2_t a, f32x2_t na, f32x2_t al, f32x2_t bh,
+                                        f32x2_t bl) {
+  const f32x2_t np = f2_mul(na, bh);
+  f32x2_t e = f2_fma(a, bh, np);
+  e = f2_fma(a, bl, e);
+  e = f2_fma(al, bh, e);
+  const f32x2_t t = f2_sub(hi, np);
+  const f32x2_t z = f2_sub(t, hi);
+  const f32x2_t err = f2_sub(f2_sub(hi, f2_sub(t, z)), f2_add(np, z));
+  hi = t;
+  lo = f2_add(lo, f2_add(err, e));
+}
+
+// Tout as k_dense_ff for an even S.  The staged K tile holds, per column pair q and
+// k, the float4 (hi_2q, hi_2q+1, lo_2q, lo_2q+1); lane l of the warp reads k = 4 (u 32
+// + l) + j at vt4[(q 4 + j) (KT / 4) + u 32 + l], so a warp's 16-byte reads are
+// contiguous.
+template <int S, int RPW>
+__global__ void __launch_bounds__(256) k_dense_ff2(const float* __restrict__ Qh, const float* __restrict__ Ql,
+                                                   int64_t ng, int64_t ld, const float2* __restrict__ Vhl,
+                                                   double* __restrict__ Tout, const int* __restrict__ active,
+                                                   int os = S) {
+  static_assert(S % 2 == 0, "column pairs");
+  if (active && *active == 0) return;
+  constexpr int KT = 32 * 4 * 2;
+  constexpr int NP = S / 2;
+  extern __shared__ __align__(16) uint8_t dsm[];
+  float4* vt4 = reinterpret_cast<float4*>(dsm);  // [NP * 4][KT / 4]
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int64_t row0 = (int64_t)blockIdx.x * (8 * RPW) + warp * RPW;
+  f32x2_t hi[RPW][NP], lo[RPW][NP];
+#pragma unroll
+  for (int r = 0; r < RPW; ++r)
+#pragma unroll
+    for (int q = 0; q < NP; ++q) hi[r][q] = lo[r][q] = 0ull;
+  for (int64_t k0 = 0; k0 < ld; k0 += KT) {
+    __syncthreads();
+    for (int v = tid; v < NP * KT; v += 256) {
+      const int q = v / KT, kk = v % KT;
+      float2 b0 = make_float2(0.f, 0.f), b1 = b0;
+      if (k0 + kk < ld) {
+        b0 = Vhl[(int64_t)(2 * q) * ld + k0 + kk];
+        b1 = Vhl[(int64_t)(2 * q + 1) * ld + k0 + kk];
+      }
+      vt4[(q * 4 + (kk & 3)) * (KT / 4) + (kk >> 2)] = make_float4(b0.x, b1.x, b0.y, b1.y);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < KT / 128; ++u) {
+      const int kk = u * 128 + lane * 4;
+      if (k0 + kk < ld) {
+        float4 ah[RPW], al[RPW];
+#pragma unroll
+        for (int r = 0; r < RPW; ++r) {
+          if (row0 + r < ng) {
+            ah[r] = __ldg(reinterpret_cast<const float4*>(Qh + (row0 + r) * ld + k0 + kk));
+            al[r] = __ldg(reinterpret_cast<const float4*>(Ql + (row0 + r) * ld + k0 + kk));
+          } else {
+            ah[r] = make_float4(0.f, 0.f, 0.f, 0.f);
+            al[r] = ah[r];
+          }
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          f32x2_t a2[RPW], na2[RPW], al2[RPW];
+#pragma unroll
+          for (int r = 0; r < RPW; ++r) {
+            const float a = j == 0 ? ah[r].x : (j == 1 ? ah[r].y : (j == 2 ? ah[r].z : ah[r].w));
+            const float l = j == 0 ? al[r].x : (j == 1 ? al[r].y : (j == 2 ? al[r].z : al[r].w));
+            a2[r] = f2_pack(a, a);
+            na2[r] = f2_pack(-a, -a);
+            al2[r] = f2_pack(l, l);
+          }
+#pragma unroll
+          for (int q = 0; q < NP; ++q) {
+            const float4 b = vt4[(q * 4 + j) * (KT / 4) + u * 32 + lane];
+            const f32x2_t bh = f2_pack(b.x, b.y), bl = f2_pack(b.z, b.w);
+#pragma unroll
+            for (int r = 0; r < RPW; ++r) ff_acc2(hi[r][q], lo[r][q], a2[r], na2[r], al2[r], bh, bl);
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < RPW; ++r)
+#pragma unroll
+      for (int q = 0; q < NP; ++q) {
+        float h0, h1, l0, l1;
+        f2_unpack(hi[r][q], h0, h1);
+        f2_unpack(lo[r][q], l0, l1);
+        ff_norm(h0, l0);
+        ff_norm(h1, l1);
+        hi[r][q] = f2_pack(h0, h1);
+        lo[r][q] = f2_pack(l0, l1);
+      }
+  }
+#pragma unroll
+  for (int r = 0; r < RPW; ++r) {
+    float h[S], l[S];
+#pragma unroll
+    for (int q = 0; q < NP; ++q) {
+      f2_unpack(hi[r][q], h[2 * q], h[2 * q + 1]);
+      f2_unpack(lo[r][q], l[2 * q], l[2 * q + 1]);
+    }
+#pragma unroll
+    for (int c = 0; c < S; ++c) {
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {
+        const float h2 = __shfl_xor_sync(0xffffffffu, h[c], off);
+        const float l2 = __shfl_xor_sync(0xffffffffu, l[c], off);
+        ff_add(h[c], l[c], h2, l2);
+      }
+    }
+    if (lane == 0 && row0 + r < ng) {
+#pragma unroll
+      for (int c = 0; c < S; ++c) Tout[(row0 + r) * os + c] = (double)h[c] + (double)l[c];
+    }
+  }
+}
+
 // Block-level sum of one double per thread, grouped by column c = tid % S.
 // Returns the total for column (tid % S) in threads tid < S.
 template <int S>

@@ -5,8 +5,8 @@
 // which any single output is accumulated.  The first call of a (family, device,
 // size class, width) key outside stream capture runs every candidate twice on the
 // live operands, times the second run with CUDA events on the handle's stream and
-// keeps the fastest; a candidate replaces the default only when it is at least 3 %
-// faster, so timing noise cannot flip between near-equal shapes.  Later calls (and
+// keeps the fastest; a candidate replaces the default only when it is at least 1.5 %
+// faster, so timing noise does not move a key off its default for nothing.  Later calls (and
 // calls during graph capture, which cannot time) use the stored choice, or the
 // default when none is stored yet.  The environment variable CBX_TUNE=0 (or
 // cbx_tune_enable(0)) pins every family to its default.  Because all candidates give
@@ -107,7 +107,7 @@ int choose(cbx_handle* h, int family, int class_a, int class_b, int width, int n
   int best = 0;
   for (int c = 1; c < ncand; ++c)
     if (d.ms[c] < d.ms[best]) best = c;
-  d.choice = (best != 0 && d.ms[best] <= 0.97f * d.ms[0]) ? best : 0;
+  d.choice = (best != 0 && d.ms[best] <= 0.985f * d.ms[0]) ? best : 0;
   std::lock_guard<std::mutex> lk(mu());
   auto ins = table().emplace(key, d);
   return ins.first->second.choice;

@@ -175,7 +175,7 @@ int cbx_timer_stop(cbx_handle* h, double* ms);
  * float-float block product's piece width and rows per warp, the single-RHS GEMV's
  * rows per warp and loads in flight, the genotype products' chunking) time each
  * shape once per (kernel, device, size class, width) on the live operands and keep
- * the fastest (a shape must beat the default by 3 %).  Tuning never changes a
+ * the fastest (a shape must beat the default by 1.5 %).  Tuning never changes a
  * result.  It is on unless the environment sets CBX_TUNE=0; cbx_tune_enable
  * switches it process-wide, cbx_tune_reset forgets every decision, and
  * cbx_tune_report writes one line per decision (kernel, device, size classes,

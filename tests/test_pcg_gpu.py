@@ -237,6 +237,24 @@ def test_dense_ff_product_accuracy(handle, S, rpw):
             assert err < 6e-14, (i, c, err)
 
 
+@pytest.mark.parametrize("S,rpw,packed", [(16, 2, -2), (16, 2, -1), (32, 1, -1)])
+def test_packed_ff_product_is_bit_identical(handle, S, rpw, packed):
+    """The f32x2 float-float product gives the scalar kernel's bits (same per-lane
+    rounding, same accumulation order), including ragged rows and a K tail."""
+    import ctypes as C
+    from cosmicblup_gb300._lib import lib, ptr
+    rng = np.random.default_rng(90 + S)
+    ng, ld = 1003, 2308
+    Q = rng.standard_normal((ng, ld)) * np.exp(rng.uniform(-5, 5, (ng, ld))) + 40.0
+    V = rng.standard_normal((S, ld))
+    Y1, Y2 = np.zeros((ng, S)), np.zeros((ng, S))
+    ms1, ms2 = C.c_double(0), C.c_double(0)
+    handle.check(lib().cbx_selftest_dense_ff(handle.raw, ptr(Q), ng, ld, ptr(V), S, rpw, 3, ptr(Y1), C.byref(ms1)))
+    handle.check(lib().cbx_selftest_dense_ff(handle.raw, ptr(Q), ng, ld, ptr(V), S, packed, 3, ptr(Y2), C.byref(ms2)))
+    assert np.array_equal(Y1, Y2)
+    print(f"S={S}: scalar rpw {rpw} {ms1.value:.4f} ms, packed rpw {-packed} {ms2.value:.4f} ms")
+
+
 def test_fused_iteration_matches_separate_kernels(handle, gblup, monkeypatch):
     """The persistent cooperative PCG iteration (CBX_FUSED=1) runs the same
     per-column recurrences as the separate kernels (its sums are ordered
