@@ -5,7 +5,7 @@ The compute lives in ``libcbx.so`` (CUDA for sm_103a + C++ host code, built by
 reference interfaces used by tests and benchmarks.
 """
 from ._lib import CbxError, Handle, lib  # noqa: F401
-from .grm import GrmBuilder, GrmOptions, PlinkReader, bed_snp_counts  # noqa: F401
+from .grm import GrmBuilder, GrmOptions, PlinkReader, bed_snp_counts, write_matrix_bin  # noqa: F401
 from .mme import DeviceMME  # noqa: F401
 from .vce import AIREML, RemlConfig, final_solve, invert_psd, reml_gradient, reml_logl_dense  # noqa: F401
 from .ped import ainv_henderson, ssgblup_qinv  # noqa: F401
@@ -14,7 +14,7 @@ from .batch import BatchProblem, BatchResult, batch_reml  # noqa: F401
 from .geno import DeviceGenotypes  # noqa: F401
 
 __all__ = ["CbxError", "Handle", "lib", "GrmBuilder", "GrmOptions", "PlinkReader",
-           "bed_snp_counts", "DeviceMME", "AIREML", "RemlConfig", "final_solve", "invert_psd",
+           "bed_snp_counts", "write_matrix_bin", "DeviceMME", "AIREML", "RemlConfig", "final_solve", "invert_psd",
            "reml_gradient", "reml_logl_dense",
            "ainv_henderson", "ssgblup_qinv", "MvEigenVce", "MvOptions", "solve_multi_trait",
            "BatchProblem", "BatchResult", "batch_reml", "DeviceGenotypes"]

@@ -47,6 +47,8 @@ SIGNATURES = [
     ("cbx_grm_bed", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.c_float,
                               C.c_int, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
                               C.POINTER(C.c_double), C.POINTER(C.c_int64)]),
+    ("cbx_write_upper_packed", C.c_int, [C.c_void_p, C.c_int32, C.c_char_p]),
+    ("cbx_write_grm_gcta", C.c_int, [C.c_void_p, C.c_char_p, C.c_char_p, C.c_int64]),
     ("cbx_mme_create", C.c_int, [C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.c_void_p, C.c_void_p,
                                  C.c_void_p, C.c_void_p, C.c_void_p]),
     ("cbx_mme_set_qinv_dense", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64]),

@@ -40,6 +40,7 @@ class PlinkReader:
             raise RuntimeError("No samples found in .fam file")
         bim = [ln.split() for ln in open(prefix + ".bim") if ln.strip()]
         self.fam_ids = [f[1] for f in fam]
+        self.fam_fids = [f[0] for f in fam]
         self.bim_ids = [b[1] for b in bim]
         self.num_samples, self.num_snps = len(fam), len(bim)
         with open(prefix + ".bed", "rb") as f:
@@ -118,6 +119,20 @@ class GrmBuilder:
         self.G, self.xx, self.allele_freqs = G, xx, freqs
         self.total_sum_2pq = s2pq.value
         self.total_valid_snps_count = nvalid.value
+        n_ids = len(getattr(reader, "fam_ids", []))
+        self.sample_iids = list(reader.fam_ids) if n_ids == n else [str(i + 1) for i in range(n)]
+        self.sample_fids = (list(reader.fam_fids) if len(getattr(reader, "fam_fids", [])) == n
+                            else list(self.sample_iids))
+
+    def save(self, out_prefix: str) -> None:
+        """GrmBuilder::save (src/core/grm_builder.cpp:1873-1922): writes .grm.id here
+        and .grm.bin / .grm.N.bin from the device GRM (cbx_write_grm_gcta)."""
+        with open(out_prefix + ".grm.id", "w") as f:
+            for fid, iid in zip(self.sample_fids, self.sample_iids):
+                f.write(f"{fid}\t{iid}\n")
+        self.handle.check(lib().cbx_write_grm_gcta(self.handle.raw, (out_prefix + ".grm.bin").encode(),
+                                                   (out_prefix + ".grm.N.bin").encode(),
+                                                   int(self.total_valid_snps_count)))
 
     def getGrm(self) -> np.ndarray:
         return self.G
@@ -144,3 +159,15 @@ def bed_snp_counts(handle: Handle, bed: bytes, n: int, m: int) -> dict:
                                   ptr(outs["n_hom2"]))
     handle.check(rc)
     return outs
+
+
+def write_matrix_bin(handle: Handle, which: int, bin_path: str, id_path: str | None = None,
+                     ids: list[str] | None = None) -> None:
+    """write_matrix_bin (src/core/matrix_io.cpp:479-484) for a device matrix: which = 0
+    the GRM left by cbx_grm_bed, 1 the G^-1 left by cbx_invert_psd (COSMIC_UPPER_PACKED)."""
+    if id_path is not None and ids is not None:
+        with open(id_path, "w") as f:
+            for i in ids:
+                f.write(f"{i}\n")
+    handle.check(lib().cbx_write_upper_packed(handle.raw, int(which), bin_path.encode()))
+

@@ -111,6 +111,18 @@ int cbx_grm_bed(cbx_handle* h, const uint8_t* bed, int64_t bed_bytes, int64_t n,
                 double* G, int32_t* xx_counts, float* allele_freqs,
                 double* sum2pq, int64_t* n_valid);
 
+/* ---- Relationship-matrix files ---------------------------------------------
+ * cbx_write_upper_packed writes the device GRM (which = 0, from cbx_grm_bed) or the
+ * device G^-1 (which = 1, from cbx_invert_psd) as a COSMIC_UPPER_PACKED file
+ * (io::write_upper_packed_binary, src/core/upper_packed_binary.cpp:27-68, as called
+ * by write_matrix_bin, src/core/matrix_io.cpp:479-484): the 60-byte header, then
+ * A(i, j) for i <= j column by column in FP64.  cbx_write_grm_gcta writes the device
+ * GRM as GrmBuilder::save does (src/core/grm_builder.cpp:1873-1922): .grm.bin holds
+ * G(i, j) for j <= i row by row as float, .grm.N.bin the same layout filled with
+ * (float)n_valid.  The .id files (sample names) stay with the caller. */
+int cbx_write_upper_packed(cbx_handle* h, int32_t which, const char* path);
+int cbx_write_grm_gcta(cbx_handle* h, const char* bin_path, const char* n_path, int64_t n_valid);
+
 /* ---- Mixed-model equations (one random component) ------------------------
  * Replaces MMELHSBuilder::initialize / build_lhs / build_rhs
  * (src/core/mme_builder.cpp:72-387, header src/core/mme_builder.h:26-71).
