@@ -268,23 +268,32 @@ def run_batch(args, cfg):
         d = fixed_design(rec["cats"])
         probs.append(BatchProblem(bed=bed, n=n, m=m, y=rec["y"], aid=rec["aid"], rows=d.csr(), p=d.p))
     gen_s = time.perf_counter() - t0
+    # independent problems: each rank (GPU) takes every world-th one, no collective
+    from cosmicblup_gb300.ranks import Replicas
+    reps = Replicas()
+    all_probs, probs = probs, reps.shard(probs)
     out = {}
     for label, prec, workers in [("mixed", MIXED, cfg["workers"]), ("fp64", FP64, cfg["workers"]),
                                  ("mixed_1worker", MIXED, 1)]:
         rc = RemlConfig.default(mode=MODE_EM, precision=prec, max_iter=cfg["max_iter"])
+        reps.barrier()
         t0 = time.perf_counter()
-        res = batch_reml(probs, rc, workers=workers)
-        wall = time.perf_counter() - t0
-        iters = sum(r.iterations for r in res)
-        out[label] = {"wall_s": wall, "problems_per_s": len(probs) / wall, "reml_iterations": iters,
+        res = batch_reml(probs, rc, workers=workers, device=reps.local_rank)
+        wall = reps.max(time.perf_counter() - t0)
+        iters = reps.sum(sum(r.iterations for r in res))
+        out[label] = {"wall_s": wall, "problems_per_s": len(all_probs) / wall, "reml_iterations": iters,
                       "reml_iter_per_s_incl_setup": iters / wall, "workers": workers,
-                      "sum_problem_s": sum(r.seconds for r in res)}
+                      "sum_problem_s": reps.sum(sum(r.seconds for r in res))}
+    if reps.rank != 0:
+        return
     line = {"metric": METRIC, "value": out["mixed"]["reml_iter_per_s_incl_setup"],
-            "unit": "REML iter/s (batch, GRM + G^-1 + REML per problem)", "n_gpus": 1,
+            "unit": "REML iter/s (batch, GRM + G^-1 + REML per problem)", "n_gpus": reps.world,
+            "scaling": "strong",
             "higher_is_better": True, "dtype": "f32+f64", "data": "synthetic (seeded generator)",
             "config": {"workload": cfg["name"], "problems": cfg["nprob"], "max_iter": cfg["max_iter"],
-                       "n_range": [min(p.n for p in probs), max(p.n for p in probs)],
-                       "m_range": [min(p.m for p in probs), max(p.m for p in probs)]},
+                       "n_range": [min(p.n for p in all_probs), max(p.n for p in all_probs)],
+                       "m_range": [min(p.m for p in all_probs), max(p.m for p in all_probs)],
+                       "parallelism": f"problems sharded round robin over {reps.world} GPU(s)"},
             "batch": out, "mixed_vs_fp64": out["fp64"]["wall_s"] / out["mixed"]["wall_s"],
             "workers_speedup": out["mixed_1worker"]["wall_s"] / out["mixed"]["wall_s"],
             "setup": {"synthetic_data_s": gen_s}}
@@ -346,13 +355,9 @@ def run_gpu(args, cfg):
     from cosmicblup_gb300.synth import simulate_bed
     from cosmicblup_gb300.vce import MODE_EM
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    dist = None
-    if world > 1:
-        import torch.distributed as dist  # scalars only: replicas share nothing
-        dist.init_process_group("gloo")
+    from cosmicblup_gb300.ranks import Replicas, job_rate
+    reps = Replicas()  # host scalars only: the replicas share no data
+    world, rank, local = reps.world, reps.rank, reps.local_rank
     hbm_peak, bf16_peak, peak_src = peaks()
     n, m = cfg["n"], cfg["m"]
     phases = {}
@@ -424,21 +429,16 @@ def run_gpu(args, cfg):
     clocks = ClockSampler(local)
     clocks.start()
     l0 = h.launches()
-    if dist:
-        dist.barrier()
+    reps.barrier()
     h.timer_start()
     infos = [r.run_iteration() for _ in range(args.steps)]
-    ms = h.timer_stop()
+    ms_local = h.timer_stop()
     launches = h.launches() - l0
     clk = clocks.stop()
     dl, dms, dbytes = h.profile_read(0)
     solves = sum(1 + i["probes"] for i in infos)
-    if dist:
-        import torch
-        t = torch.tensor([ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * args.steps / (ms * 1e-3)
+    value, ms = job_rate(args.steps, ms_local, reps)
+    solves_per_s, _ = job_rate(solves, ms_local, reps)
 
     # ---- plain FP64 path on the same state ----
     fp64 = None
@@ -459,6 +459,7 @@ def run_gpu(args, cfg):
 
     # ---- end to end through the C ABI from host buffers ----
     e2e_steps = max(1, min(args.steps, 3))
+    reps.barrier()
     h.timer_start()
     for _ in range(e2e_steps):
         dm2 = DeviceMME(h, rec["y"], rec["aid"], (fp, fc, fv), p, q)
@@ -468,8 +469,8 @@ def run_gpu(args, cfg):
             dm2.set_qinv_dense(None)
         r2 = AIREML(dm2, *state, RemlConfig.default(mode=MODE_EM, precision=MIXED, max_iter=1))
         r2.solve()
-    ms_e2e = h.timer_stop()
-    e2e = {"value": world * e2e_steps / (ms_e2e * 1e-3), "unit": UNIT,
+    e2e_rate, _ = job_rate(e2e_steps, h.timer_stop(), reps)
+    e2e = {"value": e2e_rate, "unit": UNIT,
            "h2d_bytes_per_step": int(h2d_bytes), "d2h_bytes_per_step": int(d2h_bytes)}
 
     # ---- genotype products: SNP-effect back-solve effect = Z^T G^-1 u / total 2pq ----
@@ -518,7 +519,7 @@ def run_gpu(args, cfg):
                    "precision": "mixed: FP32 PCG bulk + FP64 refinement on the true residual",
                    "l2": "inputs larger than L2 (1.6 GB FP32 G^-1 block read per PCG iteration)",
                    "parallelism": f"replicas x{world}"},
-        "pcg_solves_per_s": world * solves / (ms * 1e-3),
+        "pcg_solves_per_s": solves_per_s,
         "pcg_iterations_per_step": sum(i["pcg_iters"] for i in infos) / args.steps,
         "probes_per_step": sum(i["probes"] for i in infos) / args.steps,
         "fp64": fp64,
