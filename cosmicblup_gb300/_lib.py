@@ -84,6 +84,8 @@ SIGNATURES = [
                              C.POINTER(C.c_int32)]),
     ("cbx_mt_solve", C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
                                C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("cbx_host_register", C.c_int, [C.c_void_p, C.c_int64]),
+    ("cbx_host_unregister", C.c_int, [C.c_void_p]),
     ("cbx_tune_enable", C.c_int, [C.c_int32]),
     ("cbx_tune_reset", C.c_int, []),
     ("cbx_tune_report", C.c_int, [C.c_char_p, C.c_int64]),
@@ -220,3 +222,25 @@ def tune_report() -> list[str]:
     buf = C.create_string_buffer(1 << 16)
     lib().cbx_tune_report(buf, len(buf))
     return [ln for ln in buf.value.decode().splitlines() if ln]
+
+
+class pinned:
+    """Context manager page-locking numpy arrays for the duration (cbx_host_register):
+    the library's host <-> device copies of them then run at the link's full rate.
+    Arrays that cannot be registered are left pageable."""
+
+    def __init__(self, *arrays):
+        self.arrays = [a for a in arrays if a is not None and a.nbytes > 0]
+        self.done = []
+
+    def __enter__(self):
+        for a in self.arrays:
+            if lib().cbx_host_register(C.c_void_p(a.ctypes.data), a.nbytes) == CBX_OK:
+                self.done.append(a)
+        return self
+
+    def __exit__(self, *exc):
+        for a in self.done:
+            lib().cbx_host_unregister(C.c_void_p(a.ctypes.data))
+        self.done = []
+

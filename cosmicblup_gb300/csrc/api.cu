@@ -187,4 +187,14 @@ int cbx_tune_report(char* buf, int64_t cap) {
   return CBX_OK;
 }
 
+int cbx_host_register(void* p, int64_t bytes) {
+  if (!p || bytes <= 0) return CBX_ERR_ARG;
+  return cudaHostRegister(p, (size_t)bytes, cudaHostRegisterDefault) == cudaSuccess ? CBX_OK : CBX_ERR_CUDA;
+}
+
+int cbx_host_unregister(void* p) {
+  if (!p) return CBX_ERR_ARG;
+  return cudaHostUnregister(p) == cudaSuccess ? CBX_OK : CBX_ERR_CUDA;
+}
+
 }  // extern "C"

@@ -182,6 +182,14 @@ int cbx_profile_read(cbx_handle* h, int32_t bucket, int64_t* launches, double* t
 int cbx_timer_start(cbx_handle* h);
 int cbx_timer_stop(cbx_handle* h, double* ms);
 
+/* ---- Pinned host buffers (no reference counterpart) ------------------------
+ * Page-locks / releases a caller's host buffer (cudaHostRegister), so that the
+ * host <-> device copies of the entry points above run at the link's full rate
+ * instead of through pageable staging.  Optional; CBX_ERR_CUDA if the range cannot
+ * be registered. */
+int cbx_host_register(void* p, int64_t bytes);
+int cbx_host_unregister(void* p);
+
 /* ---- Launch-shape autotuner (no reference counterpart) ---------------------
  * Kernels with several launch shapes that give bit-identical results (the
  * float-float block product's piece width and rows per warp, the single-RHS GEMV's
