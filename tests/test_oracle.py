@@ -17,7 +17,7 @@ def test_toy_decode_and_xx(toy_golden):
 
 
 def test_toy_grm_known_answer(toy_golden):
-    # restated VanRaden G for the reference's toy fixture (survey of grm_builder.cpp:166-404)
+    # VanRaden G for the reference's toy fixture, restated from grm_builder.cpp:166-404
     bed = bytes.fromhex(toy_golden["bed_hex"])
     r = vanraden_grm(bed, 6, 4)
     assert r["sum2pq"] == toy_golden["sum2pq"] == 1.9861111044883728
