@@ -334,16 +334,16 @@ def run_geno(h, bed, n, m, seed, hbm_peak, want_host, reps: int = 5) -> dict:
            "elements_per_s_zt": n * m / (zms / zl * 1e-3),
            "note": "exact 64-bit fixed-point sums; integer multiply-issue bound (two 32-bit multiply-adds per code)"}
     if want_host:
-        # the oracle's Z^T v (numpy, all threads) on a bounded SNP sample, scaled to m
-        from oracle.geno import compute_stats, multiply_zt_v
-        from oracle.plink import decode_bed
-        ms_ = min(m, 2000)
-        g = decode_bed(bed[:3 + ms_ * ((n + 3) // 4)], n, ms_)
-        mean, inv = compute_stats(g)
+        # the C restatement of the reference's multiply_Zt_v loop on a bounded SNP sample,
+        # SNP ranges over all host cores as the reference's OpenMP loop, scaled to m
+        from oracle.geno import multiply_zt_v_c
+        js = min(m, 20000)
+        cores = os.cpu_count() or 1
         t0 = time.perf_counter()
-        multiply_zt_v(g, mean, inv, u)
-        out["cpu_port_zt_ms"] = (time.perf_counter() - t0) * 1e3 * m / ms_
-        out["cpu_port_sample"] = f"oracle multiply_zt_v on {ms_} of {m} SNPs, scaled"
+        multiply_zt_v_c(bed, n, m, dg.getMeans(), dg.getInvStds(), u, threads=cores, j0=0, j1=js)
+        out["cpu_port_zt_ms"] = (time.perf_counter() - t0) * 1e3 * m / js
+        out["cpu_port_sample"] = (f"C restatement of the reference's multiply_Zt_v loop on {js} of {m} SNPs, "
+                                  f"{cores} threads, scaled to m")
     return out
 
 

@@ -20,7 +20,12 @@ roundings of the sums of magnitudes).
 """
 from __future__ import annotations
 
+import ctypes as C
+import os
+
 import numpy as np
+
+from . import build as _build
 
 
 def compute_stats(geno: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
@@ -92,3 +97,32 @@ def snp_effects(geno: np.ndarray, Ginv: np.ndarray, u_g: np.ndarray):
     ok = (inv_std > 0.0) & (t2 > 0.0)
     effect[ok] = (zt[ok] / inv_std[ok]) / t2
     return effect, mean / 2.0, t2
+
+
+def multiply_zt_v_c(bed: bytes, n: int, m: int, mean: np.ndarray, inv_std: np.ndarray, v: np.ndarray,
+                    threads: int | None = None, j0: int = 0, j1: int | None = None) -> np.ndarray:
+    """Z^T v for SNPs [j0, j1) by the C restatement of the reference's loop
+    (oracle/csrc/oracle_geno.c), SNP ranges split over ``threads`` host threads (ctypes
+    releases the GIL), as the reference splits them over OpenMP threads."""
+    import concurrent.futures as cf
+    if not os.path.exists(_build.LIB):
+        _build.build()
+    L = C.CDLL(_build.LIB)
+    f = L.oracle_multiply_zt_v
+    f.argtypes = [C.c_void_p, C.c_int64, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                  C.c_int64, C.c_int64]
+    j1 = m if j1 is None else j1
+    bps = (n + 3) // 4
+    buf = np.frombuffer(bed, dtype=np.uint8)
+    mean = np.ascontiguousarray(mean, dtype=np.float64)
+    inv_std = np.ascontiguousarray(inv_std, dtype=np.float64)
+    v = np.ascontiguousarray(v, dtype=np.float64)
+    y = np.zeros(m)
+    threads = threads or os.cpu_count() or 1
+    cuts = np.linspace(j0, j1, threads + 1).astype(np.int64)
+    base = buf.ctypes.data + 3
+    with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+        list(ex.map(lambda k: f(base, n, bps, mean.ctypes.data, inv_std.ctypes.data, v.ctypes.data,
+                                y.ctypes.data, int(cuts[k]), int(cuts[k + 1])), range(threads)))
+    return y[j0:j1]
+

@@ -6,7 +6,8 @@ import math
 import numpy as np
 
 from cosmicblup_gb300.synth import encode_bed, simulate_bed
-from oracle.geno import compute_stats, multiply_z_v, multiply_zt_v, snp_effects, total_2pq, val_maps
+from oracle.geno import (compute_stats, multiply_z_v, multiply_zt_v, multiply_zt_v_c, snp_effects, total_2pq,
+                         val_maps)
 from oracle.plink import decode_bed
 
 LUT = {0: 2.0, 2: 1.0, 3: 0.0}  # PlinkReader::lookup_table (plink_reader.cpp:17-20), 1 = missing
@@ -146,3 +147,17 @@ def test_snp_effects_formula():
     ref = loop_zt(codes(bed, n, m), mean, inv, q)
     ok = inv > 0
     np.testing.assert_allclose(eff[ok], ref[ok] / inv[ok] / t2, rtol=1e-12, atol=1e-14)
+
+
+def test_c_restatement_matches_loop():
+    # the C restatement follows the reference's per-SNP sample order: the loop
+    # restatement above gives the same bits
+    n, m = 203, 29
+    bed, g = small_case(n, m, 11)
+    mean, inv = compute_stats(g)
+    v = np.random.default_rng(12).standard_normal(n)
+    ref = loop_zt(codes(bed, n, m), mean, inv, v)
+    for threads in (1, 3):
+        assert np.array_equal(multiply_zt_v_c(bed, n, m, mean, inv, v, threads=threads), ref)
+    assert np.array_equal(multiply_zt_v_c(bed, n, m, mean, inv, v, threads=2, j0=5, j1=20), ref[5:20])
+
