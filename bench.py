@@ -179,10 +179,10 @@ def cpu_pcg_iteration_cost(WtW, Qd, p, lam, iters: int, seed: int = 0, Ainv=None
     return dt / (iters + 2)  # iterations + the initial and final residual matvecs
 
 
-def read_work_file():
+def read_work_file(key: str = "fp64_pcg_iterations_per_reml_iteration"):
     try:
         txt = open(WORK_FILE).read()
-        m = re.search(r"fp64_pcg_iterations_per_reml_iteration:\s*([0-9.]+)", txt)
+        m = re.search(re.escape(key) + r":\s*([0-9.]+)", txt)
         return float(m.group(1)) if m else None
     except OSError:
         return None
@@ -203,39 +203,52 @@ def run_reference(args, cfg):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    if cfg.get("kind") in ("batch", "ssgblup"):
+    if cfg.get("kind") == "batch":
         print(json.dumps({"impl": "reference", "unavailable":
-                          f"the CPU port is timed on the GBLUP workloads only, not {cfg['name']}"}))
+                          f"the CPU port is timed on single-problem workloads only, not {cfg['name']}"}))
         return
-    import scipy.sparse as sp  # noqa: F401
+    import scipy.sparse as sp
     from cosmicblup_gb300.synth import simulate_gblup_records
     from oracle.mme import build_fixed_design, sparse_data_part
-    n = cfg["n"]
-    work = read_work_file()
+    ss = cfg.get("kind") == "ssgblup"
+    n = cfg["n"]                                   # genotyped animals: the dense block's order
+    q = cfg["n_gen"] * cfg["per_gen"] if ss else n  # animals in the random effect
+    work = read_work_file("ssgblup_fp64_operator_applications_per_reml_iteration" if ss else
+                          "fp64_pcg_iterations_per_reml_iteration")
     if work is None:
         print(json.dumps({"impl": "reference", "unavailable":
                           f"{WORK_FILE} (PCG work of one REML iteration) is missing"}))
         return
     rng = np.random.default_rng(7)
-    rec = simulate_gblup_records(n, cfg["levels"], rng.normal(0, 0.5, n), seed=cfg["seed"] + 3,
+    rec = simulate_gblup_records(q, cfg["levels"], rng.normal(0, 0.5, q), seed=cfg["seed"] + 3,
                                  var_e=cfg["var_e"])
     p, rows, _ = build_fixed_design(rec["cats"])
-    WtW, _ = sparse_data_part(rec["aid"], rows, p, n)
-    # the per-iteration cost of a dense-block operator does not depend on its
-    # values: a well-conditioned symmetric stand-in of the G^-1 block's size
+    WtW, _ = sparse_data_part(rec["aid"], rows, p, q)
+    # the per-iteration cost of the operator does not depend on its values:
+    # well-conditioned symmetric stand-ins of the dense block's order and, for
+    # ssGBLUP, of A^-1's sparsity (about 7 entries per row: self, two parents and
+    # their cross terms, and a few offspring)
     Qd = rng.standard_normal((n, n)) * (1.0 / n)
     Qd = 0.5 * (Qd + Qd.T)
     Qd[np.diag_indices(n)] += 2.0
+    Ainv = gmap = None
+    if ss:
+        k = 3 * q
+        r_, c_ = rng.integers(0, q, k), rng.integers(0, q, k)
+        off = sp.coo_matrix((np.full(k, -0.1), (r_, c_)), shape=(q, q)).tocsr()
+        Ainv = (off + off.T + sp.identity(q, format="csr") * 2.0).tocsr()
+        gmap = np.arange(q - n, q)
     lam = cfg["var_e"] / cfg["var_a"]
     per_step_iters = 10
     for _ in range(args.warmup):
-        cpu_pcg_iteration_cost(WtW, Qd, p, lam, per_step_iters)
-    costs = [cpu_pcg_iteration_cost(WtW, Qd, p, lam, per_step_iters, seed=s) for s in range(args.steps)]
+        cpu_pcg_iteration_cost(WtW, Qd, p, lam, per_step_iters, Ainv=Ainv, gmap=gmap)
+    costs = [cpu_pcg_iteration_cost(WtW, Qd, p, lam, per_step_iters, seed=s, Ainv=Ainv, gmap=gmap)
+             for s in range(args.steps)]
     c = float(np.mean(costs))
     value = 1.0 / (c * work)
     cores = os.cpu_count()
     sample = (f"oracle FP64 PCG ({per_step_iters} iterations per step, numpy/BLAS on {cores} threads) on "
-              f"the {n + p}-row operator; scaled by {work:.0f} PCG iterations per REML iteration")
+              f"the {q + p}-row operator; scaled by {work:.0f} PCG iterations per REML iteration")
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": c * per_step_iters * 1e3,
