@@ -213,11 +213,14 @@ def run_reference(args, cfg):
     ss = cfg.get("kind") == "ssgblup"
     n = cfg["n"]                                   # genotyped animals: the dense block's order
     q = cfg["n_gen"] * cfg["per_gen"] if ss else n  # animals in the random effect
-    work = read_work_file("ssgblup_fp64_operator_applications_per_reml_iteration" if ss else
-                          "fp64_pcg_iterations_per_reml_iteration")
+    key = {"c2": "fp64_pcg_iterations_per_reml_iteration",
+           "c3": "ssgblup_fp64_operator_applications_per_reml_iteration",
+           "c1": "gblup_c1_fp64_operator_applications_per_reml_iteration"}.get(args.config)
+    work = read_work_file(key) if key else None
     if work is None:
         print(json.dumps({"impl": "reference", "unavailable":
-                          f"{WORK_FILE} (PCG work of one REML iteration) is missing"}))
+                          f"no recorded PCG work of one REML iteration for {cfg['name']} "
+                          f"(profiles/reml_iteration_work.md)"}))
         return
     rng = np.random.default_rng(7)
     rec = simulate_gblup_records(q, cfg["levels"], rng.normal(0, 0.5, q), seed=cfg["seed"] + 3,
@@ -524,6 +527,11 @@ def run_gpu(args, cfg):
     if rank != 0:
         return
     ach = dbytes / (dms * 1e-3) / 1e9 if dms > 0 else None
+    block_mb = 4.0 * n * n / 1e6
+    l2_note = (f"inputs larger than L2 ({block_mb / 1e3:.2f} GB FP32 dense block read per PCG iteration)"
+               if block_mb > 129.0 else
+               f"the {block_mb:.0f} MB FP32 dense block fits in L2 (no flush between iterations): "
+               f"a cache-resident figure, not an HBM one")
     traffic = read_traffic()
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -534,7 +542,7 @@ def run_gpu(args, cfg):
                    "fixed_levels": cfg["levels"],
                    "step": "one EM+Hutchinson AI-REML iteration (data solve + probe solves, relres 1e-10)",
                    "precision": "mixed: FP32 PCG bulk + FP64 refinement on the true residual",
-                   "l2": "inputs larger than L2 (1.6 GB FP32 G^-1 block read per PCG iteration)",
+                   "l2": l2_note,
                    "parallelism": f"replicas x{world}"},
         "pcg_solves_per_s": solves_per_s,
         "pcg_iterations_per_step": sum(i["pcg_iters"] for i in infos) / args.steps,
