@@ -325,13 +325,14 @@ static double inner_tol_min() {
 static bool use_fused() { return env_int("CBX_FUSED", 0) != 0; }
 
 // Floor of the first inner solve's tolerance (environment CBX_FIRST_ITOL,
-// default 1e-3).  The first correction of a solve carries the residual's
-// component along an eigen-bent direction of the dense block (eigenvalue
-// clamp^-1), so the FP32 recursive residual drifts from the true one by about
-// eps32 ||A|| / ||r|| and the true residual stops falling near 1e-2 of its
-// start whatever the inner tolerance; iterations past 1e-3 are wasted there
-// (measured on GB300 at n = 20,000: 1e-5 -> 11.3, 1e-3 -> 12.9 REML it/s,
-// same number of refinements).  Later corrections reach their tolerance.
+// default 1e-3).  The correction is stored in FP32, and the eigen-bent direction
+// of the dense block (eigenvalue clamp^-1) turns the rounding of its entries into
+// a true residual of about eps32 (lambda_max / lambda_typical) of the correction
+// equation's right-hand side: for the first correction of a warm-started solve
+// the true residual stops falling near 1e-3..1e-2 of its start whatever the inner
+// tolerance, so iterations past 1e-3 are wasted there (measured on GB300 at
+// n = 20,000: 1e-5 -> 11.3, 1e-3 -> 12.9 REML it/s, same number of refinements).
+// Later corrections reach their tolerance.
 static double first_itol() {
   static double v = [] {
     const char* e = std::getenv("CBX_FIRST_ITOL");
