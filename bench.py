@@ -1,32 +1,39 @@
 #!/usr/bin/env python3
-"""Benchmark of the GBLUP hot path on GB300.
+"""Benchmark of the GBLUP / ssGBLUP hot path on GB300.
 
-Workload (default ``--config c2``): GBLUP with n = 20,000 genotyped animals,
-m = 50,000 SNPs (allele frequencies U(0.01, 0.5), HWE genotypes, 2 % missing),
-h2 = 0.3, fixed effects mean + 200-level contemporary group, one record per
-animal.  Seeded synthetic data of those shapes (no public dataset exists).
+Workload (default ``--config c3``): single-step GBLUP on a pedigree of 200,000
+animals over 10 discrete generations (500 sires x 10,000 dams per generation,
+random mating, 5 % unknown parents), the last 20,000 genotyped at m = 50,000
+SNPs (genotypes gene-dropped through the pedigree from base frequencies
+U(0.01, 0.5), 2 % missing calls), h2 = 0.35, one record per animal, fixed
+effects mean + 500-level herd-year.  H^-1 = A^-1 + [0; (0.95 G + 0.05 A22)^-1 -
+A22^-1] with tuneG.  Seeded synthetic data of those shapes (no public dataset
+exists).
 
-Setup (untimed, phases reported): BED -> GRM on the tensor cores -> eigen-bent
-G^-1 (FP64) -> mixed-model equations on the device.
+Setup (untimed, phases reported): BED -> GRM on the tensor cores, Henderson
+A^-1, A22 by the pedigree recursion, tuneG, blend and both FP64 inverses on
+the device, mixed-model equations on the device.
 
-Step: one AI-REML iteration, which at this size is the EM update with
-Hutchinson traces (one data solve plus >= 32 Rademacher probe solves, the probe
-blocks solved as multi-RHS PCG), every solve to relative residual 1e-10.
+Step: one AI-REML iteration -- the EM update with Hutchinson traces (one data
+solve plus the reference's adaptive probe schedule, >= 32 Rademacher probes,
+solved as multi-RHS blocks) -- followed by the REML gradient (the reference's
+AI-REML score) at the iteration's starting point from 64 probes, whose first
+probes are the iteration's own solves; every solve to relative residual 1e-10.
 ``value`` uses the mixed-precision solver (FP32 PCG bulk, FP64 refinement on
-the true residual) with all inputs resident in HBM; the plain FP64 path is
-timed on the same state for the mixed-vs-FP64 ratio.  ``e2e`` runs the public C
-ABI per step from host buffers (records uploaded, solution downloaded).
+the true residual) with all inputs resident in HBM.  The plain FP64 path runs
+the same number of steps from the same starting point; the variance
+components, the final EBVs and the gradient of the two paths are compared.
+``e2e`` runs the same step through the public C ABI from host buffers.
 
 ``--impl reference`` times the CPU restatement of the path (FP64 PCG, numpy
-with all host threads) on a bounded sample of iterations of the same operator
-and scales it by the PCG work of one REML iteration.
+with all host threads) and counts, in the run, the PCG iterations of the
+reference's algorithm (one right-hand side at a time, each solve from zero).
 """
 from __future__ import annotations
 
 import argparse
 import json
 import os
-import re
 import subprocess
 import sys
 import threading
@@ -41,27 +48,32 @@ METRIC = ("REML iter/s & PCG solves/s at relres 1e-10, mixed vs FP64, 1 GB300; "
           "GRM int8 TOPS")
 UNIT = "REML iter/s"
 
+_SS = dict(kind="ssgblup", n_gen=10, per_gen=20000, n_sires=500, n_dams=10000, p_unknown=0.05, n=20000,
+           m=50000, p_lo=0.01, miss=0.02, var_a=0.35, var_e=0.65, levels=500, seed=3000)
 CONFIGS = {
+    # single-step GBLUP (the default line): REML iteration + gradient from 64 probes
+    "c3": dict(_SS, name="ssgblup_ped200000_geno20000_m50000_hy500", grad_probes=64),
+    # the same data, gradient from 256 probes
+    "c4": dict(_SS, name="ssgblup_ped200000_geno20000_m50000_hy500_grad256", grad_probes=256),
     "c2": dict(name="gblup_n20000_m50000_cg200", n=20000, m=50000, p_lo=0.01, miss=0.02,
-               var_a=0.3, var_e=0.7, levels=200, seed=2000),
+               var_a=0.3, var_e=0.7, levels=200, seed=2000, grad_probes=0),
     # profiling case: same generator, G^-1 block (268 MB FP32) still larger than L2
     "c2s": dict(name="gblup_n8192_m16384_cg200", n=8192, m=16384, p_lo=0.01, miss=0.02,
-                var_a=0.3, var_e=0.7, levels=200, seed=2100),
+                var_a=0.3, var_e=0.7, levels=200, seed=2100, grad_probes=0),
+    # plain GBLUP, the dense exact AI-REML step (dim < 5000, as the reference chooses)
     "c1": dict(name="gblup_n2000_m10000_sex2", n=2000, m=10000, p_lo=0.05, miss=0.01,
-               var_a=0.4, var_e=0.6, levels=2, seed=1000),
-    # single-step GBLUP: 10 generations x 20,000 animals (500 sires x 10,000 dams
-    # per generation, 5 % unknown parents), the last 20,000 genotyped at m =
-    # 50,000; H^-1 = A^-1 + [0; (0.95 G + 0.05 A22)^-1 - A22^-1]; 500 herd-years
+               var_a=0.4, var_e=0.6, levels=2, seed=1000, grad_probes=0, dense=True),
     # 96 independent GBLUPs, n ~ log-uniform [500, 8000], m ~ log-uniform
     # [5000, 40000], h2 ~ U(0.1, 0.6), mean + 10-level group; each one GRM +
     # eigen-bent G^-1 + REML (3 EM iterations), the batch sharing the GPU
     "c5": dict(name="batch96_gblup_n500-8000_m5000-40000", kind="batch", nprob=96, n_lo=500, n_hi=8000,
                m_lo=5000, m_hi=40000, levels=10, max_iter=3, workers=16, seed=5000),
-    "c3": dict(name="ssgblup_ped200000_geno20000_m50000_hy500", kind="ssgblup", n_gen=10, per_gen=20000,
-               n_sires=500, n_dams=10000, p_unknown=0.05, n=20000, m=50000, p_lo=0.01, miss=0.02,
-               var_a=0.35, var_e=0.65, levels=500, seed=3000),
 }
-WORK_FILE = os.path.join(ROOT, "profiles", "reml_iteration_work.md")
+# DRAM bytes per launch of k_dense_tf32<64> from an ncu capture at n = 8,192
+# (1.0125 x the algorithmic bytes), scaled to a 20,000-row block by the block's bytes
+TRAFFIC_BYTES = {20000: 1.635e9}
+# the reference's adaptive estimator with one thread checks after two batches of 16
+REF_EM_PROBES = 32
 
 
 def log(*a):
@@ -123,14 +135,42 @@ class ClockSampler:
                 "samples": len(self.rows)}
 
 
-def build_records(cfg, bed):
-    """Phenotypes and the fixed-effect design (mu + contemporary group)."""
+def build_data(cfg) -> dict:
+    """Seeded synthetic inputs of a single-problem workload (host only): the
+    BED, the records and fixed-effect design, and for ssGBLUP the pedigree and
+    the genotyped rows (the last generation)."""
     from cosmicblup_gb300.design import fixed_design
-    from cosmicblup_gb300.synth import genetic_values, simulate_gblup_records
-    g = genetic_values(bed, cfg["n"], cfg["m"], seed=cfg["seed"] + 2, var_a=cfg["var_a"])
-    rec = simulate_gblup_records(cfg["n"], cfg["levels"], g, seed=cfg["seed"] + 3, var_e=cfg["var_e"])
-    d = fixed_design(rec["cats"])
-    return rec, d.p, d.csr()
+    from cosmicblup_gb300.synth import (genetic_values, pedigree_breeding_values, simulate_bed,
+                                        simulate_bed_gene_drop, simulate_gblup_records, simulate_pedigree)
+    n, m, seed = cfg["n"], cfg["m"], cfg["seed"]
+    d = {"sire": None, "dam": None, "gmap": None}
+    if cfg.get("kind") == "ssgblup":
+        sire, dam = simulate_pedigree(cfg["n_gen"], cfg["per_gen"], cfg["n_sires"], cfg["n_dams"],
+                                      seed=seed + 1, p_unknown=cfg["p_unknown"])
+        q = sire.size
+        d["bed"], _ = simulate_bed_gene_drop(sire, dam, cfg["per_gen"], m, seed=seed, p_lo=cfg["p_lo"],
+                                             miss=cfg["miss"])
+        a = pedigree_breeding_values(sire, dam, cfg["var_a"], seed=seed + 2)
+        rec = simulate_gblup_records(q, cfg["levels"], a, seed=seed + 3, var_e=cfg["var_e"])
+        d.update(sire=sire, dam=dam, gmap=np.arange(q - n, q, dtype=np.int32))
+    else:
+        q = n
+        d["bed"], _ = simulate_bed(n, m, seed=seed, p_lo=cfg["p_lo"], miss=cfg["miss"])
+        g = genetic_values(d["bed"], n, m, seed=seed + 2, var_a=cfg["var_a"])
+        rec = simulate_gblup_records(n, cfg["levels"], g, seed=seed + 3, var_e=cfg["var_e"])
+    dsg = fixed_design(rec["cats"])
+    d.update(rec=rec, p=dsg.p, rows=dsg.csr(), q=q)
+    return d
+
+
+def solves_per_step(cfg, em_probes: float) -> float:
+    """Single right-hand-side solves of one step in the reference's algorithm:
+    the EM iteration's data solve and probes, then for the gradient the score
+    of run_aireml_step (its own data solve and the trace probes)."""
+    s = 1.0 + em_probes
+    if cfg.get("grad_probes"):
+        s += 1.0 + cfg["grad_probes"]
+    return s
 
 
 def cpu_pcg_iteration_cost(WtW, Qd, p, lam, iters: int, seed: int = 0, Ainv=None, gmap=None) -> float:
@@ -142,6 +182,18 @@ def cpu_pcg_iteration_cost(WtW, Qd, p, lam, iters: int, seed: int = 0, Ainv=None
     preconditioner; numpy/BLAS uses every host thread."""
     from oracle.mme import pcg
     dim = WtW.shape[0]
+    matvec, prec = cpu_operator(WtW, Qd, p, lam, Ainv, gmap)
+    rng = np.random.default_rng(seed)
+    b = np.zeros(dim)
+    b[p:] = rng.choice([-1.0, 1.0], size=dim - p)
+    t0 = time.perf_counter()
+    pcg(matvec, b, prec, tol=0.0, maxit=iters)
+    dt = time.perf_counter() - t0
+    return dt / (iters + 2)  # iterations + the initial and final residual matvecs
+
+
+def cpu_operator(WtW, Qd, p, lam, Ainv=None, gmap=None):
+    """(matvec, block-Jacobi preconditioner) of the FP64 MME operator on the host."""
     d = WtW.diagonal().copy()
     if Ainv is None:
         d[p:] += lam * np.diag(Qd)
@@ -170,36 +222,24 @@ def cpu_pcg_iteration_cost(WtW, Qd, p, lam, iters: int, seed: int = 0, Ainv=None
         r[p:] = dinv * v[p:]
         return r
 
-    rng = np.random.default_rng(seed)
-    b = np.zeros(dim)
-    b[p:] = rng.choice([-1.0, 1.0], size=dim - p)
-    t0 = time.perf_counter()
-    pcg(matvec, b, prec, tol=0.0, maxit=iters)
-    dt = time.perf_counter() - t0
-    return dt / (iters + 2)  # iterations + the initial and final residual matvecs
-
-
-def read_work_file(key: str = "fp64_pcg_iterations_per_reml_iteration"):
-    try:
-        txt = open(WORK_FILE).read()
-        m = re.search(re.escape(key) + r":\s*([0-9.]+)", txt)
-        return float(m.group(1)) if m else None
-    except OSError:
-        return None
-
-
-def read_traffic():
-    try:
-        txt = open(os.path.join(ROOT, "profiles", "k_dense_tf32_s64_n8192.md")).read()
-        m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", txt)
-        return float(m.group(1)) if m else None
-    except OSError:
-        return None
+    return matvec, prec
 
 
 # ---------------------------------------------------------------------------
 def run_reference(args, cfg):
-    """CPU restatement of the path on a bounded sample (rank 0 only)."""
+    """The CPU restatement of the path on a bounded sample (rank 0 only).
+
+    The reference itself cannot be built (its CMake needs Eigen 3 and zstd.h).
+    Each step times PCG iterations of the oracle's FP64 block-Jacobi PCG (the
+    reference's PCGSolver, one right-hand side, numpy/BLAS on every host thread)
+    on the workload's full-size operator.  For ssGBLUP that operator has the
+    pedigree's real Henderson A^-1 and the records' real W'W, while the dense
+    block is a stand-in of its order, because the FP64 G and A22 inverses take
+    longer than the run may.  The cost of an iteration does not depend on the
+    block's values.  The PCG iterations per solve are counted in the run: the
+    data right-hand side is solved from zero to relres 1e-10 on this operator,
+    as the reference solves every probe.  One step of the workload is that many
+    iterations times the solves of the reference's algorithm per step."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
@@ -208,57 +248,77 @@ def run_reference(args, cfg):
                           f"the CPU port is timed on single-problem workloads only, not {cfg['name']}"}))
         return
     import scipy.sparse as sp
-    from cosmicblup_gb300.synth import simulate_gblup_records
-    from oracle.mme import build_fixed_design, sparse_data_part
-    ss = cfg.get("kind") == "ssgblup"
-    n = cfg["n"]                                   # genotyped animals: the dense block's order
-    q = cfg["n_gen"] * cfg["per_gen"] if ss else n  # animals in the random effect
-    key = {"c2": "fp64_pcg_iterations_per_reml_iteration",
-           "c3": "ssgblup_fp64_operator_applications_per_reml_iteration",
-           "c1": "gblup_c1_fp64_operator_applications_per_reml_iteration"}.get(args.config)
-    work = read_work_file(key) if key else None
-    if work is None:
-        print(json.dumps({"impl": "reference", "unavailable":
-                          f"no recorded PCG work of one REML iteration for {cfg['name']} "
-                          f"(profiles/reml_iteration_work.md)"}))
-        return
-    rng = np.random.default_rng(7)
-    rec = simulate_gblup_records(q, cfg["levels"], rng.normal(0, 0.5, q), seed=cfg["seed"] + 3,
-                                 var_e=cfg["var_e"])
-    p, rows, _ = build_fixed_design(rec["cats"])
-    WtW, _ = sparse_data_part(rec["aid"], rows, p, q)
-    # the per-iteration cost of the operator does not depend on its values:
-    # well-conditioned symmetric stand-ins of the dense block's order and, for
-    # ssGBLUP, of A^-1's sparsity (about 7 entries per row: self, two parents and
-    # their cross terms, and a few offspring)
-    Qd = rng.standard_normal((n, n)) * (1.0 / n)
-    Qd = 0.5 * (Qd + Qd.T)
-    Qd[np.diag_indices(n)] += 2.0
-    Ainv = gmap = None
-    if ss:
-        k = 3 * q
-        r_, c_ = rng.integers(0, q, k), rng.integers(0, q, k)
-        off = sp.coo_matrix((np.full(k, -0.1), (r_, c_)), shape=(q, q)).tocsr()
-        Ainv = (off + off.T + sp.identity(q, format="csr") * 2.0).tocsr()
-        gmap = np.arange(q - n, q)
-    lam = cfg["var_e"] / cfg["var_a"]
-    per_step_iters = 10
-    for _ in range(args.warmup):
-        cpu_pcg_iteration_cost(WtW, Qd, p, lam, per_step_iters, Ainv=Ainv, gmap=gmap)
-    costs = [cpu_pcg_iteration_cost(WtW, Qd, p, lam, per_step_iters, seed=s, Ainv=Ainv, gmap=gmap)
-             for s in range(args.steps)]
-    c = float(np.mean(costs))
-    value = 1.0 / (c * work)
+    from oracle.mme import MME, build_fixed_design, invert_psd_matrix, pcg, sparse_data_part
+    t0 = time.perf_counter()
+    d = build_data(cfg)
+    rec, p, q, n = d["rec"], d["p"], d["q"], cfg["n"]
+    _, orows, _ = build_fixed_design(rec["cats"])
     cores = os.cpu_count()
-    sample = (f"oracle FP64 PCG ({per_step_iters} iterations per step, numpy/BLAS on {cores} threads) on "
-              f"the {q + p}-row operator; scaled by {work:.0f} PCG iterations per REML iteration")
+    setup = {"synthetic_data_s": time.perf_counter() - t0}
+    lam = cfg["var_e"] / cfg["var_a"]
+    if cfg.get("dense"):
+        # the dense exact AI step of the oracle on the real problem (small: n = 2,000)
+        from oracle.grm import vanraden_grm
+        from oracle.reml import AIREML as OracleREML
+        t0 = time.perf_counter()
+        Gi = invert_psd_matrix(vanraden_grm(d["bed"], n, cfg["m"])["G"])
+        om = MME(rec["y"], rec["aid"], orows, p, q)
+        setup["grm_inverse_s"] = time.perf_counter() - t0
+        o = OracleREML(om, Gi, 0.5, 0.5)
+        for _ in range(args.warmup):
+            o.dense_exact_step()
+        times = []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            o.dense_exact_step()
+            times.append(time.perf_counter() - t0)
+        c = float(np.mean(times))
+        value = 1.0 / c
+        sample = f"oracle dense exact AI-REML step (numpy/BLAS on {cores} threads), {args.steps} steps timed"
+        ms = c * 1e3
+    else:
+        rng = np.random.default_rng(7)
+        WtW, W = sparse_data_part(rec["aid"], orows, p, q)
+        Qd = rng.standard_normal((n, n)) * (1.0 / n)
+        Qd = 0.5 * (Qd + Qd.T)
+        Qd[np.diag_indices(n)] += 2.0
+        Ainv = gmap = None
+        if d["sire"] is not None:
+            from oracle.ped import ainv_henderson
+            t0 = time.perf_counter()
+            ap, ac, av, _, _ = ainv_henderson(d["dam"], d["sire"])
+            Ainv = sp.csr_matrix((av, ac, ap), shape=(q, q))
+            gmap = d["gmap"]
+            setup["ainv_s"] = time.perf_counter() - t0
+        # PCG iterations per solve of the reference's algorithm, counted on this operator
+        matvec, prec = cpu_operator(WtW, Qd, p, lam, Ainv, gmap)
+        t0 = time.perf_counter()
+        _, it_solve, rel, _ = pcg(matvec, W.T @ rec["y"], prec, tol=1e-10, maxit=20000)
+        setup["count_solve_s"] = time.perf_counter() - t0
+        per_step_iters = 10
+        for _ in range(args.warmup):
+            cpu_pcg_iteration_cost(WtW, Qd, p, lam, per_step_iters, Ainv=Ainv, gmap=gmap)
+        costs = [cpu_pcg_iteration_cost(WtW, Qd, p, lam, per_step_iters, seed=s, Ainv=Ainv, gmap=gmap)
+                 for s in range(args.steps)]
+        c = float(np.mean(costs))
+        solves = solves_per_step(cfg, REF_EM_PROBES)
+        work = solves * (it_solve + 1)
+        value = 1.0 / (c * work)
+        ms = c * work * 1e3
+        sample = (f"oracle FP64 PCG, {per_step_iters} iterations per step on the {q + p}-row operator "
+                  f"(numpy/BLAS, {cores} threads; dense block a stand-in of order {n}); {it_solve} PCG "
+                  f"iterations per solve counted in this run (data right-hand side from zero, relres "
+                  f"{rel:.1e}); {solves:.0f} solves per step "
+                  f"({1 + REF_EM_PROBES} EM" + (f" + {1 + cfg['grad_probes']} gradient" if cfg.get("grad_probes")
+                                                  else "") + ")")
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": c * per_step_iters * 1e3,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic", "config": {"workload": cfg["name"], "precision": "fp64 (CPU restatement)"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "setup": setup,
     }))
 
 
@@ -368,34 +428,23 @@ def run_gpu(args, cfg):
     from cosmicblup_gb300 import AIREML, DeviceMME, Handle, RemlConfig, invert_psd
     from cosmicblup_gb300._lib import lib, pinned, ptr, tune_report
     from cosmicblup_gb300.mme import FP64, MIXED
-    from cosmicblup_gb300.synth import simulate_bed
-    from cosmicblup_gb300.vce import MODE_EM
+    from cosmicblup_gb300.vce import MODE_DENSE, MODE_EM, final_solve, reml_gradient
 
     from cosmicblup_gb300.ranks import Replicas, job_rate
     reps = Replicas()  # host scalars only: the replicas share no data
     world, rank, local = reps.world, reps.rank, reps.local_rank
     hbm_peak, bf16_peak, peak_src = peaks()
     n, m = cfg["n"], cfg["m"]
+    G_PROBES = cfg.get("grad_probes", 0)
+    dense = bool(cfg.get("dense"))
+    mode = MODE_DENSE if dense else MODE_EM
     phases = {}
     h = Handle(local)
 
     ss = cfg.get("kind") == "ssgblup"
     t0 = time.perf_counter()
-    bed, _ = simulate_bed(n, m, seed=cfg["seed"], p_lo=cfg["p_lo"], miss=cfg["miss"])
-    if ss:
-        from cosmicblup_gb300.synth import pedigree_breeding_values, simulate_gblup_records, simulate_pedigree
-        from cosmicblup_gb300.design import fixed_design
-        sire, dam = simulate_pedigree(cfg["n_gen"], cfg["per_gen"], cfg["n_sires"], cfg["n_dams"],
-                                      seed=cfg["seed"] + 1, p_unknown=cfg["p_unknown"])
-        q = sire.size
-        gmap = np.arange(q - n, q, dtype=np.int32)  # the last generation is genotyped
-        a = pedigree_breeding_values(sire, dam, cfg["var_a"], seed=cfg["seed"] + 2)
-        rec = simulate_gblup_records(q, cfg["levels"], a, seed=cfg["seed"] + 3, var_e=cfg["var_e"])
-        d = fixed_design(rec["cats"])
-        p, rows = d.p, d.csr()
-    else:
-        q = n
-        rec, p, rows = build_records(cfg, bed)
+    d = build_data(cfg)
+    bed, rec, p, rows, q, gmap = d["bed"], d["rec"], d["p"], d["rows"], d["q"], d["gmap"]
     phases["synthetic_data_s"] = time.perf_counter() - t0
 
     # GRM on the tensor cores
@@ -409,6 +458,7 @@ def run_gpu(args, cfg):
     gl, gms, gops = h.profile_read(2)
     grm = {"n": n, "m_valid": nval.value, "kernel_ms": gms,
            "tops_int8_equivalent": gops / (gms * 1e-3) / 1e12 if gms > 0 else None,
+           "frac_of_bf16_peak": gops / (gms * 1e-3) / 1e12 / bf16_peak if gms > 0 else None,
            "note": "2 n^2 m_valid integer ops; exact f16 digit GEMMs on tcgen05 (no int8 MMA on sm_103a)"}
 
     dm = DeviceMME(h, rec["y"], rec["aid"], rows, p, q)
@@ -419,8 +469,8 @@ def run_gpu(args, cfg):
         # recursion, tuneG + blend, eigen-bent Gb^-1 and A22^-1 (FP64)
         from cosmicblup_gb300 import ainv_henderson, ssgblup_qinv
         t0 = time.perf_counter()
-        Ainv_h = ainv_henderson(h, dam, sire)
-        _, Gd_h = ssgblup_qinv(dm, dam, sire, gmap, G=None, return_blocks=True)
+        Ainv_h = ainv_henderson(h, d["dam"], d["sire"])
+        _, Gd_h = ssgblup_qinv(dm, d["dam"], d["sire"], gmap, G=None, return_blocks=True)
         phases["hinv_setup_s"] = time.perf_counter() - t0
     else:
         # eigen-bent G^-1 (FP64, cuSOLVER syevd + GEMM); host copy for the CPU baseline
@@ -432,13 +482,20 @@ def run_gpu(args, cfg):
     h2d_bytes = rec["y"].nbytes + rec["aid"].nbytes + fp.nbytes + fc.nbytes + fv.nbytes
     if ss:
         h2d_bytes += sum(x.nbytes for x in Ainv_h) + Gd_h.nbytes + gmap.nbytes
-    d2h_bytes = 8 * (p + q) + 16
+    d2h_bytes = 8 * (p + q) + 16 + (16 if G_PROBES else 0)
 
-    # ---- mixed-precision REML iterations (the headline) ----
-    r = AIREML(dm, 0.5, 0.5, RemlConfig.default(mode=MODE_EM, precision=MIXED))
+    def step(r, prec):
+        """One REML iteration, then the gradient at its starting point."""
+        vu0, ve0 = r.var_u, r.var_e
+        info = r.run_iteration()
+        g = reml_gradient(r.mme, vu0, ve0, nprobe=G_PROBES, precision=prec) if G_PROBES else None
+        return info, g
+
+    # ---- mixed-precision steps (the headline) ----
+    r = AIREML(dm, 0.5, 0.5, RemlConfig.default(mode=mode, precision=MIXED))
     t0 = time.perf_counter()
     for _ in range(args.warmup):
-        r.run_iteration()
+        step(r, MIXED)
     phases["warmup_s"] = time.perf_counter() - t0
     state = (r.var_u, r.var_e)
     h.profile(True)
@@ -447,31 +504,62 @@ def run_gpu(args, cfg):
     l0 = h.launches()
     reps.barrier()
     h.timer_start()
-    infos = [r.run_iteration() for _ in range(args.steps)]
+    out = [step(r, MIXED) for _ in range(args.steps)]
     ms_local = h.timer_stop()
     launches = h.launches() - l0
     clk = clocks.stop()
     dl, dms, dbytes = h.profile_read(0)
-    solves = sum(1 + i["probes"] for i in infos)
+    _, _, ffbytes = h.profile_read(1)
+    infos = [o[0] for o in out]
+    grads = [o[1] for o in out]
+    solves = sum(1 + i["probes"] for i in infos) + sum(G_PROBES + 1 for g in grads if g)
     value, ms = job_rate(args.steps, ms_local, reps)
     solves_per_s, _ = job_rate(solves, ms_local, reps)
+    mixed_final = (r.var_u, r.var_e)
+    gradient = None
+    if G_PROBES:
+        gradient = {"probes": G_PROBES,
+                    "pcg_iterations_per_step": sum(g["pcg_iters"] for g in grads) / args.steps,
+                    "em_probe_solves_reused_per_step": sum(min(i["probes"], G_PROBES) for i in infos) / args.steps,
+                    "last": {"grad": list(grads[-1]["grad"]), "trace": grads[-1]["trace"]}}
 
-    # ---- plain FP64 path on the same state ----
-    fp64 = None
-    if args.fp64_steps > 0:
-        r64 = AIREML(dm, *state, RemlConfig.default(mode=MODE_EM, precision=FP64))
+    # ---- plain FP64 path: the same number of steps from the same start ----
+    fp64 = agreement = None
+    fp64_steps = args.steps if args.fp64_steps is None else args.fp64_steps
+    if fp64_steps > 0 and not dense:
+        r64 = AIREML(dm, *state, RemlConfig.default(mode=mode, precision=FP64))
         h.profile(True)
         h.timer_start()
-        i64 = [r64.run_iteration() for _ in range(args.fp64_steps)]
+        out64 = [step(r64, FP64) for _ in range(fp64_steps)]
         ms64 = h.timer_stop()
         dl64, dms64, db64 = h.profile_read(1)
-        fp64 = {"reml_iter_per_s": args.fp64_steps / (ms64 * 1e-3),
-                "pcg_solves_per_s": sum(1 + i["probes"] for i in i64) / (ms64 * 1e-3),
-                "ms_per_step": ms64 / args.fp64_steps,
-                "pcg_iterations_per_step": sum(i["pcg_iters"] for i in i64) / args.fp64_steps,
-                "solves_per_step": sum(1 + i["probes"] for i in i64) / args.fp64_steps,
-                "matvecs_per_step": sum(i["matvecs"] for i in i64) / args.fp64_steps,
-                "k_dense_fp64_GBps": db64 / (dms64 * 1e-3) / 1e9 if dms64 > 0 else None}
+        i64 = [o[0] for o in out64]
+        g64 = [o[1] for o in out64]
+        s64 = sum(1 + i["probes"] for i in i64) + sum(G_PROBES + 1 for g in g64 if g)
+        fp64 = {"steps": fp64_steps, "reml_iter_per_s": fp64_steps / (ms64 * 1e-3),
+                "pcg_solves_per_s": s64 / (ms64 * 1e-3), "ms_per_step": ms64 / fp64_steps,
+                "pcg_iterations_per_step": (sum(i["pcg_iters"] for i in i64)
+                                            + sum(g["pcg_iters"] for g in g64 if g)) / fp64_steps,
+                "solves_per_step": s64 / fp64_steps,
+                "matvecs_per_step": sum(i["matvecs"] for i in i64) / fp64_steps,
+                "k_dense_fp64_GBps": db64 / (dms64 * 1e-3) / 1e9 if dms64 > 0 else None,
+                "variances": {"var_u": r64.var_u, "var_e": r64.var_e}}
+        if fp64_steps == args.steps:
+            # the two paths after the same steps from the same start: variance
+            # components, final EBVs (each at its own estimates), and the
+            # gradient of both at the FP64 estimates
+            fin = (r64.var_u, r64.var_e)
+            sm = final_solve(dm, *mixed_final, solver=1, precision=MIXED, calc_se=False)["u"]
+            s64_ = final_solve(dm, *fin, solver=1, precision=FP64, calc_se=False)["u"]
+            agreement = {
+                "steps": args.steps,
+                "max_rel_diff_var": max(abs(mixed_final[0] - fin[0]) / fin[0], abs(mixed_final[1] - fin[1]) / fin[1]),
+                "max_rel_diff_ebv": float(np.abs(sm - s64_).max() / np.abs(s64_).max()),
+                "bars": {"var": 1e-6, "ebv": 1e-8}}
+            if G_PROBES:
+                gm = reml_gradient(dm, *fin, nprobe=G_PROBES, precision=MIXED)["grad"]
+                gd = reml_gradient(dm, *fin, nprobe=G_PROBES, precision=FP64)["grad"]
+                agreement["max_rel_diff_grad"] = float(np.abs(gm - gd).max() / np.abs(gd).max())
 
     # ---- end to end through the C ABI from host buffers ----
     e2e_steps = max(1, min(args.steps, 3))
@@ -487,8 +575,10 @@ def run_gpu(args, cfg):
                 dm2.set_qinv_split(*Ainv_h, Gd=Gd_h, gmap=gmap)
             else:
                 dm2.set_qinv_dense(None)
-            r2 = AIREML(dm2, *state, RemlConfig.default(mode=MODE_EM, precision=MIXED, max_iter=1))
+            r2 = AIREML(dm2, *state, RemlConfig.default(mode=mode, precision=MIXED, max_iter=1))
             r2.solve()
+            if G_PROBES:
+                reml_gradient(dm2, *state, nprobe=G_PROBES, precision=MIXED)
         e2e_rate, _ = job_rate(e2e_steps, h.timer_stop(), reps)
     e2e = {"value": e2e_rate, "unit": UNIT,
            "h2d_bytes_per_step": int(h2d_bytes), "d2h_bytes_per_step": int(d2h_bytes)}
@@ -498,31 +588,53 @@ def run_gpu(args, cfg):
     if not ss:
         geno = run_geno(h, bed, n, m, cfg["seed"], hbm_peak, want_host)
 
-    # ---- CPU baseline: the oracle's FP64 PCG on this operator, bounded sample ----
+    # ---- CPU baseline: the reference's algorithm on this operator, bounded sample ----
     cpu = None
-    if want_host and fp64 is not None:
-        from oracle.mme import build_fixed_design, sparse_data_part
+    if want_host:
+        from oracle.mme import MME, build_fixed_design, sparse_data_part
         _, orows, _ = build_fixed_design(rec["cats"])
-        WtW, _ = sparse_data_part(rec["aid"], orows, p, q)
-        lam = state[1] / state[0]
-        iters = 10 if n >= 10000 else 50
-        if ss:
-            import scipy.sparse as sp
-            ap, ac, av = Ainv_h
-            Ainv = sp.csr_matrix((av, ac, ap), shape=(q, q))
-            c = cpu_pcg_iteration_cost(WtW, Gd_h, p, lam, iters, Ainv=Ainv, gmap=gmap)
+        cores = os.cpu_count()
+        if dense:
+            from oracle.reml import AIREML as OracleREML
+            o = OracleREML(MME(rec["y"], rec["aid"], orows, p, q), Ginv_host, *state)
+            o.dense_exact_step()
+            t0 = time.perf_counter()
+            o.dense_exact_step()
+            c = time.perf_counter() - t0
+            cpu = {"value": 1.0 / c, "unit": UNIT, "cores": cores, "kind": "port",
+                   "sample": f"one oracle dense exact AI-REML step on this problem (numpy/BLAS, {cores} threads)"}
         else:
-            c = cpu_pcg_iteration_cost(WtW, Ginv_host, p, lam, iters)
-        # one RHS at a time on the CPU: every CG iteration of every solve plus
-        # the initial residual of each solve is one operator application; the
-        # count of the reference's algorithm (probes from x0 = 0) where it was
-        # recorded for this workload, else the FP64 path's
-        work = read_work_file() if cfg["name"].startswith("gblup_n20000") else None
-        if work is None:
-            work = fp64["pcg_iterations_per_step"] + fp64["solves_per_step"]
-        cpu = {"value": 1.0 / (c * work), "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
-               "sample": f"oracle FP64 PCG, {iters} iterations on this operator (numpy/BLAS, all threads); "
-                         f"scaled by {work:.0f} single-RHS operator applications per REML iteration"}
+            from oracle.rng import rademacher
+            WtW, W = sparse_data_part(rec["aid"], orows, p, q)
+            lam = state[1] / state[0]
+            iters = 10 if n >= 10000 else 50
+            if ss:
+                import scipy.sparse as sp
+                ap, ac, av = Ainv_h
+                c = cpu_pcg_iteration_cost(WtW, Gd_h, p, lam, iters, Ainv=sp.csr_matrix((av, ac, ap), shape=(q, q)),
+                                           gmap=gmap)
+            else:
+                c = cpu_pcg_iteration_cost(WtW, Ginv_host, p, lam, iters)
+            # PCG iterations per solve of the reference's algorithm on this operator,
+            # counted in this run: the data right-hand side and two probes, each a
+            # single-RHS FP64 PCG from zero to relres 1e-10 (the GPU's FP64 path runs
+            # the same iterations as the oracle's PCG, in seconds instead of minutes)
+            B = [W.T @ rec["y"]]
+            for z in rademacher(42, q, 2):
+                b = np.zeros(p + q)
+                b[p:] = z
+                B.append(b)
+            its = [int(dm2.pcg_solve(lam, b, precision=FP64)[1][0]) for b in B]
+            per_solve = float(np.mean(its)) + 1.0
+            em_probes = sum(i["probes"] for i in infos) / args.steps
+            nsolve = solves_per_step(cfg, em_probes)
+            work = nsolve * per_solve
+            cpu = {"value": 1.0 / (c * work), "unit": UNIT, "cores": cores, "kind": "port",
+                   "sample": (f"oracle FP64 PCG, {iters} iterations on this operator (numpy/BLAS, {cores} "
+                              f"threads) = {c * 1e3:.1f} ms per iteration; x {work:.0f} single-RHS operator "
+                              f"applications per step = {nsolve:.0f} solves x {per_solve:.0f} (PCG iterations "
+                              f"per solve from zero counted in this run: data {its[0]}, probes {its[1]}, "
+                              f"{its[2]})")}
 
     if rank != 0:
         return
@@ -532,23 +644,31 @@ def run_gpu(args, cfg):
                if block_mb > 129.0 else
                f"the {block_mb:.0f} MB FP32 dense block fits in L2 (no flush between iterations): "
                f"a cache-resident figure, not an HBM one")
-    traffic = read_traffic()
+    if dense:
+        l2_note = f"dense exact step on {p + q}-order FP64 matrices (32 MB each); cache-resident"
+    step_desc = ("one dense exact AI-REML step (FP64 Cholesky, P, AI traces, logL-checked halving)" if dense else
+                 "one EM+Hutchinson AI-REML iteration (data solve + adaptive probe solves, relres 1e-10)"
+                 + (f", then the REML gradient at its starting point from {G_PROBES} probes (the iteration's "
+                    f"probe solves reused)" if G_PROBES else ""))
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if dense else "f32+f64",
         "data": "synthetic (seeded generator with the workload's shapes)",
         "config": {"workload": cfg["name"], "n_animals": q, "n_genotyped": n, "n_snps": m,
-                   "fixed_levels": cfg["levels"],
-                   "step": "one EM+Hutchinson AI-REML iteration (data solve + probe solves, relres 1e-10)",
-                   "precision": "mixed: FP32 PCG bulk + FP64 refinement on the true residual",
+                   "fixed_levels": cfg["levels"], "step": step_desc,
+                   "precision": ("fp64" if dense else "mixed: FP32 PCG bulk + FP64 refinement on the true residual"),
+                   "genotypes": "gene-dropped through the pedigree" if ss else "HWE, independent samples",
                    "l2": l2_note,
                    "parallelism": f"replicas x{world}"},
         "pcg_solves_per_s": solves_per_s,
-        "pcg_iterations_per_step": sum(i["pcg_iters"] for i in infos) / args.steps,
+        "pcg_iterations_per_step": (sum(i["pcg_iters"] for i in infos)
+                                    + sum(g["pcg_iters"] for g in grads if g)) / args.steps,
         "probes_per_step": sum(i["probes"] for i in infos) / args.steps,
+        "gradient": gradient,
         "fp64": fp64,
         "mixed_vs_fp64": (value / world) / fp64["reml_iter_per_s"] if fp64 else None,
+        "agreement": agreement,
         "grm": grm,
         "snp_backsolve": geno,
         "setup": phases,
@@ -556,10 +676,15 @@ def run_gpu(args, cfg):
         "e2e": e2e,
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm",
-                     "kernel": "k_dense_tf32<64> (tcgen05 3xTF32, G^-1 block x [data | 32 probes])",
+                     "kernel": "k_dense_tf32<64> (tcgen05 3xTF32, dense H^-1 / G^-1 block x up to 64 columns)",
                      "achieved": ach, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": (ach / hbm_peak) if ach else None, "traffic": traffic,
-                     "peak_source": peak_src, "launches": dl, "avg_launch_ms": dms / dl if dl else None},
+                     "frac": (ach / hbm_peak) if ach else None, "traffic": TRAFFIC_BYTES.get(n),
+                     "peak_source": peak_src, "launches": dl, "avg_launch_ms": dms / dl if dl else None,
+                     "step_dense_bytes_GBps": (dbytes + ffbytes) / (ms_local * 1e-3) / 1e9,
+                     "step_hbm_frac": (dbytes + ffbytes) / (ms_local * 1e-3) / 1e9 / hbm_peak,
+                     "step_note": "the step's dense-block bytes (FP32 products and float-float "
+                                  "refinement products) over the whole step time; sparse and vector "
+                                  "traffic not counted"},
         "cpu_baseline": cpu,
         "variances": {"var_u": r.var_u, "var_e": r.var_e},
         "autotune": tune_report(),
@@ -573,8 +698,9 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="cbx", choices=["cbx", "reference"])
-    ap.add_argument("--config", default="c2", choices=sorted(CONFIGS))
-    ap.add_argument("--fp64-steps", type=int, default=1)
+    ap.add_argument("--config", default="c3", choices=sorted(CONFIGS))
+    ap.add_argument("--fp64-steps", type=int, default=None,
+                    help="FP64 comparison steps (default: --steps)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     cfg = CONFIGS[args.config]

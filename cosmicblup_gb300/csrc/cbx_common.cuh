@@ -67,16 +67,20 @@ __device__ __forceinline__ bool mbar_try(uint64_t* bar, uint32_t parity) {
   return ok != 0;
 }
 // Wait until the phase with the given parity has completed.  Gives up after
-// kWaitLimitNs or when *abort becomes non-zero; returns false in that case.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity,
-                                          volatile int* abort) {
+// limit_ns or when *abort becomes non-zero; returns false in that case.
+__device__ __forceinline__ bool mbar_wait_for(uint64_t* bar, uint32_t parity,
+                                              volatile int* abort, uint64_t limit_ns) {
   if (mbar_try(bar, parity)) return true;
   const uint64_t t0 = global_ns();
   while (true) {
     if (mbar_try(bar, parity)) return true;
     if (*abort) return false;
-    if (global_ns() - t0 > kWaitLimitNs) return false;
+    if (global_ns() - t0 > limit_ns) return false;
   }
+}
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity,
+                                          volatile int* abort) {
+  return mbar_wait_for(bar, parity, abort, kWaitLimitNs);
 }
 
 // ---- async proxy / cp.async ---------------------------------------------

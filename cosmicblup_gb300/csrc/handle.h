@@ -34,6 +34,9 @@ struct cbx_handle {
   std::shared_ptr<void> dense_slot;
   // genotypes kept on the device by cbx_geno_attach (matrix-free Z / Z^T products)
   std::shared_ptr<void> geno_slot;
+  // device address of the static scratch array of cbx_dense_apply_noalloc,
+  // resolved by this handle's first call (with the handle's device current)
+  void* noalloc_scratch = nullptr;
 
   // optional per-launch timing of the dense block product (bench roofline):
   // bucket 0 = FP32 launches, bucket 1 = FP64 launches

@@ -1457,14 +1457,16 @@ extern "C" int cbx_pcg_solve(cbx_handle* h, double lambda, int32_t nrhs, const d
     pcg_solve(h, lambda, nrhs, m.io_b.p, xb.p, use_x0 != 0, tol, maxit, tol_mode, precision, r);
     CBX_CUDA(cudaMemcpyAsync(X, xb.p, n * sizeof(double), cudaMemcpyDeviceToHost, s));
     CBX_CUDA(cudaStreamSynchronize(s));
+    // A column that breaks down twice (|p'Ap| < 1e-300 after the restart) stops
+    // with its iterate, as PCGSolver::solve does (pcg_solver.h:482-495): the
+    // reference leaves its loop, reports max_iter iterations and the true
+    // residual (pcg_solver.h:530-534) and raises nothing; so does this call.
     for (int c = 0; c < nrhs; ++c) {
-      if (iters) iters[c] = r.iters[c];
+      if (iters) iters[c] = r.status[c] == sv::COL_BREAKDOWN ? maxit : r.iters[c];
       if (relres) relres[c] = r.relres[c];
     }
-    for (int c = 0; c < nrhs; ++c) {
+    for (int c = 0; c < nrhs; ++c)
       if (r.status[c] == sv::COL_NONFINITE) throw Error(CBX_ERR_NONFINITE, "non-finite PCG iterate");
-      if (r.status[c] == sv::COL_BREAKDOWN) throw Error(CBX_ERR_BREAKDOWN, "PCG breakdown");
-    }
   });
 }
 

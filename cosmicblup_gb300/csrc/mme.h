@@ -72,23 +72,38 @@ struct Mme {
   DevBuf<double> last_resid;
   bool has_last_resid = false;
   double last_lam = 0.0;
-  // probe solutions of the previous REML iteration (the probe stream repeats
-  // every iteration), with their residuals and lambda per column
+  // probe solutions of the previous REML iteration or gradient (the probe
+  // stream repeats at every call), with their residuals and lambda per column
   DevBuf<double> probe_x, probe_r;
   std::vector<double> probe_lam;   // per stored column
   std::vector<char> probe_r_ok;    // residual column valid (mixed-precision solve)
   int probe_seed = -1;
-  // right-hand sides of the EM iteration, column-major dim x (1 + max probes):
-  // column 0 = W'y, column 1 + j = [0; z_j] for Rademacher probe j.  The
-  // probe stream restarts at the same seed every iteration, so each batch of
-  // probes is generated on the host and uploaded once (probe_have[j]).
+  // right-hand sides of the EM iteration and the gradient, column-major
+  // dim x (1 + probe_cap): column 0 = W'y, column 1 + j = [0; z_j] for
+  // Rademacher probe j.  The probe stream restarts at the same seed at every
+  // call, so each batch of probes is generated on the host and uploaded once
+  // (probe_have[j]).
   DevBuf<double> em_B;
   std::vector<char> probe_have;
   int em_B_seed = -1;
+  int probe_cap = 0;               // probe columns allocated in em_B / probe_x / probe_r / probe_zv
+  // z_j' Qinv C^uu z_j of every probe column solved by the last forward pass
+  DevBuf<double> probe_zv;
+  // Forward state of the last EM iteration (or gradient): its point (var_u,
+  // var_e), solver settings, e'e and u'Qinv u of its data solve, and how many
+  // leading probe columns were solved there (their probe_zv values are valid).
+  // The REML score at that point needs nothing else.
+  struct Forward {
+    bool valid = false;
+    double vu = 0.0, ve = 0.0, pcg_tol = 0.0;
+    int precision = -1, seed = -1, solved = 0;
+    double uQu = 0.0, e_sse = 0.0;
+  } fwd;
   void drop_carry() {
     has_last = has_last_resid = false;
     probe_lam.clear();
     probe_r_ok.clear();
+    fwd.valid = false;
   }
   // persistent solver workspaces, indexed by log2 of the RHS block width
   std::unique_ptr<SolverBase> solvers[7];

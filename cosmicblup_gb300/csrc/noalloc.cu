@@ -1,19 +1,20 @@
 // Dense Qinv block product that allocates no device memory.
 //
-// Some callers cannot allocate device memory while they run: code that is
-// being captured into a CUDA graph (cudaMalloc is not allowed during stream
-// capture), code running inside a host framework that owns the device memory
-// pool, or latency-critical loops that must not pay for cudaMalloc / cudaFree.
+// Some callers cannot allocate device memory while they run: code running
+// inside a host framework that owns the whole device memory pool (its
+// allocator must not be bypassed), and latency-critical loops that must not
+// pay for cudaMalloc / cudaFree, which may synchronize the device.
 // cbx_dense_apply_noalloc gives them Y = Qd X for the dense Qinv block of the
 // handle's MME with every intermediate in a fixed static device array:
 //   * the array holds kScratchBytes (32 MiB) and stays resident on every GPU
 //     that loads libcbx until the process exits;
-//   * its device address is resolved with cudaGetSymbolAddress the first time
-//     the entry point runs on a device (with that device current), so that
-//     first call should come before any stream capture;
+//   * its device address is resolved with cudaGetSymbolAddress by a handle's
+//     first call (with the handle's device current) and kept in the handle, so
+//     that first call should come before any stream capture;
 //   * every call reuses the same array, which keeps the previous call's
 //     contents; the padding the kernel reads is cleared on every call;
-//   * calls that overlap on the GPU (two streams, two threads) race on the array.
+//   * calls that overlap on the GPU (two streams, two threads, two handles on
+//     one device) race on the array.
 #include "handle.h"
 #include "solver.cuh"
 
@@ -22,8 +23,6 @@ namespace noalloc {
 
 constexpr size_t kScratchBytes = size_t(32) << 20;
 static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
-constexpr int kMaxDevices = 64;
-static void* g_scratch_dev[kMaxDevices] = {};
 
 // Vt[c][k] = X[c * q + k] for k < q, 0 for q <= k < ld (column-major X of nc columns)
 __global__ void k_pad_cols(const double* __restrict__ X, int64_t q, int64_t ld, int nc, int S, double* __restrict__ Vt) {
@@ -58,7 +57,7 @@ static void chunk(cbx_handle* h, const Mme& m, int nc, const double* X, double* 
   constexpr int R = sizeof(double) == 8 ? (S <= 8 ? 8 : (S == 16 ? 4 : 2)) : 8;
   constexpr int KT = 32 * sv::Vec16<double>::n * 4;
   const int smem = S * KT * (int)sizeof(double);
-  CBX_CUDA(cudaFuncSetAttribute(sv::k_dense<double, S, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  ensure_smem((const void*)sv::k_dense<double, S, R>, smem, h->device);
   sv::k_dense<double, S, R><<<(unsigned)((m.ng + 8 * R - 1) / (8 * R)), 256, smem, h->stream>>>(
       m.Qd64.p, m.ng, m.ld, Vt, Tout, nullptr);
   h->launched("k_dense");
@@ -78,29 +77,29 @@ extern "C" int cbx_dense_apply_noalloc(cbx_handle* h, int32_t nrhs, const double
     CBX_REQUIRE(m.has_dense && !m.has_sparse && m.ng == m.q, CBX_ERR_UNSUPPORTED,
                 "the no-allocation product covers a dense Qinv only");
     CBX_REQUIRE(nrhs > 0 && X_dev && Y_dev, CBX_ERR_ARG, "bad vectors");
-    CBX_REQUIRE(h->device >= 0 && h->device < noalloc::kMaxDevices, CBX_ERR_ARG, "device index too large");
     CBX_CUDA(cudaSetDevice(h->device));
-    const int S = nrhs >= 32 ? 32 : (nrhs > 16 ? 32 : nrhs > 8 ? 16 : nrhs > 4 ? 8 : nrhs > 2 ? 4 : nrhs > 1 ? 2 : 1);
-    const size_t need = sizeof(double) * ((size_t)S * m.ld + (size_t)m.ng * S);
+    // columns per pass: 32, and for the last pass the smallest width that holds it
+    auto width = [](int nc) { return nc > 16 ? 32 : nc > 8 ? 16 : nc > 4 ? 8 : nc > 2 ? 4 : nc > 1 ? 2 : 1; };
+    const int S0 = width(std::min(32, (int)nrhs));
+    const size_t need = sizeof(double) * ((size_t)S0 * m.ld + (size_t)m.ng * S0);
     CBX_REQUIRE(need <= noalloc::kScratchBytes, CBX_ERR_ARG,
-                "q = " + std::to_string(m.q) + " with " + std::to_string(S) + " columns per pass needs " +
+                "q = " + std::to_string(m.q) + " with " + std::to_string(S0) + " columns per pass needs " +
                     std::to_string(need) + " bytes of scratch; the no-allocation product is limited to " +
                     std::to_string(noalloc::kScratchBytes) + " bytes (q <= ~65,000 at 32 columns)");
-    // set-up on first use on this device: resolve the static array's device address
-    void*& sp = noalloc::g_scratch_dev[h->device];
-    if (!sp) {
+    // set-up on this handle's first call: the static array's device address
+    if (!h->noalloc_scratch) {
       void* p = nullptr;
       const cudaError_t e = cudaGetSymbolAddress(&p, noalloc::g_scratch);
       CBX_REQUIRE(e == cudaSuccess && p, CBX_ERR_CUDA,
                   std::string("cudaGetSymbolAddress of the scratch array: ") + cudaGetErrorString(e));
-      sp = p;
+      h->noalloc_scratch = p;
     }
-    unsigned char* scratch = static_cast<unsigned char*>(sp);
+    unsigned char* scratch = static_cast<unsigned char*>(h->noalloc_scratch);
     for (int c0 = 0; c0 < nrhs; c0 += 32) {
       const int nc = std::min(32, nrhs - c0);
       const double* X = X_dev + (int64_t)c0 * m.q;
       double* Y = Y_dev + (int64_t)c0 * m.q;
-      switch (S == 32 ? 32 : S) {
+      switch (width(nc)) {
         case 1: noalloc::chunk<1>(h, m, nc, X, Y, scratch); break;
         case 2: noalloc::chunk<2>(h, m, nc, X, Y, scratch); break;
         case 4: noalloc::chunk<4>(h, m, nc, X, Y, scratch); break;

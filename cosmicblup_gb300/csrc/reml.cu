@@ -243,6 +243,129 @@ static std::vector<double> coldots(cbx_handle* h, const double* A, int64_t lda, 
   return d2h(h, out.p, ncols);
 }
 
+// ---------------------------------------------------------------------------
+// Probe stores shared by the EM iteration and the gradient.
+//
+// The reference's probe stream restarts at the same seed at every call
+// (AdaptiveTraceEstimator: batches of 16, batch b drawn from
+// mt19937_64(seed + first index of b)), so probe j is the same vector in every
+// EM iteration and every gradient call.  Per probe column the handle keeps the
+// right-hand side [0; z_j] (em_B column 1 + j), the latest solution with the
+// lambda it belongs to and, in mixed precision, its true residual, and
+// z_j' Qinv C^uu z_j of the last forward pass (probe_zv).
+
+// Grow b to count elements, keeping its first keep elements and zeroing the rest.
+template <typename T>
+static void grow_keep(cbx_handle* h, DevBuf<T>& b, size_t keep, size_t count) {
+  if (b.n >= count) return;
+  DevBuf<T> nb;
+  nb.resize(count);
+  CBX_CUDA(cudaMemsetAsync(nb.p, 0, count * sizeof(T), h->stream));
+  keep = std::min(keep, b.n);
+  if (keep && b.p)
+    CBX_CUDA(cudaMemcpyAsync(nb.p, b.p, keep * sizeof(T), cudaMemcpyDeviceToDevice, h->stream));
+  b = std::move(nb);  // the old buffer's cudaFree waits for the copy
+}
+
+// Make room for cap probe columns of the stream `seed`; a new seed forgets
+// every stored probe.
+static void probe_store(cbx_handle* h, Mme& m, int seed, int cap) {
+  if (m.em_B_seed != seed || m.probe_seed != seed) {
+    m.probe_have.assign(m.probe_have.size(), 0);
+    m.probe_lam.clear();
+    m.probe_r_ok.clear();
+    m.fwd.valid = false;
+    m.em_B_seed = m.probe_seed = seed;
+  }
+  if (m.probe_cap >= cap) return;
+  const size_t dim = (size_t)m.dim, old = (size_t)m.probe_cap;
+  grow_keep(h, m.em_B, dim * (1 + old), dim * (1 + (size_t)cap));
+  grow_keep(h, m.probe_x, dim * old, dim * (size_t)cap);
+  grow_keep(h, m.probe_r, dim * old, dim * (size_t)cap);
+  grow_keep(h, m.probe_zv, old, (size_t)cap);
+  m.probe_have.resize(cap, 0);
+  m.probe_cap = cap;
+}
+
+// Upload the batch of probes [start, start + size) (rows p.. of em_B columns
+// 1 + start ..; the fixed rows stay zero) unless every column is there.
+static void probe_batch(cbx_handle* h, Mme& m, int seed, int start, int size) {
+  bool all = true;
+  for (int j = 0; j < size; ++j) all = all && m.probe_have[start + j];
+  if (all) return;
+  const int64_t q = m.q, dim = m.dim, p = m.p;
+  std::vector<double> Zb((size_t)q * size);
+  std::mt19937_64 gen((unsigned long)(seed + start));
+  std::uniform_int_distribution<int> dist(0, 1);
+  for (int j = 0; j < size; ++j)
+    for (int64_t i = 0; i < q; ++i) Zb[(size_t)j * q + i] = dist(gen) == 0 ? -1.0 : 1.0;
+  CBX_CUDA(cudaMemcpy2DAsync(m.em_B.p + (size_t)(1 + start) * dim + p, dim * sizeof(double), Zb.data(),
+                             q * sizeof(double), q * sizeof(double), size, cudaMemcpyHostToDevice, h->stream));
+  CBX_CUDA(cudaStreamSynchronize(h->stream));
+  for (int j = 0; j < size; ++j) m.probe_have[start + j] = 1;
+}
+
+// The stored solutions of probes [c0, c0 + k) are a warm start when every one
+// exists, and (mixed precision) their residuals carry to a new lambda when
+// all were solved at one lambda.
+static bool probes_warm(const Mme& m, int c0, int k) { return (int)m.probe_lam.size() >= c0 + k; }
+static bool probes_carry(const Mme& m, int c0, int k) {
+  bool ok = probes_warm(m, c0, k);
+  if (ok)
+    for (int c = c0; c < c0 + k; ++c) ok = ok && m.probe_r_ok[c] && m.probe_lam[c] == m.probe_lam[c0];
+  return ok;
+}
+static void probes_record(Mme& m, int c0, int k, double lam, bool mixed) {
+  if ((int)m.probe_lam.size() < c0 + k) {
+    m.probe_lam.resize(c0 + k);
+    m.probe_r_ok.resize(c0 + k);
+  }
+  for (int c = c0; c < c0 + k; ++c) {
+    m.probe_lam[c] = lam;
+    m.probe_r_ok[c] = mixed;
+  }
+}
+
+// Solve probes [c0, c0 + k) at lam in place in probe_x (residuals into probe_r).
+static void probe_solve(cbx_handle* h, Mme& m, double lam, int c0, int k, int precision, double tol, int maxit,
+                        PcgResult& pr) {
+  const int64_t dim = m.dim;
+  const bool warm = probes_warm(m, c0, k), carry = probes_carry(m, c0, k);
+  ResidCarry pc;
+  pc.r_prev = carry ? m.probe_r.p + (size_t)c0 * dim : nullptr;
+  pc.dlam = carry ? lam - m.probe_lam[c0] : 0.0;
+  pc.r_out = m.probe_r.p + (size_t)c0 * dim;
+  pcg_solve(h, lam, k, m.em_B.p + (size_t)(1 + c0) * dim, m.probe_x.p + (size_t)c0 * dim, warm, tol, maxit, 0,
+            precision, pr, &pc);
+  probes_record(m, c0, k, lam, precision != 0);
+  for (int c = 0; c < k; ++c)
+    if (pr.status[c] == sv::COL_NONFINITE) throw Error(CBX_ERR_NONFINITE, "non-finite probe solve");
+}
+
+// z_j' Qinv C^uu z_j for probe columns [c0, c0 + k) into probe_zv[c0 ..]:
+// Qinv C^uu z from the solutions and their true residuals in mixed precision
+// (qinv_from_solution: one sparse product), else the product with the u rows.
+static void probe_values(cbx_handle* h, Mme& m, double lam, int c0, int k, bool mixed) {
+  cudaStream_t s = h->stream;
+  const int64_t p = m.p, q = m.q, dim = m.dim;
+  const double* B = m.em_B.p + (size_t)(1 + c0) * dim;
+  const double* X = m.probe_x.p + (size_t)c0 * dim;
+  DevBuf<double> QW;
+  QW.resize((size_t)q * k);
+  if (mixed) {
+    qinv_from_solution(h, lam, k, B, X, m.probe_r.p + (size_t)c0 * dim, QW.p);
+  } else {
+    DevBuf<double> Wu;
+    Wu.resize((size_t)q * k);
+    CBX_CUDA(cudaMemcpy2DAsync(Wu.p, q * sizeof(double), X + p, dim * sizeof(double), q * sizeof(double), k,
+                               cudaMemcpyDeviceToDevice, s));
+    qinv_apply(h, k, Wu.p, QW.p);
+  }
+  // the u rows of the probe columns are z
+  k_coldot<<<k, 256, 0, s>>>(B + p, dim, QW.p, q, q, m.probe_zv.p + c0);
+  h->launched("k_coldot");
+}
+
 // One EM iteration (vce.cpp:1490-1574).
 //
 // The reference solves the data system, then the probe batches of the
@@ -251,7 +374,8 @@ static std::vector<double> coldots(cbx_handle* h, const double* A, int64_t lda, 
 // and in mixed precision the data right-hand side joins that block (the
 // systems share the matrix, so one read of the dense block per PCG iteration
 // serves them all).  Results per column are those of separate solves: every
-// column runs its own CG recurrence and refinement.
+// column runs its own CG recurrence and refinement.  The iteration leaves its
+// forward state (m.fwd) for a gradient at its starting point.
 static void em_iteration(cbx_handle* h, const RemlConfigI& cfg, double& vu, double& ve, IterInfo& info) {
   Mme& m = *h->mme;
   cudaStream_t s = h->stream;
@@ -259,6 +383,7 @@ static void em_iteration(cbx_handle* h, const RemlConfigI& cfg, double& vu, doub
   const double start_vu = vu, start_ve = ve;
   const double lam = ve / std::max(vu, 1e-9);
   const bool mixed = cfg.precision != 0;
+  m.fwd.valid = false;
   m.last_solution.resize(dim);
   m.last_resid.resize(dim);
 
@@ -271,40 +396,9 @@ static void em_iteration(cbx_handle* h, const RemlConfigI& cfg, double& vu, doub
   if (min_s <= 0) min_s = 10;
   if (max_s < min_s) max_s = min_s;
   const int batch = 16;  // max(16, 4 * threads) with one thread
-  if (m.probe_seed != cfg.seed) {
-    m.probe_lam.clear();
-    m.probe_r_ok.clear();
-    m.probe_seed = cfg.seed;
-  }
-  const size_t cap = (size_t)dim * max_s;
-  if (m.probe_x.n < cap) {
-    m.probe_x.resize(cap);
-    m.probe_r.resize(cap);
-    m.probe_lam.clear();
-    m.probe_r_ok.clear();
-  }
-
-  // right-hand sides: W'y and the probe columns, generated once per seed
-  if (m.em_B_seed != cfg.seed || m.em_B.n < (size_t)dim * (1 + max_s)) {
-    m.em_B.resize((size_t)dim * (1 + max_s));
-    m.em_B.zero(s);
-    m.probe_have.assign(max_s, 0);
-    m.em_B_seed = cfg.seed;
-  }
+  probe_store(h, m, cfg.seed, max_s);
+  // column 0 of em_B: W'y
   CBX_CUDA(cudaMemcpyAsync(m.em_B.p, m.rhs.p, dim * sizeof(double), cudaMemcpyDeviceToDevice, s));
-  auto ensure_batch = [&](int start, int size) {
-    if (m.probe_have[start]) return;
-    std::vector<double> Zb((size_t)q * size);
-    std::mt19937_64 gen((unsigned long)(cfg.seed + start));
-    std::uniform_int_distribution<int> dist(0, 1);
-    for (int j = 0; j < size; ++j)
-      for (int64_t i = 0; i < q; ++i) Zb[(size_t)j * q + i] = dist(gen) == 0 ? -1.0 : 1.0;
-    // the u rows of columns 1 + start .. (the fixed rows stay zero)
-    CBX_CUDA(cudaMemcpy2DAsync(m.em_B.p + (size_t)(1 + start) * dim + p, dim * sizeof(double), Zb.data(),
-                               q * sizeof(double), q * sizeof(double), size, cudaMemcpyHostToDevice, s));
-    CBX_CUDA(cudaStreamSynchronize(s));
-    for (int j = 0; j < size; ++j) m.probe_have[start + j] = 1;
-  };
 
   // the probe group starting at `done`: batches solved before the next check
   struct Group {
@@ -320,28 +414,8 @@ static void em_iteration(cbx_handle* h, const RemlConfigI& cfg, double& vu, doub
       next += sz;
     } while (next < min_s && next < max_s);
     g.k = next - done;
-    for (auto& bt : g.batches) ensure_batch(bt.first, bt.second);
+    for (auto& bt : g.batches) probe_batch(h, m, cfg.seed, bt.first, bt.second);
     return g;
-  };
-  // The probe stream restarts at the same seed every REML iteration, so the
-  // previous iteration's solutions of these probes are a warm start, and in
-  // mixed precision their residuals carry to the new lambda.
-  auto probes_warm = [&](int done, int k) { return (int)m.probe_lam.size() >= done + k; };
-  auto probes_carry = [&](int done, int k) {
-    bool ok = probes_warm(done, k);
-    if (ok)
-      for (int c = done; c < done + k; ++c) ok = ok && m.probe_r_ok[c] && m.probe_lam[c] == m.probe_lam[done];
-    return ok;
-  };
-  auto record_probes = [&](int done, int k) {
-    if ((int)m.probe_lam.size() < done + k) {
-      m.probe_lam.resize(done + k);
-      m.probe_r_ok.resize(done + k);
-    }
-    for (int c = done; c < done + k; ++c) {
-      m.probe_lam[c] = lam;
-      m.probe_r_ok[c] = mixed;
-    }
   };
   auto count = [&](const PcgResult& pr, int c0, int k, const char* what) {
     for (int c = c0; c < c0 + k; ++c) {
@@ -352,16 +426,15 @@ static void em_iteration(cbx_handle* h, const RemlConfigI& cfg, double& vu, doub
 
   int done = 0;
   Group g0 = make_group(0);
-  DevBuf<double> X, QW;
   // --- 1. the data solve (with the first probe group in mixed precision)
   const bool data_warm = m.has_last;
-  const bool merge = mixed && data_warm == probes_warm(0, g0.k);
+  const bool merge = mixed && data_warm == probes_warm(m, 0, g0.k);
   if (merge) {
     const int k = g0.k, nc = 1 + k;
+    DevBuf<double> X, R;
     X.resize((size_t)dim * nc);
-    DevBuf<double> R;
     R.resize((size_t)dim * nc);
-    const bool carry = data_warm && m.has_last_resid && probes_carry(0, k) && m.last_lam == m.probe_lam[0];
+    const bool carry = data_warm && m.has_last_resid && probes_carry(m, 0, k) && m.last_lam == m.probe_lam[0];
     if (data_warm) {
       CBX_CUDA(cudaMemcpyAsync(X.p, m.last_solution.p, dim * sizeof(double), cudaMemcpyDeviceToDevice, s));
       CBX_CUDA(cudaMemcpyAsync(X.p + dim, m.probe_x.p, (size_t)dim * k * sizeof(double), cudaMemcpyDeviceToDevice,
@@ -386,7 +459,7 @@ static void em_iteration(cbx_handle* h, const RemlConfigI& cfg, double& vu, doub
     CBX_CUDA(cudaMemcpyAsync(m.last_resid.p, R.p, dim * sizeof(double), cudaMemcpyDeviceToDevice, s));
     CBX_CUDA(cudaMemcpyAsync(m.probe_x.p, X.p + dim, (size_t)dim * k * sizeof(double), cudaMemcpyDeviceToDevice, s));
     CBX_CUDA(cudaMemcpyAsync(m.probe_r.p, R.p + dim, (size_t)dim * k * sizeof(double), cudaMemcpyDeviceToDevice, s));
-    record_probes(0, k);
+    probes_record(m, 0, k, lam, mixed);
   } else {
     // data solve alone, warm-started from the previous data solution (and, in
     // mixed precision, from its residual carried to the new lambda)
@@ -419,54 +492,21 @@ static void em_iteration(cbx_handle* h, const RemlConfigI& cfg, double& vu, doub
   double tsum = 0, tsq = 0;
   bool stop = false;
   bool first = true;
+  int solved = 0;
   while (done < max_s && !stop) {
     Group g = first ? std::move(g0) : make_group(done);
     const int k = g.k;
-    // B / X / residual columns of this group (dim x k each)
-    const double *Bg, *Xg, *Rg;
-    DevBuf<double> Xp;
-    if (first && merge) {
-      Bg = m.em_B.p + dim;
-      Xg = m.probe_x.p;
-      Rg = m.probe_r.p;
-    } else {
-      Xp.resize((size_t)dim * k);
-      const bool warm = probes_warm(done, k), carry = probes_carry(done, k);
-      if (warm)
-        CBX_CUDA(cudaMemcpyAsync(Xp.p, m.probe_x.p + (size_t)done * dim, (size_t)dim * k * sizeof(double),
-                                 cudaMemcpyDeviceToDevice, s));
-      ResidCarry pc;
-      pc.r_prev = carry ? m.probe_r.p + (size_t)done * dim : nullptr;
-      pc.dlam = carry ? lam - m.probe_lam[done] : 0.0;
-      pc.r_out = m.probe_r.p + (size_t)done * dim;
+    if (!(first && merge)) {
       PcgResult pr;
-      pcg_solve(h, lam, k, m.em_B.p + (size_t)(1 + done) * dim, Xp.p, warm, cfg.pcg_tol, cfg.pcg_max_iter, 0,
-                cfg.precision, pr, &pc);
+      probe_solve(h, m, lam, done, k, cfg.precision, cfg.pcg_tol, cfg.pcg_max_iter, pr);
       if (h->trace_on) h->trace_mark("#em: probe solve");
-      CBX_CUDA(cudaMemcpyAsync(m.probe_x.p + (size_t)done * dim, Xp.p, (size_t)dim * k * sizeof(double),
-                               cudaMemcpyDeviceToDevice, s));
-      record_probes(done, k);
       count(pr, 0, k, "non-finite probe solve");
       info.matvecs += pr.matvecs;
-      Bg = m.em_B.p + (size_t)(1 + done) * dim;
-      Xg = Xp.p;
-      Rg = m.probe_r.p + (size_t)done * dim;
     }
     first = false;
-    // Qinv C^uu z for each probe: from the solutions and their true residuals
-    // in mixed precision, else the product with the u rows (strided by dim)
-    QW.resize((size_t)q * k);
-    if (mixed) {
-      qinv_from_solution(h, lam, k, Bg, Xg, Rg, QW.p);
-    } else {
-      DevBuf<double> Wu;
-      Wu.resize((size_t)q * k);
-      CBX_CUDA(cudaMemcpy2DAsync(Wu.p, q * sizeof(double), Xg + p, dim * sizeof(double), q * sizeof(double), k,
-                                 cudaMemcpyDeviceToDevice, s));
-      qinv_apply(h, k, Wu.p, QW.p);
-    }
-    // z' Qinv C^uu z per probe (the u rows of the probe columns are z)
-    const std::vector<double> zv = coldots(h, Bg + p, dim, QW.p, q, q, k);
+    probe_values(h, m, lam, done, k, mixed);
+    solved = done + k;
+    const std::vector<double> zv = d2h(h, m.probe_zv.p + done, k);
     int col = 0;
     for (auto& bt : g.batches) {
       double bs = 0, bq = 0;
@@ -501,6 +541,47 @@ static void em_iteration(cbx_handle* h, const RemlConfigI& cfg, double& vu, doub
   info.uQu = uQu;
   info.var_u = vu;
   info.var_e = ve;
+  Mme::Forward& f = m.fwd;
+  f.vu = start_vu;
+  f.ve = start_ve;
+  f.pcg_tol = cfg.pcg_tol;
+  f.precision = cfg.precision;
+  f.seed = cfg.seed;
+  f.solved = solved;
+  f.uQu = uQu;
+  f.e_sse = e_sse;
+  f.valid = true;
+}
+
+// ---------------------------------------------------------------------------
+// The REML score from the forward terms, on the device.  tr = scale * (the sum
+// of the per-probe values z' Qinv C^uu z, fixed order); scale = 1 / nprobe for
+// Hutchinson probes, 1 for the q unit vectors.  Then (vce.cpp:2648-2675)
+//   grad_u = (u'Qinv u + var_e tr - q var_u) / (2 var_u^2)
+//   grad_e = (e'e - var_e (n - p - q + min(lambda tr, q - 1e-6))) / (2 var_e^2)
+// out = {grad_u, grad_e, tr}.
+__global__ void __launch_bounds__(256) k_reml_score(const double* __restrict__ zv, int64_t count, double scale,
+                                                    double uQu, double e_sse, double vu, double ve, int64_t n,
+                                                    int64_t p, int64_t q, double* __restrict__ out) {
+  __shared__ double red[256];
+  const int tid = threadIdx.x;
+  double a = 0.0;
+  for (int64_t i = tid; i < count; i += 256) a += zv[i];
+  red[tid] = a;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (tid < o) red[tid] += red[tid + o];
+    __syncthreads();
+  }
+  if (tid == 0) {
+    const double tr = red[0] * scale;
+    const double lam = ve / fmax(vu, 1e-9);
+    double lambda_tr = lam * tr;
+    if (lambda_tr > (double)q - 1e-6) lambda_tr = (double)q - 1e-6;  // as the reference (vce.cpp:2662)
+    out[0] = 0.5 * (uQu + tr * ve - (double)q * vu) / (vu * vu);
+    out[1] = 0.5 * (e_sse - ve * ((double)(n - p - q) + lambda_tr)) / (ve * ve);
+    out[2] = tr;
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -509,96 +590,132 @@ static void em_iteration(cbx_handle* h, const RemlConfigI& cfg, double& vu, doub
 //   d logL / d var_u = (u'Qinv u + var_e tr - q var_u) / (2 var_u^2)
 //   d logL / d var_e = (e'e - var_e (n - p - q + lambda tr)) / (2 var_e^2)
 // with tr = tr(Qinv C^uu) estimated from `nprobe` Rademacher probes (the
-// reference's probe stream, batches of 16 seeded seed + done) solved as
+// reference's probe stream, batches of 16 seeded seed + first index) solved as
 // multi-RHS blocks, or exactly from the q unit vectors (exact != 0).
+//
+// Backward pass over the forward state: when the handle's last EM iteration
+// (or gradient) ran at this very point with the same probe seed, precision and
+// tolerance, its data-solve terms and the values of the probes it solved are
+// reused, and only probes beyond those are solved.  Those start from their
+// stored solutions of the previous call, with their true residuals carried to
+// the new lambda in mixed precision.  A gradient right after an EM iteration
+// with nprobe no larger than the iteration's probe count costs no solve.
 static void reml_gradient(cbx_handle* h, double vu, double ve, int nprobe, int seed, int exact, int precision,
                           double pcg_tol, int pcg_maxit, double* grad, double* trace_out, int64_t* iters_out) {
   Mme& m = *h->mme;
   cudaStream_t s = h->stream;
   const int64_t p = m.p, q = m.q, dim = m.dim, n = m.n_rec;
   const double lam = ve / std::max(vu, 1e-9);
-  int64_t iters = 0;
-  DevBuf<double> sol;
-  sol.resize(dim);
-  PcgResult r;
-  // mixed precision returns the true residual, from which Qinv u follows
-  // without a dense product (qinv_from_solution)
-  DevBuf<double> res;
-  ResidCarry rc;
-  if (precision != 0) {
-    res.resize(dim);
-    rc.r_out = res.p;
-  }
-  pcg_solve(h, lam, 1, m.rhs.p, sol.p, false, pcg_tol, pcg_maxit, 0, precision, r, &rc);
-  iters += r.iters[0];
-  const double e_sse = record_residual(h, sol.p, nullptr);
-  DevBuf<double> Qu;
-  Qu.resize(q);
-  if (precision != 0)
-    qinv_from_solution(h, lam, 1, m.rhs.p, sol.p, res.p, Qu.p);
-  else
-    qinv_apply(h, 1, sol.p + p, Qu.p);
-  const double uQu = dot_h(d2h(h, sol.p + p, q), d2h(h, Qu.p, q));
+  const bool mixed = precision != 0;
   const int64_t total = exact ? q : nprobe;
   CBX_REQUIRE(total > 0, CBX_ERR_ARG, "nprobe must be positive");
-  double tsum = 0.0;
-  // mixed precision reads the FP32 block once per iteration for up to 64
-  // columns; the FP64 product is FP64-bound, so 32 there
-  const int64_t blk = precision != 0 ? 64 : 32;
-  // probe generator state: the reference's batches of 16 from mt19937_64(seed + done)
-  std::mt19937_64 gen;
-  std::uniform_int_distribution<int> dist(0, 1);
-  for (int64_t c0 = 0; c0 < total; c0 += blk) {
-    const int k = (int)std::min<int64_t>(blk, total - c0);
-    std::vector<double> Bh((size_t)dim * k, 0.0), Z((size_t)q * k, 0.0);
-    for (int j = 0; j < k; ++j) {
-      const int64_t idx = c0 + j;
-      if (exact) {
-        Z[(size_t)j * q + idx] = 1.0;
-        Bh[(size_t)j * dim + p + idx] = 1.0;
-      } else {
-        if (idx % 16 == 0) gen.seed((unsigned long)(seed + idx));
-        for (int64_t i = 0; i < q; ++i) {
-          const double z = dist(gen) == 0 ? -1.0 : 1.0;
-          Z[(size_t)j * q + i] = z;
-          Bh[(size_t)j * dim + p + i] = z;
-        }
-      }
-    }
-    DevBuf<double> B, X, Wu, QW, R;
-    B.resize((size_t)dim * k);
-    X.resize((size_t)dim * k);
-    QW.resize((size_t)q * k);
-    CBX_CUDA(cudaMemcpyAsync(B.p, Bh.data(), Bh.size() * sizeof(double), cudaMemcpyHostToDevice, s));
-    PcgResult pr;
-    ResidCarry pc;
-    if (precision != 0) {
-      R.resize((size_t)dim * k);
-      pc.r_out = R.p;
-    }
-    pcg_solve(h, lam, k, B.p, X.p, false, pcg_tol, pcg_maxit, 0, precision, pr, &pc);
-    for (int c = 0; c < k; ++c) iters += pr.iters[c];
-    if (precision != 0) {
-      qinv_from_solution(h, lam, k, B.p, X.p, R.p, QW.p);
-    } else {
-      Wu.resize((size_t)q * k);
-      CBX_CUDA(cudaMemcpy2DAsync(Wu.p, q * sizeof(double), X.p + p, dim * sizeof(double), q * sizeof(double), k,
-                                 cudaMemcpyDeviceToDevice, s));
-      qinv_apply(h, k, Wu.p, QW.p);
-    }
-    const auto QWh = d2h(h, QW.p, (size_t)q * k);
-    for (int j = 0; j < k; ++j) {
-      double v = 0;
-      for (int64_t i = 0; i < q; ++i) v += Z[(size_t)j * q + i] * QWh[(size_t)j * q + i];
-      tsum += v;
-    }
+  int64_t iters = 0;
+  Mme::Forward& f = m.fwd;
+  const bool reuse = f.valid && f.vu == vu && f.ve == ve && f.precision == precision && f.pcg_tol == pcg_tol;
+  double uQu, e_sse;
+  if (reuse) {
+    uQu = f.uQu;
+    e_sse = f.e_sse;
+  } else {
+    // the data solve, warm-started from the last data solution (its residual
+    // carried to this lambda in mixed precision)
+    f.valid = false;
+    m.last_solution.resize(dim);
+    m.last_resid.resize(dim);
+    PcgResult r;
+    ResidCarry dc;
+    dc.r_prev = (m.has_last && m.has_last_resid) ? m.last_resid.p : nullptr;
+    dc.dlam = lam - m.last_lam;
+    dc.r_out = m.last_resid.p;
+    pcg_solve(h, lam, 1, m.rhs.p, m.last_solution.p, m.has_last, pcg_tol, pcg_maxit, 0, precision, r, &dc);
+    CBX_REQUIRE(r.status[0] != sv::COL_NONFINITE, CBX_ERR_NONFINITE, "non-finite data solve");
+    iters += r.iters[0];
+    m.has_last = true;
+    m.has_last_resid = mixed;
+    m.last_lam = lam;
+    e_sse = record_residual(h, m.last_solution.p, nullptr);
+    DevBuf<double> Qu;
+    Qu.resize(q);
+    if (mixed)
+      qinv_from_solution(h, lam, 1, m.rhs.p, m.last_solution.p, m.last_resid.p, Qu.p);
+    else
+      qinv_apply(h, 1, m.last_solution.p + p, Qu.p);
+    uQu = coldots(h, m.last_solution.p + p, q, Qu.p, q, q, 1)[0];
   }
-  const double tr = exact ? tsum : tsum / (double)total;
-  double lambda_tr = lam * tr;
-  if (lambda_tr > q - 1e-6) lambda_tr = q - 1e-6;  // as the reference (vce.cpp:2662)
-  grad[0] = 0.5 * (uQu + tr * ve - (double)q * vu) / (vu * vu);
-  grad[1] = 0.5 * (e_sse - ve * ((double)(n - p - q) + lambda_tr)) / (ve * ve);
-  if (trace_out) *trace_out = tr;
+  DevBuf<double> zv_exact, out;
+  out.resize(3);
+  const double* zv = nullptr;
+  if (exact) {
+    // the q unit vectors, cold, in blocks (64 columns in mixed precision, whose
+    // PCG bulk reads the FP32 block once per iteration for all of them; the
+    // FP64 product is FP64-bound, so 32 there)
+    const int64_t blk = mixed ? 64 : 32;
+    zv_exact.resize(q);
+    for (int64_t c0 = 0; c0 < q; c0 += blk) {
+      const int k = (int)std::min<int64_t>(blk, q - c0);
+      std::vector<double> Bh((size_t)dim * k, 0.0);
+      for (int j = 0; j < k; ++j) Bh[(size_t)j * dim + p + c0 + j] = 1.0;
+      DevBuf<double> B, X, QW, R;
+      B.resize((size_t)dim * k);
+      X.resize((size_t)dim * k);
+      QW.resize((size_t)q * k);
+      CBX_CUDA(cudaMemcpyAsync(B.p, Bh.data(), Bh.size() * sizeof(double), cudaMemcpyHostToDevice, s));
+      PcgResult pr;
+      ResidCarry pc;
+      if (mixed) {
+        R.resize((size_t)dim * k);
+        pc.r_out = R.p;
+      }
+      pcg_solve(h, lam, k, B.p, X.p, false, pcg_tol, pcg_maxit, 0, precision, pr, &pc);
+      for (int c = 0; c < k; ++c) iters += pr.iters[c];
+      if (mixed) {
+        qinv_from_solution(h, lam, k, B.p, X.p, R.p, QW.p);
+      } else {
+        DevBuf<double> Wu;
+        Wu.resize((size_t)q * k);
+        CBX_CUDA(cudaMemcpy2DAsync(Wu.p, q * sizeof(double), X.p + p, dim * sizeof(double), q * sizeof(double), k,
+                                   cudaMemcpyDeviceToDevice, s));
+        qinv_apply(h, k, Wu.p, QW.p);
+      }
+      k_coldot<<<k, 256, 0, s>>>(B.p + p, dim, QW.p, q, q, zv_exact.p + c0);
+      h->launched("k_coldot");
+      CBX_CUDA(cudaStreamSynchronize(s));  // B and Bh are released at the end of this block
+    }
+    zv = zv_exact.p;
+  } else {
+    probe_store(h, m, seed, std::max(nprobe, m.probe_cap));
+    const int prev = (reuse && f.seed == seed) ? f.solved : 0;
+    const int have = std::min(prev, nprobe);
+    // blocks of 64 columns in mixed precision, 32 in FP64 (as above), on
+    // 16-probe batch boundaries
+    const int blk = mixed ? 64 : 32;
+    for (int c0 = have; c0 < nprobe;) {
+      const int k = std::min(blk - (c0 % 16), nprobe - c0);
+      for (int b = c0 - c0 % 16; b < c0 + k; b += 16) probe_batch(h, m, seed, b, std::min(16, m.probe_cap - b));
+      PcgResult pr;
+      probe_solve(h, m, lam, c0, k, precision, pcg_tol, pcg_maxit, pr);
+      for (int c = 0; c < k; ++c) iters += pr.iters[c];
+      probe_values(h, m, lam, c0, k, mixed);
+      c0 += k;
+    }
+    zv = m.probe_zv.p;
+    // this call's solves are now the forward state at (vu, ve)
+    f.vu = vu;
+    f.ve = ve;
+    f.pcg_tol = pcg_tol;
+    f.precision = precision;
+    f.seed = seed;
+    f.solved = std::max(prev, nprobe);
+    f.uQu = uQu;
+    f.e_sse = e_sse;
+    f.valid = true;
+  }
+  k_reml_score<<<1, 256, 0, s>>>(zv, total, exact ? 1.0 : 1.0 / (double)total, uQu, e_sse, vu, ve, n, p, q, out.p);
+  h->launched("k_reml_score");
+  const std::vector<double> o = d2h(h, out.p, 3);
+  grad[0] = o[0];
+  grad[1] = o[1];
+  if (trace_out) *trace_out = o[2];
   if (iters_out) *iters_out = iters;
 }
 

@@ -71,8 +71,49 @@ __global__ void __launch_bounds__(128, 1) k_umma_probe(const float* A, const flo
   if (warp == 0) tmem_dealloc(tm, 32);
 }
 
+// The bounded mbarrier wait of the pipelined kernels, on a barrier that no
+// thread ever arrives at: every thread's wait gives up after limit_ns and
+// thread 0 records DEV_TIMEOUT in the status word.  Nothing else is in flight
+// (no TMA copy, no MMA, no TMEM), so the kernel returns normally and the
+// context stays usable.
+__global__ void k_wait_probe(int* status, uint64_t limit_ns) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  volatile int abort_flag = 0;
+  const bool ok = mbar_wait_for(&bar, 0, &abort_flag, limit_ns);
+  if (__syncthreads_count(ok ? 0 : 1) > 0 && threadIdx.x == 0) atomicExch(status, DEV_TIMEOUT);
+}
+
 }  // namespace selftest
 }  // namespace cbx
+
+// Runs k_wait_probe with the given limit (1 us .. 1 s) and returns its status:
+// CBX_ERR_TIMEOUT when the wait gave up, as every bounded wait of the library
+// reports it.  *elapsed_ms receives the kernel's run time.
+extern "C" int cbx_selftest_wait_timeout(cbx_handle* h, int64_t limit_ns, double* elapsed_ms) {
+  return cbx_guard(h, [&] {
+    CBX_REQUIRE(limit_ns >= 1000 && limit_ns <= 1000000000, CBX_ERR_ARG, "limit must be 1 us .. 1 s");
+    CBX_CUDA(cudaSetDevice(h->device));
+    cudaEvent_t a, b;
+    CBX_CUDA(cudaEventCreate(&a));
+    CBX_CUDA(cudaEventCreate(&b));
+    CBX_CUDA(cudaEventRecord(a, h->stream));
+    cbx::selftest::k_wait_probe<<<1, 128, 0, h->stream>>>(h->status.p, (uint64_t)limit_ns);
+    h->launched("k_wait_probe");
+    CBX_CUDA(cudaEventRecord(b, h->stream));
+    CBX_CUDA(cudaEventSynchronize(b));
+    float ms = 0;
+    CBX_CUDA(cudaEventElapsedTime(&ms, a, b));
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    if (elapsed_ms) *elapsed_ms = ms;
+    h->check_status("k_wait_probe");
+  });
+}
 
 extern "C" int cbx_selftest_umma(cbx_handle* h, const float* A, const float* B, float* D) {
   return cbx_guard(h, [&] {

@@ -142,6 +142,77 @@ def simulate_pedigree(n_gen: int, per_gen: int, n_sires: int, n_dams: int, seed:
     return sire, dam
 
 
+def simulate_bed_gene_drop(sire: np.ndarray, dam: np.ndarray, per_gen: int, m: int, seed: int,
+                           p_lo: float = 0.01, miss: float = 0.02, chunk: int = 4096,
+                           threads: int | None = None) -> tuple[bytes, np.ndarray]:
+    """Genotypes of a pedigree's last generation by gene dropping.
+
+    The pedigree lists ``per_gen`` animals per discrete generation, founders
+    first, every known parent in the previous generation (simulate_pedigree).
+    Per SNP a base frequency p ~ U(p_lo, 0.5) of the counted allele; founder
+    haplotypes and the haplotype passed by an unknown parent are drawn from
+    it, and each known parent passes one of its two alleles with probability
+    1/2, independently per SNP (no linkage).  Only the last generation is
+    kept; each of its calls is then set missing with probability ``miss``.
+    Returns (bed_bytes, p) with samples in pedigree order.  Chunks of SNPs are
+    independent (child seeds of ``seed``) and run in parallel threads, so the
+    result depends only on the arguments."""
+    import concurrent.futures as cf
+    import os
+    sire = np.asarray(sire, dtype=np.int64)
+    dam = np.asarray(dam, dtype=np.int64)
+    n_all = sire.size
+    n_gen = n_all // per_gen
+    assert n_gen * per_gen == n_all, "pedigree size must be a whole number of generations"
+    for gen in range(1, n_gen):
+        lo, prev = gen * per_gen, (gen - 1) * per_gen
+        for par in (sire[lo:lo + per_gen], dam[lo:lo + per_gen]):
+            k = par[par >= 0]
+            assert np.all((k >= prev) & (k < lo)), "parents must come from the previous generation"
+    ss = np.random.SeedSequence(seed)
+    p_seed, *chunk_seeds = ss.spawn(1 + (m + chunk - 1) // chunk)
+    p = np.random.default_rng(p_seed).uniform(p_lo, 0.5, size=m)
+    tmiss = np.uint16(round(miss * 65536))
+
+    def drop(arg):
+        cs, j0 = arg
+        k = min(m, j0 + chunk) - j0
+        kb = (k + 7) // 8
+        rng = np.random.default_rng(cs)
+        thr = np.round(p[j0:j0 + k] * 65536.0).astype(np.uint32)
+
+        def fresh(rows):  # haplotypes from the base frequencies, bit-packed per SNP
+            u = rng.integers(0, 65536, size=(rows, k), dtype=np.uint16)
+            return np.packbits(u < thr, axis=1, bitorder="little")
+
+        hA, hB = fresh(per_gen), fresh(per_gen)
+        for gen in range(1, n_gen):
+            lo, prev = gen * per_gen, (gen - 1) * per_gen
+
+            def gamete(par):
+                known = par >= 0
+                idx = np.where(known, par - prev, 0)
+                mask = rng.integers(0, 256, size=(per_gen, kb), dtype=np.uint8)
+                g = (hA[idx] & mask) | (hB[idx] & ~mask)
+                nu = int((~known).sum())
+                if nu:
+                    g[~known] = fresh(nu)
+                return g
+
+            hA, hB = gamete(sire[lo:lo + per_gen]), gamete(dam[lo:lo + per_gen])
+        x = (np.unpackbits(hA, axis=1, count=k, bitorder="little")
+             + np.unpackbits(hB, axis=1, count=k, bitorder="little"))
+        g = np.ascontiguousarray(x.T).astype(np.int8)
+        g[rng.integers(0, 65536, size=(k, per_gen), dtype=np.uint16) < tmiss] = -1
+        return encode_bed(g)[len(BED_MAGIC):]
+
+    starts = list(range(0, m, chunk))
+    threads = threads or min(16, os.cpu_count() or 1)
+    with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+        parts = list(ex.map(drop, zip(chunk_seeds, starts)))
+    return BED_MAGIC + b"".join(parts), p
+
+
 def simulate_mt_records(bed: bytes, n: int, m: int, seed: int, Vg: np.ndarray, Ve: np.ndarray,
                         n_levels: int = 2) -> dict:
     """Multi-trait records y_i = mu + level effect + g_i + e_i (one row per animal).

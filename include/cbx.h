@@ -30,9 +30,11 @@ enum {
   CBX_ERR_CUDA = 2,        /* CUDA runtime / library failure */
   CBX_ERR_FORMAT = 3,      /* malformed input file bytes (bad BED magic, truncated, ...) */
   CBX_ERR_TIMEOUT = 4,     /* a device-side wait gave up (bounded spin) */
-  CBX_ERR_BREAKDOWN = 5,   /* PCG breakdown twice in a row (|p'Ap| < 1e-300) */
+  CBX_ERR_BREAKDOWN = 5,   /* breakdown where the caller cannot continue (PCG itself returns its
+                              iterate, as the reference does) */
   CBX_ERR_NONFINITE = 6,   /* NaN / Inf in inputs or iterates */
-  CBX_ERR_NOTCONV = 7,     /* iteration limit reached without convergence */
+  CBX_ERR_NOTCONV = 7,     /* iteration limit reached where the caller needs convergence (PCG
+                              itself returns its iterate and true residual, as the reference) */
   CBX_ERR_FACTOR = 8,      /* dense factorization failed (not positive definite) */
   CBX_ERR_STATE = 9,       /* call order violated (e.g. solve before upload) */
   CBX_ERR_UNSUPPORTED = 10 /* option the GPU path does not implement */
@@ -158,7 +160,11 @@ int cbx_mme_set_qinv_split(cbx_handle* h, const int64_t* a_ptr, const int32_t* a
  * once a correction d is below 2^-8 of x, updated as r -= A d with a
  * float-float block product (error below that of an FP64 b - A x).
  * iters / relres (length nrhs, may be NULL) receive CG iterations and the
- * final relative residual. */
+ * final relative residual.  As PCGSolver::solve (pcg_solver.h:482-495, 530-534),
+ * neither the iteration limit nor a breakdown (|p'Ap| < 1e-300 again after one
+ * restart from p = z) is an error: the column keeps its last iterate, iters gets
+ * maxit and relres its true residual ||b - A x|| / ||b|| (0 when b = 0).
+ * CBX_ERR_NONFINITE for a NaN / Inf iterate. */
 int cbx_pcg_solve(cbx_handle* h, double lambda, int32_t nrhs, const double* B, double* X,
                   int32_t use_x0, double tol, int32_t maxit, int32_t tol_mode,
                   int32_t precision, int32_t* iters, double* relres);
@@ -358,6 +364,14 @@ int cbx_mt_solve(cbx_handle* h, int64_t n, int32_t t, int64_t p, const double* Y
  * reference's stream: batches of 16 from mt19937_64(seed + done)) solved as
  * multi-RHS blocks (64 columns in mixed precision, 32 in FP64), or computed exactly from the
  * q unit vectors when exact_trace != 0.  precision as cbx_pcg_solve.
+ * The entry is the backward pass of cbx_reml_iterate: when the handle's last EM
+ * iteration (or gradient call) started at exactly (var_u, var_e) with the same seed,
+ * precision and pcg_tol, its data-solve terms and the z'Qinv C^uu z values of the
+ * probes it solved are reused; only probes beyond those are solved, from their stored
+ * solutions of the previous call (true residuals carried to the new lambda in mixed
+ * precision).  Right after an EM iteration with nprobe <= its probe count no solve runs
+ * (*pcg_iters == 0).  Otherwise the data solve starts from the last data solution.
+ * The trace sum and the score are formed on the device.
  * trace / pcg_iters may be NULL. */
 int cbx_reml_gradient(cbx_handle* h, double var_u, double var_e, int32_t nprobe, int32_t seed,
                       int32_t exact_trace, int32_t precision, double pcg_tol, int32_t pcg_maxit,
@@ -368,15 +382,16 @@ int cbx_reml_logl_dense(cbx_handle* h, double var_u, double var_e, double* logL)
 
 /* ---- Dense Qinv product without device allocation -------------------------
  * No counterpart in the reference.  For callers that cannot allocate device
- * memory while they run (code under CUDA stream capture, where cudaMalloc is
- * not allowed; hosts that own the device memory pool; latency-critical loops):
- * Y = Qd X for the dense Qinv of the handle's MME (cbx_mme_set_qinv_dense), X
- * and Y column-major q x nrhs DEVICE arrays.  Every intermediate lives in one
- * static 32 MiB device array (resident on each GPU that loads the library):
- * q is limited to about 65,000 (CBX_ERR_ARG beyond).  The first call on a
- * device resolves that array's address and should come before any stream
- * capture; calls that overlap on the GPU share the array and race.  Runs on the
- * handle's stream; the result equals cbx_qinv_apply's. */
+ * memory while they run (a host framework that owns the whole device memory
+ * pool; latency-critical loops that must not call cudaMalloc / cudaFree, which
+ * may synchronize the device): Y = Qd X for the dense Qinv of the handle's MME
+ * (cbx_mme_set_qinv_dense), X and Y column-major q x nrhs DEVICE arrays.  Every
+ * intermediate lives in one static 32 MiB device array (resident on each GPU
+ * that loads the library until the process exits): q is limited to about 65,000
+ * (CBX_ERR_ARG beyond).  A handle's first call resolves that array's address and
+ * should come before any stream capture; calls that overlap on the GPU share the
+ * array and race.  Runs on the handle's stream; the result agrees within rounding
+ * with cbx_qinv_apply's (the two sum in different orders). */
 int cbx_dense_apply_noalloc(cbx_handle* h, int32_t nrhs, const double* X_dev, double* Y_dev);
 
 #ifdef __cplusplus

@@ -4,6 +4,9 @@
 * when the reference checkout is present, ``oracle/ref_trace`` compiles the
   reference's own rng.h / adaptive_trace_estimator.cpp into
   ``oracle/_ref/libref_trace.so`` (used to pin the restatement).
+
+The checkout is the directory named by the environment variable
+CBX_REFERENCE_SRC, else the read-only mount this recipe was written for.
 """
 from __future__ import annotations
 
@@ -15,7 +18,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "liboracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libref_trace.so")
-REFERENCE = "/root/reference"
+REFERENCE = os.environ.get("CBX_REFERENCE_SRC", "/root/reference")
 
 
 def build() -> str:

@@ -1,6 +1,7 @@
 """Generate ``toy_grm.json``: known answers for the reference's 6 x 4 toy BED.
 
-Run from the repository root: ``python tests/golden/make_toy_golden.py``.
+Run from the repository root: ``python tests/golden/make_toy_golden.py [REFERENCE_DIR]``
+(default: the checkout oracle/build.py uses).
 
 The reference ships ``tests/fixtures/toy_plink/toy.bed`` (6 samples, 4 SNPs,
 SNP-major).  This script reads that file from the reference checkout, checks
@@ -27,7 +28,10 @@ from oracle.plink import decode_bed  # noqa: E402
 from oracle.grm import vanraden_grm, vanraden_grm_exact, xx_counts  # noqa: E402
 from cosmicblup_gb300.synth import encode_bed  # noqa: E402
 
-REF_BED = "/root/reference/tests/fixtures/toy_plink/toy.bed"
+from oracle.build import REFERENCE  # noqa: E402
+
+REF_BED = os.path.join(sys.argv[1] if len(sys.argv) > 1 else REFERENCE, "tests", "fixtures", "toy_plink",
+                       "toy.bed")
 DOCUMENTED = [[0, 1, 2, 0, 1, 2], [1, 1, 0, 2, 2, 1], [2, 2, 1, 0, 1, 0], [0, 1, 2, 1, 0, 2]]
 
 

@@ -82,3 +82,38 @@ def test_hutchinson_gradient_matches_oracle(handle, prob, precision):
     adaptive_trace(prob["n"], lambda z: (probes.append(z.copy()), np.zeros_like(z))[1], 256, 256, 0.0, 42)
     ref = oracle_score(prob["mme"], prob["Gi"], vu, ve, probes=probes)
     np.testing.assert_allclose(res["grad"], ref, rtol=1e-6)
+
+
+@pytest.mark.parametrize("precision", [0, MIXED])
+def test_gradient_after_iteration_reuses_forward_solves(handle, prob, precision):
+    """The gradient right after an EM iteration at the same point takes the
+    iteration's data-solve terms and probe solves (no PCG iteration when it
+    needs no more probes than the iteration solved) and equals the standalone
+    gradient; more probes than the iteration solved cost only the extra ones."""
+    from cosmicblup_gb300 import AIREML, RemlConfig
+    from cosmicblup_gb300.vce import MODE_EM
+    vu, ve = 0.45, 0.55
+    dm = dev(handle, prob)
+    r = AIREML(dm, vu, ve, RemlConfig.default(mode=MODE_EM, precision=precision))
+    k = r.run_iteration()["probes"]
+    g_reuse = reml_gradient(dm, vu, ve, nprobe=k, seed=42, precision=precision)
+    assert g_reuse["pcg_iters"] == 0
+    g_more = reml_gradient(dm, vu, ve, nprobe=96, seed=42, precision=precision)
+    assert g_more["pcg_iters"] > 0
+    again = reml_gradient(dm, vu, ve, nprobe=96, seed=42, precision=precision)
+    assert again["pcg_iters"] == 0 and np.array_equal(again["grad"], g_more["grad"])
+    dm2 = dev(handle, prob)  # a fresh MME: no forward state
+    g_alone = reml_gradient(dm2, vu, ve, nprobe=k, seed=42, precision=precision)
+    assert g_alone["pcg_iters"] > 0
+    # Each score component is a difference of terms of order q / (2 var_u) and
+    # n / (2 var_e) (u'Qinv u + var_e tr against q var_u, and so on): the two
+    # gradients come from different solves to relres 1e-10, so they agree to
+    # 1e-8 of those terms.
+    scale = max(prob["n"] / (2 * vu), prob["n"] / (2 * ve))
+    np.testing.assert_allclose(g_reuse["grad"], g_alone["grad"], rtol=1e-8, atol=1e-8 * scale)
+    g_alone96 = reml_gradient(dm2, vu, ve, nprobe=96, seed=42, precision=precision)
+    np.testing.assert_allclose(g_more["grad"], g_alone96["grad"], rtol=1e-8, atol=1e-8 * scale)
+    probes = []
+    adaptive_trace(prob["n"], lambda z: (probes.append(z.copy()), np.zeros_like(z))[1], 96, 96, 0.0, 42)
+    np.testing.assert_allclose(g_more["grad"], oracle_score(prob["mme"], prob["Gi"], vu, ve, probes=probes),
+                               rtol=1e-6)

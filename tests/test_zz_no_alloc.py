@@ -1,6 +1,7 @@
 """GPU test of cbx_dense_apply_noalloc, the entry point for callers that cannot
-allocate device memory while they run (for example code under CUDA stream
-capture).  It must give the same product as cbx_qinv_apply, which allocates its
+allocate device memory while they run (a host framework that owns the device
+memory pool, a latency-critical loop that must not call cudaMalloc).  Its
+product must agree within rounding with cbx_qinv_apply's, which allocates its
 own buffers, on consecutive calls that reuse its static scratch array.
 
 The file name sorts last so that a stop-at-first-failure run has already run
@@ -28,7 +29,9 @@ def test_noalloc_matches_qinv_apply_twice():
         dm = DeviceMME(h, rec["y"], rec["aid"], rows, p, n)
         dm.set_qinv_dense(Gi)
         rng = np.random.default_rng(79)
-        for k in (5, 40):  # second call: more columns, two passes over the scratch array
+        # calls in a row with every pass width (1, 2, 4, 8, 16, 32 columns; 40 and
+        # 33 take two passes, the second narrower than the first)
+        for k in (5, 40, 1, 2, 3, 12, 33, 5):
             X = rng.normal(size=(n, k))
             ref = dm.qinv_apply(X)
             xd = torch.from_numpy(np.ascontiguousarray(X.T)).to("cuda")  # column-major q x k
