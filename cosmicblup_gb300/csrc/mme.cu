@@ -11,6 +11,7 @@
 //    (src/core/pcg_solver.h:60-128, 436-536) and MatrixFreePCG's absolute stop
 //    (src/core/matrix_free_pcg.h:20-66).
 #include <algorithm>
+#include <cstdio>
 #include <cmath>
 #include <vector>
 #include "handle.h"
@@ -144,14 +145,16 @@ __global__ void k_scale_down(const double* __restrict__ r64, const double* __res
     r32[idx] = sc[c] > 0 ? (float)(r64[idx] / sc[c]) : 0.0f;
   }
 }
-// Dc = s_c * d32 (0 for columns with s_c = 0); x64 += Dc
+// Dc = s_c * (d32 + d32lo) (0 for columns with s_c = 0; d32lo may be null); x64 += Dc
 __global__ void k_correction(double* __restrict__ x64, const float* __restrict__ d32,
-                             const double* __restrict__ sc, int64_t dim, int S, double* __restrict__ dc) {
+                             const float* __restrict__ d32lo, const double* __restrict__ sc, int64_t dim, int S,
+                             double* __restrict__ dc) {
   const int64_t total = dim * S;
   for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
        idx += (int64_t)gridDim.x * blockDim.x) {
     const int c = (int)(idx % S);
-    const double d = sc[c] > 0 ? sc[c] * (double)d32[idx] : 0.0;
+    const double dv = d32lo ? (double)d32[idx] + (double)d32lo[idx] : (double)d32[idx];
+    const double d = sc[c] > 0 ? sc[c] * dv : 0.0;
     dc[idx] = d;
     x64[idx] += d;
   }
@@ -333,13 +336,37 @@ static bool use_fused() { return env_int("CBX_FUSED", 0) != 0; }
 // tolerance, so iterations past 1e-3 are wasted there (measured on GB300 at
 // n = 20,000: 1e-5 -> 11.3, 1e-3 -> 12.9 REML it/s, same number of refinements).
 // Later corrections reach their tolerance.
+// With the float-float iterate (below) the floor is gone and the first inner
+// solve takes the same tolerance as the others.
+static bool use_xff();
+static double inner_tol_min();
 static double first_itol() {
   static double v = [] {
     const char* e = std::getenv("CBX_FIRST_ITOL");
-    const double x = (e && *e) ? std::atof(e) : 1e-3;
-    return (x > 0 && x < 1e-1) ? x : 1e-3;
+    const double def = use_xff() ? inner_tol_min() : 1e-3;
+    const double x = (e && *e) ? std::atof(e) : def;
+    return (x > 0 && x < 1e-1) ? x : def;
   }();
   return v;
+}
+
+// The inner FP32 solve accumulates its iterate (the correction) as a
+// float-float pair unless the environment sets CBX_XFF=0.  An FP32 iterate
+// rounds each entry to 2^-24 of itself; multiplied by the largest eigenvalue of
+// the operator, that rounding is a residual which no inner iteration removes
+// (with an eigen-bent G^-1 it stalled the first correction near 1e-3 of its
+// right-hand side).  The pair costs 8 bytes per entry and a few FP32
+// operations in k_update.
+static bool use_xff() {
+  static int v = env_int("CBX_XFF", 1);
+  return v != 0;
+}
+
+// Diagnostics: the environment CBX_LOG_REFINE=1 prints every refinement step
+// of the mixed solver (inner iterations, worst relative true residual) to stderr.
+static bool log_refine() {
+  static int v = env_int("CBX_LOG_REFINE", 0);
+  return v != 0;
 }
 
 // CUDA graphs for the PCG iteration body (environment CBX_GRAPHS=0 launches
@@ -594,7 +621,7 @@ void matvec(cbx_handle* h, const sv::OpView<T>& op, Workspace<T, S>& w, const T*
 template <typename T, int S>
 void run_pcg(cbx_handle* h, Mme& m, const sv::OpView<T>& op, Workspace<T, S>& w, double lam, const T* B, T* X,
              int ncols, const double* tol_col, int abs_tol, int maxit, bool use_x0, std::vector<sv::Col>& out,
-             int64_t& matvecs) {
+             int64_t& matvecs, T* Xlo = nullptr) {
   cudaStream_t s = h->stream;
   const int64_t n = m.dim * S;
   if (use_x0) {
@@ -603,6 +630,7 @@ void run_pcg(cbx_handle* h, Mme& m, const sv::OpView<T>& op, Workspace<T, S>& w,
   } else {
     CBX_CUDA(cudaMemsetAsync(X, 0, n * sizeof(T), s));
   }
+  if (Xlo) CBX_CUDA(cudaMemsetAsync(Xlo, 0, n * sizeof(T), s));
   sv::k_init_resid<T, S><<<w.nblk_vec, sv::NT, 0, s>>>(op, B, w.Q.p, use_x0 ? 1 : 0, w.R.p, w.Z.p, w.part.p);
   h->launched(sizeof(T) == 4 ? "k_init_resid<f32>" : "k_init_resid<f64>");
   if (m.p > 0) {
@@ -624,7 +652,7 @@ void run_pcg(cbx_handle* h, Mme& m, const sv::OpView<T>& op, Workspace<T, S>& w,
   // FP32: one persistent cooperative kernel per iteration after the dense
   // product (pcg_fused.cuh); CHECK is even, so the direction is back in w.P
   // after every block of CHECK iterations
-  const bool fused = sizeof(T) == 4 && w.nb_fused > 0 && use_fused() && CHECK % 2 == 0;
+  const bool fused = sizeof(T) == 4 && w.nb_fused > 0 && use_fused() && CHECK % 2 == 0 && !Xlo;
   const Mme& mm = m;
   if (fused && op.Qd) {
     sv::k_gather_t<T, S><<<grid_for(S * op.ld, 256, 4 * h->num_sms), 256, 0, s>>>(w.P.p, w.Vt.p, op.p, op.ng, op.ld,
@@ -690,7 +718,7 @@ void run_pcg(cbx_handle* h, Mme& m, const sv::OpView<T>& op, Workspace<T, S>& w,
       matvec<T, S>(h, op, w, w.P.p, w.Q.p, lam, 1, w.P.p, w.pq_part.p, w.active.p, false, ncols);
       sv::k_scalar_alpha<S><<<1, sv::NTS, 0, s>>>(w.col.p, w.pq_part.p, w.nblk_spmv);
       h->launched(sizeof(T) == 4 ? "k_scalar_alpha<f32>" : "k_scalar_alpha<f64>");
-      sv::k_update<T, S><<<w.nblk_vec, sv::NT, 0, s>>>(op, w.col.p, X, w.R.p, w.Z.p, w.P.p, w.Q.p, w.part.p);
+      sv::k_update<T, S><<<w.nblk_vec, sv::NT, 0, s>>>(op, w.col.p, X, Xlo, w.R.p, w.Z.p, w.P.p, w.Q.p, w.part.p);
       h->launched(sizeof(T) == 4 ? "k_update<f32>" : "k_update<f64>");
       if (m.p > 0) {
         sv::k_fixed<T, S><<<(unsigned)m.p, sv::NT, 0, s>>>(op, w.R.p, w.Z.p, w.col.p, w.rz_fix.p);
@@ -764,7 +792,7 @@ struct Solver : public SolverBase {
   Workspace<double, S> w64;
   Workspace<float, S> w32;
   DevBuf<double> dinv64, Bi, Xi, R64, Y64, part, scale, Dc64;
-  DevBuf<float> dinv32, R32, D32;
+  DevBuf<float> dinv32, R32, D32, D32lo;
   double dinv_lam = std::nan("");
 
   void prepare(cbx_handle* h, Mme& m, double lam, bool need32) {
@@ -788,6 +816,7 @@ struct Solver : public SolverBase {
       R32.resize(n);
       D32.resize(n);
       Dc64.resize(n);
+      if (use_xff() && !use_fused()) D32lo.resize(n);
     }
   }
 
@@ -879,8 +908,15 @@ struct Solver : public SolverBase {
     }
     for (auto& b : bn) if (!(b > 0)) b = 1.0;
     std::vector<int> done(ncols, 0);
-    for (int c = 0; c < ncols; ++c)
-      if ((abs_tol ? rn[c] : rn[c] / bn[c]) < tol) done[c] = 1;
+    double worst0 = 0.0;
+    for (int c = 0; c < ncols; ++c) {
+      const double rel = abs_tol ? rn[c] : rn[c] / bn[c];
+      worst0 = std::max(worst0, rel);
+      if (rel < tol) done[c] = 1;
+    }
+    if (log_refine())
+      std::fprintf(stderr, "[cbx refine] S=%d cols=%d start warm=%d carried=%d worst_relres=%.3e\n", S, ncols,
+                   use_x0 ? 1 : 0, (use_x0 && have_r0) ? 1 : 0, worst0);
     for (int outer = 0; outer < 60; ++outer) {
       std::vector<double> sc(S, 0.0), itol(S, 1.0);
       int inner_max = 0;
@@ -896,9 +932,10 @@ struct Solver : public SolverBase {
       k_scale_down<<<grid_for(n, 256, 4 * h->num_sms), 256, 0, s>>>(R64.p, scale.p, m.dim, S, R32.p);
       h->launched("k_scale_down");
       std::vector<sv::Col> cols;
+      float* dlo = (use_xff() && !use_fused()) ? D32lo.p : nullptr;
       run_pcg<float, S>(h, m, op32, w32, lam, R32.p, D32.p, ncols, itol.data(), 0, inner_max, false, cols,
-                        res.matvecs);
-      k_correction<<<grid_for(n, 256, 4 * h->num_sms), 256, 0, s>>>(Xi.p, D32.p, scale.p, m.dim, S, Dc64.p);
+                        res.matvecs, dlo);
+      k_correction<<<grid_for(n, 256, 4 * h->num_sms), 256, 0, s>>>(Xi.p, D32.p, dlo, scale.p, m.dim, S, Dc64.p);
       h->launched("k_correction");
       res.refinements += 1;
       // Residual of the new iterate, with the float-float product of the
@@ -924,14 +961,21 @@ struct Solver : public SolverBase {
       } else {
         rn_new = residual(h, m, op64, lam, res.matvecs, ncols, use_resid_ff());
       }
+      double worst = 0.0;
+      int inner = 0;
       for (int c = 0; c < ncols; ++c) {
         if (sc[c] <= 0) continue;
         res.iters[c] += cols[c].iters;
+        inner = std::max(inner, cols[c].iters);
         const double rel = abs_tol ? rn_new[c] : rn_new[c] / bn[c];
+        worst = std::max(worst, rel);
         if (rel < tol) done[c] = 1;
         else if (!(rn_new[c] < 0.9 * rn[c])) done[c] = 2;  // FP32 refinement stalled
         rn[c] = rn_new[c];
       }
+      if (log_refine())
+        std::fprintf(stderr, "[cbx refine] S=%d cols=%d outer=%d inner_iters=%d recursive=%d worst_relres=%.3e\n",
+                     S, ncols, outer, inner, recursive ? 1 : 0, worst);
     }
     for (int c = 0; c < ncols; ++c) {
       res.relres[c] = abs_tol ? rn[c] : rn[c] / bn[c];
@@ -1307,6 +1351,11 @@ extern "C" int cbx_mme_create(cbx_handle* h, int64_t n_rec, int64_t p, int64_t q
     }
     m->y_host.assign(y, y + n_rec);
     m->yty = yty;
+    m->aid_host.assign(aid, aid + n_rec);
+    m->xp_host = xp;
+    m->xc_host.assign(fx_col, fx_col + nx);
+    m->xv_host.assign(fx_val, fx_val + nx);
+    m->rhs_host = rhs;
     CBX_CUDA(cudaStreamSynchronize(s));
     h->mme = std::move(m);
   });

@@ -62,9 +62,12 @@ struct Mme {
   // block-Jacobi fixed block: (X'X + ridge I)^-1, p x p
   DevBuf<double> A11inv64;
   DevBuf<float> A11inv32;
-  // host copies used by the REML driver
+  // host copies used by the REML driver: records, the fixed-effect design
+  // (CSR per record) and W'y
   std::vector<double> y_host;
   double yty = 0.0;
+  std::vector<int32_t> aid_host, xp_host, xc_host;
+  std::vector<double> xv_host, rhs_host;
   // warm start of the data solve (the reference keeps last_solution)
   DevBuf<double> last_solution;
   bool has_last = false;

@@ -151,12 +151,13 @@ __global__ void __launch_bounds__(NT) k_pcg_iter(FusedArgs<T> a) {
     __syncthreads();
   }
   {
-    double pq[RowLayout<S>::CPL];
-#pragma unroll
-    for (int j = 0; j < RowLayout<S>::CPL; ++j) pq[j] = 0.0;
+    DotAcc<T> pqa[RowLayout<S>::CPL];
     const int64_t nwarps = (int64_t)nb * (NT / 32);
     for (int64_t i = p + (int64_t)b * (NT / 32) + warp; i < dim; i += nwarps)
-      spmv_random_row<T, S>(op, i, a.P, a.Tout, a.tsplit, colsum, a.tshift, a.lam, 1, a.Q, a.P, pq, lane);
+      spmv_random_row<T, S>(op, i, a.P, a.Tout, a.tsplit, colsum, a.tshift, a.lam, 1, a.Q, a.P, pqa, lane);
+    double pq[RowLayout<S>::CPL];
+#pragma unroll
+    for (int j = 0; j < RowLayout<S>::CPL; ++j) pq[j] = pqa[j].value();
     block_sum_row_pq<S>(pq, red, blk);  // blk[c] = this block's random-row p'q
   }
   grid.sync();
@@ -203,7 +204,7 @@ __global__ void __launch_bounds__(NT) k_pcg_iter(FusedArgs<T> a) {
     __syncthreads();
   }
   {
-    double rr = 0, rz = 0;
+    DotAcc<T> arr, arz;
     const int c = tid % S;
     const bool upd = cs[c].active != 0 && !cs[c].skip;
     const T alpha = (T)cs[c].alpha;
@@ -216,16 +217,17 @@ __global__ void __launch_bounds__(NT) k_pcg_iter(FusedArgs<T> a) {
         r -= alpha * a.Q[idx];
         a.R[idx] = r;
       }
-      rr += (double)r * r;
+      arr.add(r, r);
       if (i >= p) {
         T z = a.Z[idx];
         if (upd) {
           z = op.dinv[i - p] * r;
           a.Z[idx] = z;
         }
-        rz += (double)r * z;
+        arz.add(r, z);
       }
     }
+    const double rr = arr.value(), rz = arz.value();
     double t = block_sum_cols<S>(rr, red);
     if (tid < S) a.part[(int64_t)b * 4 * S + 1 * S + tid] = t;
     t = block_sum_cols<S>(rz, red);

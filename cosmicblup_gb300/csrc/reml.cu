@@ -930,10 +930,276 @@ static bool dense_exact_step(cbx_handle* h, double& vu_io, double& ve_io, IterIn
   return false;
 }
 
+// ---------------------------------------------------------------------------
+// Data-driven AI step: run_aireml_step (vce.cpp:2414-2857) for one random
+// component, on the branch where the reference has a direct solver.  The LHS
+// is factored densely on the device (Cholesky), which gives the exact
+// tr(Qinv C^uu) (the reference's Takahashi value), the AI matrix from two extra
+// solves and calc_logL_internal (vce.cpp:3533-3588) for the logL-checked step
+// halving.  Without a factorization the reference cannot check logL and falls
+// back to EM (vce.cpp:2791-2797); so does this step above kAiDenseMax.
+constexpr int64_t kAiDenseMax = 24576;
+
+// Dense q x q Qinv: the sparse part scattered row by row, then the dense block
+// at its genotyped rows (each entry written by one thread).
+__global__ void k_qinv_sparse_scatter(int64_t q, const int32_t* __restrict__ Sptr, const int32_t* __restrict__ Scol,
+                                      const double* __restrict__ Sval, double* __restrict__ Q) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < q; r += (int64_t)gridDim.x * blockDim.x)
+    for (int32_t j = Sptr[r]; j < Sptr[r + 1]; ++j) Q[(int64_t)Scol[j] * q + r] += Sval[j];
+}
+__global__ void k_qinv_dense_scatter(int64_t ng, const double* __restrict__ Qd, int64_t ld,
+                                     const int32_t* __restrict__ gmap, int64_t q, double* __restrict__ Q) {
+  const int64_t total = ng * ng;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t k = idx / ng, l = idx - k * ng;
+    Q[(int64_t)gmap[l] * q + gmap[k]] += Qd[k * ld + l];
+  }
+}
+// partial sums of sum_{i,j < q} Q[j q + i] Ci[(p + j) dim + p + i]: tr(Qinv C^uu)
+__global__ void k_trace_qc(const double* __restrict__ Q, const double* __restrict__ Ci, int64_t q, int64_t p,
+                           int64_t dim, double* __restrict__ part) {
+  __shared__ double red[256];
+  double s = 0.0;
+  const int64_t total = q * q;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t j = idx / q, i = idx - j * q;
+    s += Q[idx] * Ci[(p + j) * dim + p + i];
+  }
+  const double t = sv::block_sum_cols<1>(s, red);
+  if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
+static void dense_qinv(cbx_handle* h, DevBuf<double>& Q) {
+  Mme& m = *h->mme;
+  cudaStream_t s = h->stream;
+  const int64_t q = m.q;
+  Q.resize((size_t)q * q);
+  Q.zero(s);
+  if (m.has_sparse) {
+    k_qinv_sparse_scatter<<<gridn(q, 256, 4 * h->num_sms), 256, 0, s>>>(q, m.Qs64.ptr.p, m.Qs64.col.p, m.Qs64.val.p,
+                                                                       Q.p);
+    h->launched("k_qinv_sparse_scatter");
+  }
+  if (m.has_dense) {
+    k_qinv_dense_scatter<<<gridn(m.ng * m.ng, 256, 8 * h->num_sms), 256, 0, s>>>(m.ng, m.Qd64.p, m.ld, m.gmap.p,
+                                                                                q, Q.p);
+    h->launched("k_qinv_dense_scatter");
+  }
+}
+
+// C = W'W + lam [0 0; 0 Q] (dim x dim) factored in place; false if not PD
+static bool factor_lhs_q(cbx_handle* h, const double* Q, double lam, DevBuf<double>& C) {
+  Mme& m = *h->mme;
+  cudaStream_t s = h->stream;
+  const int64_t dim = m.dim;
+  C.resize((size_t)dim * dim);
+  k_build_lhs<<<gridn(dim * dim, 256, 8 * h->num_sms), 256, 0, s>>>(dim, m.p, m.D64.ptr.p, m.D64.col.p, m.D64.val.p,
+                                                                     Q, m.q, lam, C.p);
+  h->launched("k_build_lhs");
+  k_scatter_csr<<<gridn(dim, 256, 4 * h->num_sms), 256, 0, s>>>(dim, m.D64.ptr.p, m.D64.col.p, m.D64.val.p, C.p);
+  h->launched("k_scatter_csr");
+  return potrf(h, C.p, dim);
+}
+
+// calc_logL_internal: -1/2 (log|C| + (n - p - q) log ve + q log vu + (y'y - sol'W'y) / ve),
+// log|C| from the Cholesky factor; -1e20 when C is not positive definite.  C
+// keeps the factor and sol the data solution.
+static double ai_logl(cbx_handle* h, const double* Q, double vu, double ve, DevBuf<double>& C,
+                      std::vector<double>& sol) {
+  Mme& m = *h->mme;
+  const int64_t n = m.n_rec, p = m.p, q = m.q, dim = m.dim;
+  if (!factor_lhs_q(h, Q, ve / std::max(vu, 1e-9), C)) return -1e20;
+  const double ld = 2.0 * log_diag(h, C.p, dim);
+  if (!std::isfinite(ld)) return -1e20;
+  DevBuf<double> x;
+  x.resize(dim);
+  CBX_CUDA(cudaMemcpyAsync(x.p, m.rhs.p, dim * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+  potrs(h, C.p, dim, x.p, 1);
+  sol = d2h(h, x.p, dim);
+  const double yPy = (m.yty - dot_h(sol, m.rhs_host)) / ve;
+  return -0.5 * (ld + (double)(n - p - q) * std::log(ve) + (double)q * std::log(std::max(vu, 1e-9)) + yPy);
+}
+
+// W'v (mult_transpose_design, mme_builder.cpp:330-388) and W x (mult_design,
+// :390-423) over the host copy of the records, in record order
+static std::vector<double> wt_v(const Mme& m, const std::vector<double>& v) {
+  std::vector<double> out(m.dim, 0.0);
+  for (int64_t i = 0; i < m.n_rec; ++i) {
+    for (int32_t a = m.xp_host[i]; a < m.xp_host[i + 1]; ++a) out[m.xc_host[a]] += m.xv_host[a] * v[i];
+    const int32_t an = m.aid_host[i];
+    if (an > 0 && an <= m.q) out[m.p + an - 1] += v[i];
+  }
+  return out;
+}
+static std::vector<double> w_x(const Mme& m, const std::vector<double>& x) {
+  std::vector<double> out(m.n_rec, 0.0);
+  for (int64_t i = 0; i < m.n_rec; ++i) {
+    double val = 0.0;
+    for (int32_t a = m.xp_host[i]; a < m.xp_host[i + 1]; ++a)
+      if (m.xc_host[a] < m.p) val += m.xv_host[a] * x[m.xc_host[a]];
+    const int32_t an = m.aid_host[i];
+    if (an > 0 && an <= m.q) val += x[m.p + an - 1];
+    out[i] = val;
+  }
+  return out;
+}
+
+// Newton direction AI^-1 grad with the reference's fallbacks (vce.cpp:2697-2737):
+// LLT of the 2x2; if that fails, a gradient-ascent step of 10 % of the variances
+// when |det AI| < 1e-20, else the inverse.
+static void ai_direction(const double AI[2][2], const double g[2], double vu, double ve, double d[2]) {
+  const double l11sq = AI[0][0];
+  const double l11 = l11sq > 0 ? std::sqrt(l11sq) : 0.0;
+  const double l21 = l11 > 0 ? AI[1][0] / l11 : 0.0;
+  const double l22sq = AI[1][1] - l21 * l21;
+  if (l11 > 0 && l22sq > 0) {
+    const double l22 = std::sqrt(l22sq);
+    const double y0 = g[0] / l11, y1 = (g[1] - l21 * y0) / l22;
+    d[1] = y1 / l22;
+    d[0] = (y0 - l21 * d[1]) / l11;
+    return;
+  }
+  const double det = AI[0][0] * AI[1][1] - AI[0][1] * AI[1][0];
+  if (std::abs(det) < 1e-20) {
+    const double mx = std::max(std::abs(g[0]) / vu, std::abs(g[1]) / ve);
+    const double sc = mx > 0 ? 0.1 / mx : 0.0;
+    d[0] = g[0] * sc;
+    d[1] = g[1] * sc;
+    return;
+  }
+  d[0] = (AI[1][1] * g[0] - AI[0][1] * g[1]) / det;
+  d[1] = (-AI[1][0] * g[0] + AI[0][0] * g[1]) / det;
+}
+
+static bool ai_data_step(cbx_handle* h, double& vu_io, double& ve_io, IterInfo& info) {
+  Mme& m = *h->mme;
+  if (m.dim > kAiDenseMax) return false;
+  // guard against non-finite variances entering the step (vce.cpp:2417-2419)
+  if (!std::isfinite(vu_io) || vu_io <= 0.0) vu_io = 1e-6;
+  if (!std::isfinite(ve_io) || ve_io <= 0.0) ve_io = 1e-6;
+  const double vu = vu_io, ve = ve_io;
+  const int64_t n = m.n_rec, p = m.p, q = m.q, dim = m.dim;
+  const double lam = ve / std::max(vu, 1e-9);
+  cudaStream_t s = h->stream;
+  DevBuf<double> Q, C;
+  dense_qinv(h, Q);
+  std::vector<double> sol;
+  const double cur0 = ai_logl(h, Q.p, vu, ve, C, sol);
+  if (cur0 <= -1e20) return false;
+  // data terms: u, e = y - W sol, u'Qinv u
+  const std::vector<double> u(sol.begin() + p, sol.end());
+  const std::vector<double> yhat = w_x(m, sol);
+  std::vector<double> e(n);
+  for (int64_t i = 0; i < n; ++i) e[i] = m.y_host[i] - yhat[i];
+  DevBuf<double> du, dQu;
+  du.resize(q);
+  dQu.resize(q);
+  CBX_CUDA(cudaMemcpyAsync(du.p, u.data(), q * sizeof(double), cudaMemcpyHostToDevice, s));
+  qinv_apply(h, 1, du.p, dQu.p);
+  const double uQu = dot_h(u, d2h(h, dQu.p, q));
+  // exact tr(Qinv C^uu) from C^-1
+  double tr = 0.0;
+  {
+    DevBuf<double> Ci;
+    Ci.resize((size_t)dim * dim);
+    k_build_lhs<<<gridn(dim * dim, 256, 8 * h->num_sms), 256, 0, s>>>(dim, p, m.D64.ptr.p, m.D64.col.p,
+                                                                       m.D64.val.p, Q.p, q, lam, Ci.p);
+    h->launched("k_build_lhs");
+    k_scatter_csr<<<gridn(dim, 256, 4 * h->num_sms), 256, 0, s>>>(dim, m.D64.ptr.p, m.D64.col.p, m.D64.val.p, Ci.p);
+    h->launched("k_scatter_csr");
+    if (!chol_inverse_device(h, Ci.p, dim)) return false;
+    const unsigned g = gridn(q * q, 256, 4 * h->num_sms);
+    DevBuf<double> part;
+    part.resize(g);
+    k_trace_qc<<<g, 256, 0, s>>>(Q.p, Ci.p, q, p, dim, part.p);
+    h->launched("k_trace_qc");
+    for (double v : d2h(h, part.p, g)) tr += v;
+  }
+  // AI_ij = 1/2 v_i' P v_j from two extra solves (vce.cpp:2596-2633):
+  // v_u = Z u / vu, v_e = e / ve; P v = (v - W C^-1 W'v) / ve
+  std::vector<double> vu_v(n, 0.0), ve_v(n);
+  for (int64_t i = 0; i < n; ++i) {
+    const int32_t an = m.aid_host[i];
+    if (an > 0 && an <= q) vu_v[i] = u[an - 1] / vu;
+    ve_v[i] = e[i] / ve;
+  }
+  std::vector<double> rhs2 = wt_v(m, vu_v);
+  {
+    const std::vector<double> r2 = wt_v(m, ve_v);
+    rhs2.insert(rhs2.end(), r2.begin(), r2.end());
+  }
+  DevBuf<double> B2;
+  B2.resize((size_t)dim * 2);
+  CBX_CUDA(cudaMemcpyAsync(B2.p, rhs2.data(), rhs2.size() * sizeof(double), cudaMemcpyHostToDevice, s));
+  potrs(h, C.p, dim, B2.p, 2);
+  const std::vector<double> x2 = d2h(h, B2.p, (size_t)dim * 2);
+  const std::vector<double> xu(x2.begin(), x2.begin() + dim), xe(x2.begin() + dim, x2.end());
+  const std::vector<double> yu = w_x(m, xu), ye = w_x(m, xe);
+  std::vector<double> Pvu(n), Pve(n);
+  for (int64_t i = 0; i < n; ++i) {
+    Pvu[i] = (vu_v[i] - yu[i]) / ve;
+    Pve[i] = (ve_v[i] - ye[i]) / ve;
+  }
+  double AI[2][2];
+  AI[0][0] = 0.5 * dot_h(vu_v, Pvu);
+  AI[1][1] = 0.5 * dot_h(ve_v, Pve);
+  AI[0][1] = AI[1][0] = 0.5 * dot_h(vu_v, Pve);
+  // the EM-consistent score (vce.cpp:2648-2675)
+  double lambda_tr = lam * tr;
+  if (lambda_tr > (double)q - 1e-6) lambda_tr = (double)q - 1e-6;
+  const double grad[2] = {0.5 * (uQu + tr * ve - (double)q * vu) / (vu * vu),
+                          0.5 * (dot_h(e, e) - ve * ((double)(n - p - q) + lambda_tr)) / (ve * ve)};
+  project_spd_2x2(AI);
+  double d[2];
+  ai_direction(AI, grad, vu, ve, d);
+  if (!std::isfinite(d[0]) || !std::isfinite(d[1])) return false;
+  if (std::abs(d[0]) > 100.0 * vu || std::abs(d[1]) > 100.0 * ve) return false;
+  const double cur = std::isfinite(cur0) ? cur0 : -1e18;
+  // at most 15 halvings; a candidate must keep both variances positive, move
+  // neither by more than 5x, and raise logL (vce.cpp:2797-2839)
+  for (int k = 0; k < 15; ++k) {
+    const double vu_n = vu + d[0], ve_n = ve + d[1];
+    if (vu_n <= 0.0 || ve_n <= 0.0 || std::abs(d[0]) > 5.0 * vu || std::abs(d[1]) > 5.0 * ve) {
+      d[0] *= 0.5;
+      d[1] *= 0.5;
+      continue;
+    }
+    DevBuf<double> C2;
+    std::vector<double> sol2;
+    const double nl = ai_logl(h, Q.p, vu_n, ve_n, C2, sol2);
+    if (std::isfinite(nl) && nl > cur) {
+      vu_io = vu_n;
+      ve_io = ve_n;
+      m.last_solution.resize(dim);
+      CBX_CUDA(cudaMemcpyAsync(m.last_solution.p, sol.data(), dim * sizeof(double), cudaMemcpyHostToDevice, s));
+      CBX_CUDA(cudaStreamSynchronize(s));
+      m.has_last = true;
+      m.has_last_resid = false;
+      info.kind = 2;
+      info.logL = nl;
+      info.trace = tr;
+      info.e_sse = dot_h(e, e);
+      info.uQu = uQu;
+      info.var_u = vu_n;
+      info.var_e = ve_n;
+      return true;
+    }
+    d[0] *= 0.5;
+    d[1] *= 0.5;
+  }
+  return false;
+}
+
 static void reml_iterate(cbx_handle* h, const RemlConfigI& cfg, double& vu, double& ve, IterInfo& info) {
   Mme& m = *h->mme;
-  const bool dense = cfg.mode == 2 || (cfg.mode == 0 && m.dim < 5000);
-  if (dense && dense_exact_step(h, vu, ve, info)) return;
+  if (cfg.mode == 3) {
+    if (ai_data_step(h, vu, ve, info)) return;
+  } else {
+    const bool dense = cfg.mode == 2 || (cfg.mode == 0 && m.dim < 5000);
+    if (dense && dense_exact_step(h, vu, ve, info)) return;
+  }
   em_iteration(h, cfg, vu, ve, info);
 }
 

@@ -36,6 +36,29 @@ struct OpView {
   const T* dinv;    // q (Jacobi of the random part)
 };
 
+// Per-thread dot-product accumulator.  The FP64 solver sums in FP64.  The
+// FP32 solver sums its FP32 products with Kahan compensation in FP32: GB300
+// runs FP64 arithmetic at 1/64 of the FP32 rate, so one FP64 multiply-add per
+// vector element made the FP32 vector kernels FP64-bound; the compensated
+// FP32 sum keeps the error of the per-thread sums near one FP32 rounding of
+// the sum, and the block and grid sums stay in FP64.
+template <typename T> struct DotAcc;
+template <> struct DotAcc<double> {
+  double s = 0.0;
+  __device__ __forceinline__ void add(double a, double b) { s += a * b; }
+  __device__ __forceinline__ double value() const { return s; }
+};
+template <> struct DotAcc<float> {
+  float s = 0.0f, c = 0.0f;
+  __device__ __forceinline__ void add(float a, float b) {
+    const float y = fmaf(a, b, -c);
+    const float t = s + y;
+    c = (t - s) - y;
+    s = t;
+  }
+  __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+};
+
 template <typename T> struct Vec16;
 template <> struct Vec16<float> { using type = float4; static constexpr int n = 4; };
 template <> struct Vec16<double> { using type = double2; static constexpr int n = 2; };
@@ -616,29 +639,40 @@ __device__ __forceinline__ void spmv_random_row(const OpView<T>& op, int64_t i, 
                                                 const T* __restrict__ Tout, int tsplit,
                                                 const double* __restrict__ colsum, double tshift, T lam,
                                                 int use_D, T* __restrict__ Y, const T* __restrict__ P,
-                                                double (&pq)[RowLayout<S>::CPL], int lane) {
+                                                DotAcc<T> (&pq)[RowLayout<S>::CPL], int lane) {
   const int64_t p = op.p, u = i - p;
   if constexpr (S > 32) {
     constexpr int CPL = S / 32;
     T acc[CPL], qv[CPL];
 #pragma unroll
     for (int j = 0; j < CPL; ++j) acc[j] = qv[j] = T(0);
-    if (use_D) {
-      for (int32_t e = op.Dptr[i]; e < op.Dptr[i + 1]; ++e) {
-        const T dv = op.Dval[e];
-        const T* xr = X + (int64_t)op.Dcol[e] * S + lane;
+    // entries in batches of 4: all the batch's row loads are issued before its
+    // multiply-adds (same order of additions as one entry at a time)
+    auto rowsum = [&](const int32_t* __restrict__ cidx, const T* __restrict__ val, int32_t e, int32_t e1,
+                      int64_t off, T (&out)[CPL]) {
+      for (; e + 3 < e1; e += 4) {
+        T dv[4], xv[4][CPL];
 #pragma unroll
-        for (int j = 0; j < CPL; ++j) acc[j] += dv * xr[32 * j];
-      }
-    }
-    if (op.Sptr) {
-      for (int32_t e = op.Sptr[u]; e < op.Sptr[u + 1]; ++e) {
-        const T sv = op.Sval[e];
-        const T* xr = X + (p + op.Scol[e]) * S + lane;
+        for (int k = 0; k < 4; ++k) {
+          dv[k] = val[e + k];
+          const T* xr = X + (off + cidx[e + k]) * S + lane;
 #pragma unroll
-        for (int j = 0; j < CPL; ++j) qv[j] += sv * xr[32 * j];
+          for (int j = 0; j < CPL; ++j) xv[k][j] = xr[32 * j];
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+#pragma unroll
+          for (int j = 0; j < CPL; ++j) out[j] += dv[k] * xv[k][j];
       }
-    }
+      for (; e < e1; ++e) {
+        const T dv = val[e];
+        const T* xr = X + (off + cidx[e]) * S + lane;
+#pragma unroll
+        for (int j = 0; j < CPL; ++j) out[j] += dv * xr[32 * j];
+      }
+    };
+    if (use_D) rowsum(op.Dcol, op.Dval, op.Dptr[i], op.Dptr[i + 1], 0, acc);
+    if (op.Sptr) rowsum(op.Scol, op.Sval, op.Sptr[u], op.Sptr[u + 1], p, qv);
     if (op.Qd) {
       const int32_t k = op.ginv[u];
       if (k >= 0) {
@@ -657,7 +691,7 @@ __device__ __forceinline__ void spmv_random_row(const OpView<T>& op, int64_t i, 
     for (int j = 0; j < CPL; ++j) {
       const T yv = acc[j] + lam * qv[j];
       Y[i * S + lane + 32 * j] = yv;
-      if (P) pq[j] += (double)P[i * S + lane + 32 * j] * (double)yv;
+      if (P) pq[j].add(P[i * S + lane + 32 * j], yv);
     }
   } else {
     constexpr int G = 32 / S;
@@ -686,7 +720,7 @@ __device__ __forceinline__ void spmv_random_row(const OpView<T>& op, int64_t i, 
       }
       const T yv = acc + lam * qv;
       Y[i * S + c] = yv;
-      if (P) pq[0] += (double)P[i * S + c] * (double)yv;
+      if (P) pq[0].add(P[i * S + c], yv);
     }
   }
 }
@@ -757,12 +791,13 @@ __global__ void __launch_bounds__(NT) k_spmv(OpView<T> op, const T* __restrict__
     }
   } else {
     // random-effect rows, one warp per row
-    double pqv[RowLayout<S>::CPL];
-#pragma unroll
-    for (int j = 0; j < RowLayout<S>::CPL; ++j) pqv[j] = 0.0;
+    DotAcc<T> pqa[RowLayout<S>::CPL];
     const int64_t nwarps = (int64_t)(gridDim.x - nfix) * (NT / 32);
     for (int64_t i = p + (int64_t)(blockIdx.x - nfix) * (NT / 32) + warp; i < op.dim; i += nwarps)
-      spmv_random_row<T, S>(op, i, X, Tout, tsplit, colsum, tshift, lam, use_D, Y, P, pqv, lane);
+      spmv_random_row<T, S>(op, i, X, Tout, tsplit, colsum, tshift, lam, use_D, Y, P, pqa, lane);
+    double pqv[RowLayout<S>::CPL];
+#pragma unroll
+    for (int j = 0; j < RowLayout<S>::CPL; ++j) pqv[j] = pqa[j].value();
     if (pq_part) {
       __shared__ double blk[S];
       block_sum_row_pq<S>(pqv, red, blk);
@@ -781,7 +816,7 @@ __global__ void __launch_bounds__(NT) k_init_resid(OpView<T> op, const T* __rest
                                                    T* __restrict__ R, T* __restrict__ Z,
                                                    double* __restrict__ part /*[grid][3][S]*/) {
   __shared__ double red[NT];
-  double rr = 0, rz = 0, bb = 0;
+  DotAcc<T> arr, arz, abb;
   const int64_t total = op.dim * S;
   for (int64_t idx = blockIdx.x * (int64_t)NT + threadIdx.x; idx < total;
        idx += (int64_t)gridDim.x * NT) {
@@ -789,14 +824,15 @@ __global__ void __launch_bounds__(NT) k_init_resid(OpView<T> op, const T* __rest
     const T b = B[idx];
     const T r = have_Y ? b - Y[idx] : b;
     R[idx] = r;
-    rr += (double)r * r;
-    bb += (double)b * b;
+    arr.add(r, r);
+    abb.add(b, b);
     if (i >= op.p) {
       const T z = op.dinv[i - op.p] * r;
       Z[idx] = z;
-      rz += (double)r * z;
+      arz.add(r, z);
     }
   }
+  const double rr = arr.value(), rz = arz.value(), bb = abb.value();
   const int c = threadIdx.x % S;
   double t;
   t = block_sum_cols<S>(rr, red);
@@ -831,15 +867,18 @@ __global__ void __launch_bounds__(NT) k_fixed(OpView<T> op, const T* __restrict_
 }
 
 // x += alpha p, r -= alpha q (active, non-skipped columns), z = Jacobi r on random
-// rows; partial sums of r'r and r'z (random rows).
+// rows; partial sums of r'r and r'z (random rows).  With Xlo (FP32 only) the
+// iterate is a float-float pair x = Xs + Xlo: alpha p is formed exactly as a
+// product and its rounding error, and added with a two-sum, so x carries about
+// 48 bits although r, z, p and q stay FP32.
 template <typename T, int S>
 __global__ void __launch_bounds__(NT) k_update(OpView<T> op, const Col* __restrict__ col,
-                                               T* __restrict__ Xs, T* __restrict__ R,
+                                               T* __restrict__ Xs, T* __restrict__ Xlo, T* __restrict__ R,
                                                T* __restrict__ Z, const T* __restrict__ P,
                                                const T* __restrict__ Q,
                                                double* __restrict__ part /*[grid][2][S]*/) {
   __shared__ double red[NT];
-  double rr = 0, rz = 0;
+  DotAcc<T> arr, arz;
   const int c = threadIdx.x % S;
   const bool act = col[c].active != 0;
   const bool upd = act && !col[c].skip;
@@ -850,20 +889,41 @@ __global__ void __launch_bounds__(NT) k_update(OpView<T> op, const Col* __restri
     const int64_t i = idx / S;
     T r = R[idx];
     if (upd) {
-      Xs[idx] += alpha * P[idx];
+      if constexpr (sizeof(T) == 4) {
+        if (Xlo) {
+          // the _rn intrinsics are never contracted into FMAs, which would
+          // break the error-free transformations
+          const float pv = P[idx];
+          const float pr = __fmul_rn(alpha, pv);
+          const float pe = fmaf(alpha, pv, -pr);                   // alpha p = pr + pe exactly
+          const float xh = Xs[idx];
+          const float sh = __fadd_rn(xh, pr);                      // two-sum: xh + pr = sh + se
+          const float bv = __fsub_rn(sh, xh);
+          const float se = __fadd_rn(__fsub_rn(xh, __fsub_rn(sh, bv)), __fsub_rn(pr, bv));
+          const float lo = __fadd_rn(Xlo[idx], __fadd_rn(se, pe));
+          const float nh = __fadd_rn(sh, lo);                      // renormalise the pair
+          Xlo[idx] = __fsub_rn(lo, __fsub_rn(nh, sh));
+          Xs[idx] = nh;
+        } else {
+          Xs[idx] += alpha * P[idx];
+        }
+      } else {
+        Xs[idx] += alpha * P[idx];
+      }
       r -= alpha * Q[idx];
       R[idx] = r;
     }
-    rr += (double)r * r;
+    arr.add(r, r);
     if (i >= op.p) {
       T z = Z[idx];
       if (upd) {
         z = op.dinv[i - op.p] * r;
         Z[idx] = z;
       }
-      rz += (double)r * z;
+      arz.add(r, z);
     }
   }
+  const double rr = arr.value(), rz = arz.value();
   double t = block_sum_cols<S>(rr, red);
   if (threadIdx.x < S) part[((int64_t)blockIdx.x * 2 + 0) * S + c] = t;
   t = block_sum_cols<S>(rz, red);

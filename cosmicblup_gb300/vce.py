@@ -40,7 +40,7 @@ class RemlIterInfo(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
-MODE_AUTO, MODE_EM, MODE_DENSE = 0, 1, 2
+MODE_AUTO, MODE_EM, MODE_DENSE, MODE_AI = 0, 1, 2, 3
 
 
 class AIREML:

@@ -252,16 +252,23 @@ typedef struct cbx_reml_config {
   double pcg_tol;        /* relative residual of every PCG solve */
   int32_t precision;     /* 0: FP64 PCG, 1: FP32 PCG + FP64 refinement */
   int32_t mode;          /* 0: dense exact AI when dim < 5000, else EM + Hutchinson
-                            (run_ai_iteration's choice); 1: EM; 2: dense exact */
+                            (run_ai_iteration's choice); 1: EM; 2: dense exact;
+                            3: data-driven AI (run_aireml_step, src/core/vce.cpp:2414-2857)
+                            with the LHS factored on the device (dim <= 24,576): exact
+                            tr(Qinv C^uu), AI_ij = 1/2 v_i'P v_j from two extra solves,
+                            Newton step with up to 15 logL-checked halvings; EM when the
+                            step fails or no factorization fits, as the reference does
+                            without a direct solver */
   int32_t seed;          /* probe seed (AdaptiveTraceEstimator default 42) */
 } cbx_reml_config;
 
 /* Diagnostics of one REML iteration. */
 typedef struct cbx_reml_iter_info {
-  int32_t kind;          /* 0: EM + Hutchinson, 1: dense exact AI */
+  int32_t kind;          /* 0: EM + Hutchinson, 1: dense exact AI, 2: data-driven AI */
   double var_u, var_e;   /* variances after the iteration */
-  double logL;           /* REML log-likelihood (dense exact step), NaN otherwise */
-  double trace;          /* Hutchinson estimate of tr(Qinv C^uu) (EM), NaN otherwise */
+  double logL;           /* REML log-likelihood (dense exact step; calc_logL_internal at the
+                            accepted point for the data-driven AI step), NaN otherwise */
+  double trace;          /* tr(Qinv C^uu): Hutchinson estimate (EM), exact (data-driven AI) */
   int32_t probes;        /* probe vectors used */
   int64_t pcg_iters;     /* CG iterations over all solves of the iteration */
   int64_t matvecs;       /* operator applications (one matrix read each) */

@@ -129,3 +129,41 @@ def vanraden_grm_exact(bed, n: int, m: int, min_maf=np.float32(0.01), block_size
 def _div_exact(v: int, s2pq: float) -> float:
     """round(v * 2^-58) then divide by s2pq in double, as an FP64 GEMM result would be."""
     return (float(v) * 2.0**-58) / s2pq
+
+
+def grm_tiles_exact(bed, n: int, m: int, tiles, min_maf=np.float32(0.01), block_size: int = 2048) -> dict:
+    """Exact X X^T counts and correctly-rounded G on sample tiles of a large GRM.
+
+    ``tiles`` lists (rows, cols) index arrays.  The SNP statistics (validity,
+    float means, blocked sum 2pq) come from all n samples; the tiles' counts are
+    exact integer sums (float64 products of small integers), and G follows
+    vanraden_grm_exact: Z entries are multiples of 2^-29, summed exactly in
+    16-bit halves, rounded once.  Returns dict(xx=[...], G=[...], sum2pq, n_valid).
+    """
+    geno = decode_bed(bed, n, m)
+    st = snp_stats(geno, min_maf)
+    s2pq = sum_2pq_blocked(st["two_pq"], st["valid"], block_size)
+    gv = geno[st["valid"]]
+    a = (st["mean"][st["valid"]].astype(np.float64) * 2.0**29).astype(np.int64)
+    xx, gg = [], []
+    for rows, cols in tiles:
+        rows, cols = np.asarray(rows), np.asarray(cols)
+        xr = np.where(gv[:, rows] >= 0, gv[:, rows], 0).astype(np.float64)
+        xc = np.where(gv[:, cols] >= 0, gv[:, cols], 0).astype(np.float64)
+        xx.append(np.rint(xr.T @ xc).astype(np.int64))  # exact: every partial sum < 2^53
+
+        def u(idx):
+            g = gv[:, idx].astype(np.int64)
+            return np.where(g >= 0, (g << 29) - a[:, None], 0)
+
+        Ur, Uc = u(rows), u(cols)
+        Ur1, Uc1 = Ur >> 16, Uc >> 16
+        Ur0, Uc0 = Ur - (Ur1 << 16), Uc - (Uc1 << 16)
+        hh, hl, lh, ll = Ur1.T @ Uc1, Ur1.T @ Uc0, Ur0.T @ Uc1, Ur0.T @ Uc0
+        G = np.empty((rows.size, cols.size))
+        for i in range(rows.size):
+            for k in range(cols.size):
+                v = (int(hh[i, k]) << 32) + ((int(hl[i, k]) + int(lh[i, k])) << 16) + int(ll[i, k])
+                G[i, k] = float(v) * 2.0**-58 if s2pq <= 0 else _div_exact(v, s2pq)
+        gg.append(G)
+    return {"xx": xx, "G": gg, "sum2pq": s2pq, "n_valid": int(st["valid"].sum())}

@@ -8,7 +8,11 @@ Restates ``AI_REML`` for one random component with a dense Qinv
   (oracle.rng.adaptive_trace), each MME solve by block-Jacobi PCG warm-started
   from the previous solve's solution (``last_solution``, :1226-1235);
 * ``stabilize_variance`` clamping to [0.1x, 10x] of the previous value (:1379-1389);
-* ``run_dense_exact_step`` (:2949-3195) with ``project_spd_2x2`` (:267-283).
+* ``run_dense_exact_step`` (:2949-3195) with ``project_spd_2x2`` (:267-283);
+* ``ai_data_step``: ``run_aireml_step`` (:2414-2857) on its direct-solver
+  branch, with ``calc_logL_internal`` (:3533-3588);
+* ``SparseEM``: the same EM iteration on a sparse MME (single-step H^-1 of
+  thousands of animals), each system solved directly by sparse LU.
 """
 from __future__ import annotations
 
@@ -167,6 +171,90 @@ class AIREML:
             delta = delta * 0.5
         return False
 
+    # --- data-driven AI step (direct-solver branch) -----------------------------------
+    def logL_internal(self, vu, ve):
+        """calc_logL_internal (vce.cpp:3533-3588): log|C| from the factor of the LHS,
+        -1e20 when it is not positive definite."""
+        m = self.mme
+        n, p, q = m.n, m.p, m.q
+        C = m.lhs(self.Qinv, ve / max(vu, 1e-9))
+        try:
+            L = np.linalg.cholesky(C)
+        except np.linalg.LinAlgError:
+            return -1e20
+        ld = 2.0 * np.log(np.diag(L)).sum()
+        rhs = m.rhs()
+        sol = np.linalg.solve(C, rhs)
+        yPy = (m.y @ m.y - sol @ rhs) / ve
+        return -0.5 * (ld + (n - p - q) * np.log(ve) + q * np.log(max(vu, 1e-9)) + yPy)
+
+    def ai_data_step(self):
+        """run_aireml_step (vce.cpp:2414-2857) with a direct solver: the exact
+        trace tr(Qinv C^uu) (the Takahashi value), AI_ij = 1/2 v_i' P v_j from two
+        extra solves (:2596-2633), the EM-consistent score (:2648-2675),
+        project_spd_2x2, the Newton direction with its fallbacks (:2697-2737),
+        the 100x / 5x step guards and up to 15 logL-checked halvings (:2760-2839).
+        Returns False when the step fails (the caller runs EM)."""
+        m = self.mme
+        n, p, q = m.n, m.p, m.q
+        if not np.isfinite(self.var_u) or self.var_u <= 0:
+            self.var_u = 1e-6
+        if not np.isfinite(self.var_e) or self.var_e <= 0:
+            self.var_e = 1e-6
+        vu, ve = self.var_u, self.var_e
+        lam = ve / max(vu, 1e-9)
+        C = m.lhs(self.Qinv, lam)
+        rhs = m.rhs()
+        sol = np.linalg.solve(C, rhs)
+        u = sol[p:]
+        e = m.y - m.mult_design(sol[:p], u)
+        Ci = np.linalg.inv(C)
+        tr = float(np.sum(self.Qinv * Ci[p:, p:]))
+        v_u = m.Z @ u / vu
+        v_e = e / ve
+
+        def Pv(v):
+            x = np.linalg.solve(C, m.W.T @ v)
+            return (v - m.W @ x) / ve
+
+        Pvu, Pve = Pv(v_u), Pv(v_e)
+        AI = 0.5 * np.array([[v_u @ Pvu, v_u @ Pve], [v_u @ Pve, v_e @ Pve]])
+        ltr = min(lam * tr, q - 1e-6)
+        grad = np.array([0.5 * (u @ (self.Qinv @ u) + tr * ve - q * vu) / vu**2,
+                         0.5 * (e @ e - ve * (n - p - q + ltr)) / ve**2])
+        AI = project_spd_2x2(AI)
+        try:
+            np.linalg.cholesky(AI)
+            delta = np.linalg.solve(AI, grad)
+        except np.linalg.LinAlgError:
+            det = np.linalg.det(AI)
+            if abs(det) < 1e-20:
+                mx = max(abs(grad[0]) / vu, abs(grad[1]) / ve)
+                delta = grad * (0.1 / mx if mx > 0 else 0.0)
+            else:
+                delta = np.linalg.inv(AI) @ grad
+        if not np.all(np.isfinite(delta)):
+            return False
+        if abs(delta[0]) > 100 * vu or abs(delta[1]) > 100 * ve:
+            return False
+        cur = self.logL_internal(vu, ve)
+        if not np.isfinite(cur):
+            cur = -1e18
+        for _ in range(15):
+            vu_n, ve_n = vu + delta[0], ve + delta[1]
+            if vu_n <= 0 or ve_n <= 0 or abs(delta[0]) > 5 * vu or abs(delta[1]) > 5 * ve:
+                delta = delta * 0.5
+                continue
+            new = self.logL_internal(vu_n, ve_n)
+            if np.isfinite(new) and new > cur:
+                self.var_u, self.var_e = vu_n, ve_n
+                self.history.append(("AI(data)", new, vu_n, ve_n))
+                self.last_ai_step = {"trace": tr, "logL": new, "AI": AI, "grad": grad}
+                self.solution = sol
+                return True
+            delta = delta * 0.5
+        return False
+
     # --- outer loop -----------------------------------------------------------------
     def solve(self, dense_exact=None):
         dim = self.mme.dim
@@ -186,3 +274,76 @@ class AIREML:
                 self.converged = True
                 break
         return self.var_u, self.var_e
+
+
+def hinv_sparse(Ainv_csr, Gd, gmap):
+    """H^-1 = A^-1 + S Gd S^T as a scipy CSR matrix (SplitMatrixAdapter's operator,
+    src/core/matrix_adapter.h:252-278, formed explicitly)."""
+    import scipy.sparse as sp
+    ptr, col, val = Ainv_csr
+    q = len(ptr) - 1
+    A = sp.csr_matrix((val, col, ptr), shape=(q, q))
+    g = np.asarray(gmap)
+    r = np.repeat(g, g.size)
+    c = np.tile(g, g.size)
+    D = sp.csr_matrix((np.asarray(Gd).ravel(), (r, c)), shape=(q, q))
+    return (A + D).tocsr()
+
+
+class SparseEM:
+    """EM + Hutchinson REML iterations (vce.cpp:1490-1574) on a sparse MME.
+
+    The same algorithm as AIREML.em_iteration -- data solve, e'e, u'Qinv u, the
+    adaptive trace estimator of tr(Qinv C^uu) with the reference's probe stream
+    (oracle.rng.adaptive_trace), the EM updates and stabilize_variance -- for
+    problems too large for the dense restatement.  Each system is solved
+    directly (scipy sparse LU of W'W + lambda [0 0; 0 Qinv]): the exact value
+    the reference's PCG approximates to relative residual 1e-10.
+    """
+
+    def __init__(self, W, y, Qinv, p, var_u, var_e, mc_samples=100, seed=42):
+        import scipy.sparse as sp
+        self.W = sp.csr_matrix(W)
+        self.y = np.asarray(y, dtype=np.float64)
+        self.Qinv = sp.csr_matrix(Qinv)
+        self.p = int(p)
+        self.q = self.Qinv.shape[0]
+        self.n = self.y.size
+        self.WtW = (self.W.T @ self.W).tocsc()
+        self.rhs = self.W.T @ self.y
+        self.var_u, self.var_e = float(var_u), float(var_e)
+        self.mc_samples, self.seed = mc_samples, seed
+        y = self.y
+        self.y_var = max(1e-12, ((y - y.mean()) ** 2).sum() / (len(y) - 1)) if len(y) > 1 \
+            else max(1e-12, float(y @ y))
+
+    stabilize = AIREML.stabilize
+
+    def lhs(self, lam):
+        import scipy.sparse as sp
+        Z = sp.csr_matrix((self.p, self.p))
+        return (self.WtW + sp.block_diag([Z, lam * self.Qinv])).tocsc()
+
+    def em_iteration(self):
+        from scipy.sparse.linalg import splu
+        p, q, n = self.p, self.q, self.n
+        start_vu, start_ve = self.var_u, self.var_e
+        lam = start_ve / max(start_vu, 1e-9)
+        lu = splu(self.lhs(lam), permc_spec="MMD_AT_PLUS_A")  # symmetric ordering: little fill
+        sol = lu.solve(self.rhs)
+        u = sol[p:]
+        e = self.y - self.W @ sol
+        e_sse = float(e @ e)
+        uQu = float(u @ (self.Qinv @ u))
+        n_samp = max(5, self.mc_samples // 2)
+
+        def op(z):
+            b = np.zeros(p + q)
+            b[p:] = z
+            return self.Qinv @ lu.solve(b)[p:]
+
+        tr, used, _ = adaptive_trace(q, op, max(30, n_samp // 3), max(100, n_samp), 0.05, self.seed)
+        self.var_u = self.stabilize((uQu + tr * start_ve) / q, start_vu)
+        self.var_e = self.stabilize((e_sse + start_ve * ((p + q) - lam * tr)) / n, start_ve)
+        self.solution = sol
+        return {"sol": sol, "e_sse": e_sse, "uQu": uQu, "trace": tr, "samples": used}

@@ -34,11 +34,16 @@ CBX_ERR_TIMEOUT = 4
 def prob():
     n, m = 200, 1500
     bed, _ = simulate_bed(n, m, seed=900, p_lo=0.05, miss=0.01)
-    Gi = invert_psd_matrix(vanraden_grm(bed, n, m)["G"])
+    G = vanraden_grm(bed, n, m)["G"]
+    Gi = invert_psd_matrix(G)
+    # a well-conditioned Qinv for comparing iterates after a few iterations: with
+    # the eigen-bent G^-1 (condition ~1e10) the iterates of two FP64 CG runs that
+    # round differently part after a handful of iterations
+    Qwc = np.linalg.inv(0.8 * G + 0.2 * np.eye(n))
     g = genetic_values(bed, n, m, seed=901, var_a=0.4)
     rec = simulate_gblup_records(n, 3, g, seed=902, var_e=0.6)
     p, rows, _ = build_fixed_design(rec["cats"])
-    return {"n": n, "Gi": Gi, "rec": rec, "p": p, "rows": rows}
+    return {"n": n, "Gi": Gi, "Qwc": Qwc, "rec": rec, "p": p, "rows": rows}
 
 
 def test_bounded_wait_times_out_and_handle_survives(handle, prob):
@@ -64,10 +69,10 @@ def test_bounded_wait_times_out_and_handle_survives(handle, prob):
 def test_iteration_limit_returns_iterate_and_true_residual(handle, prob, precision):
     d = prob
     dm = DeviceMME(handle, d["rec"]["y"], d["rec"]["aid"], d["rows"], d["p"], d["n"])
-    dm.set_qinv_dense(d["Gi"])
+    dm.set_qinv_dense(d["Qwc"])
     om = MME(d["rec"]["y"], d["rec"]["aid"], d["rows"], d["p"], d["n"])
-    A, b = om.lhs(d["Gi"], 1.5), om.rhs()
-    maxit = 15
+    A, b = om.lhs(d["Qwc"], 1.5), om.rhs()
+    maxit = 8
     x, it, rr = dm.pcg_solve(1.5, b, maxit=maxit, precision=precision)  # raises on an error status
     true_rel = np.linalg.norm(b - A @ x) / np.linalg.norm(b)
     assert rr[0] > 1e-10 and abs(rr[0] - true_rel) <= 1e-6 * true_rel
