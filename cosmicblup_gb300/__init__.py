@@ -12,6 +12,7 @@ from .ped import ainv_henderson, ssgblup_qinv  # noqa: F401
 from .mt import MvEigenVce, MvOptions, solve_multi_trait  # noqa: F401
 from .batch import BatchProblem, BatchResult, batch_reml  # noqa: F401
 from .geno import DeviceGenotypes  # noqa: F401
+from .results import write_beta, write_rand, write_vars  # noqa: F401
 
 __all__ = ["CbxError", "Handle", "lib", "GrmBuilder", "GrmOptions", "PlinkReader",
            "bed_snp_counts", "write_matrix_bin", "DeviceMME", "AIREML", "RemlConfig", "final_solve", "invert_psd",

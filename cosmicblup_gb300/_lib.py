@@ -90,6 +90,11 @@ SIGNATURES = [
     ("cbx_tune_reset", C.c_int, []),
     ("cbx_tune_report", C.c_int, [C.c_char_p, C.c_int64]),
     ("cbx_dense_apply_noalloc", C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
+    ("cbx_write_vars", C.c_int, [C.c_char_p, C.c_char_p, C.c_double, C.c_double, C.c_double, C.c_double]),
+    ("cbx_write_beta", C.c_int, [C.c_char_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("cbx_write_rand", C.c_int, [C.c_char_p, C.c_char_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
+                                 C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_void_p,
+                                 C.c_void_p]),
     ("cbx_batch_reml", C.c_int, [C.c_int, C.c_int32, C.c_void_p, C.c_float, C.c_void_p, C.c_int32, C.c_void_p]),
     # diagnostics and self-test exports (not in the public header)
     ("cbx_trace_enable", C.c_int, [C.c_void_p, C.c_int32]),

@@ -125,6 +125,27 @@ int cbx_grm_bed(cbx_handle* h, const uint8_t* bed, int64_t bed_bytes, int64_t n,
 int cbx_write_upper_packed(cbx_handle* h, int32_t which, const char* path);
 int cbx_write_grm_gcta(cbx_handle* h, const char* bin_path, const char* n_path, int64_t n_valid);
 
+/* ---- Text result files -----------------------------------------------------
+ * GSOutput::writeResults (src/solve/result_writer.cpp:64-430) for one genetic
+ * component, tag "GA" (GBLUP), "HA" (ssGBLUP) or "PA" (pedigree); numbers in the
+ * default C++ stream format (6 significant digits), as the reference writes them.
+ * No GPU is involved.
+ *  cbx_write_vars: Item / Var / Var_SE / h2 / h2_SE / h2_Pr(Chisq) rows for the
+ *    component and "e" (h2 SEs by the delta method, Pr = erfc((h2/se)/sqrt 2)).
+ *  cbx_write_beta: Levels / Estimation / SE per fixed-effect column (names[p]);
+ *    beta_se NULL writes "nan".
+ *  cbx_write_rand: ID / tag / residuals / n_obs per animal (q animals, ids[q] or
+ *    NULL for "UNK_<k>"): the mean over its records of u and of y - Xb - u and
+ *    its record count, animals in order of first record, then the others sorted
+ *    by ID with their solution u and "nan" residual.  Records and design as
+ *    cbx_mme_create. */
+int cbx_write_vars(const char* path, const char* tag, double var_u, double se_u, double var_e, double se_e);
+int cbx_write_beta(const char* path, int64_t p, const char* const* names, const double* beta,
+                   const double* beta_se);
+int cbx_write_rand(const char* path, const char* tag, int64_t n_rec, const double* y, const int32_t* aid,
+                   const int64_t* fx_ptr, const int32_t* fx_col, const double* fx_val, int64_t p,
+                   const double* beta, int64_t q, const double* u, const char* const* ids);
+
 /* ---- Mixed-model equations (one random component) ------------------------
  * Replaces MMELHSBuilder::initialize / build_lhs / build_rhs
  * (src/core/mme_builder.cpp:72-387, header src/core/mme_builder.h:26-71).
