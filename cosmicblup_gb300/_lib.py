@@ -67,6 +67,8 @@ SIGNATURES = [
     ("cbx_profile_read", C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int64), C.POINTER(C.c_double),
                                    C.POINTER(C.c_double)]),
     ("cbx_timer_start", C.c_int, [C.c_void_p]),
+    ("cbx_range_push", C.c_int, [C.c_char_p]),
+    ("cbx_range_pop", C.c_int, []),
     ("cbx_timer_stop", C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     ("cbx_ainv_henderson", C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.POINTER(C.c_int64),
                                      C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),

@@ -5,6 +5,7 @@
 #include <map>
 #include "handle.h"
 #include "tune.h"
+#include <nvtx3/nvToolsExt.h>
 
 void cbx_handle::check_status(const char* what) {
   int st = 0;
@@ -116,6 +117,19 @@ int cbx_timer_stop(cbx_handle* h, double* ms) {
     CBX_CUDA(cudaEventElapsedTime(&t, h->timer_a, h->timer_b));
     if (ms) *ms = t;
   });
+}
+
+// Named NVTX ranges on the calling thread (benchmark instrumentation): a
+// profiler can keep only the kernels launched inside one (ncu --nvtx
+// --nvtx-include "<name>/").  NVTX is header-only and does nothing unless a
+// tool is attached.
+int cbx_range_push(const char* name) {
+  nvtxRangePushA(name ? name : "cbx");
+  return CBX_OK;
+}
+int cbx_range_pop(void) {
+  nvtxRangePop();
+  return CBX_OK;
 }
 
 // Launch trace (diagnostics, not in the public header).  cbx_trace_enable(h, 1)

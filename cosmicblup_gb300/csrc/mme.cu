@@ -254,8 +254,10 @@ struct Workspace {
     const int64_t n = m.dim * S;
     R.resize(n); Z.resize(n); P.resize(n); Q.resize(n); X.resize(n);
     if (m.has_dense) { Vt.resize((size_t)S * m.ld); Tout.resize((size_t)m.ng * S * 8); colsum.resize(S); }
-    nblk_vec = (int)grid_for(n, sv::NT, 2 * num_sms);
-    nblk_spmv = (int)m.p + (int)grid_for(m.dim - m.p, 8, 4 * num_sms);
+    // enough warps per SM to keep the loads of these streaming kernels in flight
+    // (2 blocks per SM ran k_update at about a quarter of HBM bandwidth)
+    nblk_vec = (int)grid_for(n, sv::NT, 8 * num_sms);
+    nblk_spmv = (int)m.p + (int)grid_for(m.dim - m.p, 8, 6 * num_sms);
     part.resize((size_t)nblk_vec * 3 * S);
     pq_part.resize((size_t)nblk_spmv * S);
     rz_fix.resize((size_t)std::max<int64_t>(m.p, 1) * S);
@@ -820,18 +822,20 @@ struct Solver : public SolverBase {
     }
   }
 
-  // column norms of an interleaved FP64 block
+  // column norms of an interleaved FP64 block (2 blocks per SM: the partials
+  // come back to the host)
   std::vector<double> norms(cbx_handle* h, Mme& m, const double* V) {
     cudaStream_t s = h->stream;
-    sv::k_colnorm2<S><<<w64.nblk_vec, sv::NT, 0, s>>>(V, m.dim, part.p);
+    const int nb = std::min(w64.nblk_vec, 2 * h->num_sms);
+    sv::k_colnorm2<S><<<nb, sv::NT, 0, s>>>(V, m.dim, part.p);
     h->launched("k_colnorm2");
-    std::vector<double> ph((size_t)w64.nblk_vec * S);
+    std::vector<double> ph((size_t)nb * S);
     CBX_CUDA(cudaMemcpyAsync(ph.data(), part.p, ph.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
     CBX_CUDA(cudaStreamSynchronize(s));
     std::vector<double> r(S, 0.0);
     for (int c = 0; c < S; ++c) {
       double t = 0;
-      for (int b = 0; b < w64.nblk_vec; ++b) t += ph[(size_t)b * S + c];
+      for (int b = 0; b < nb; ++b) t += ph[(size_t)b * S + c];
       r[c] = std::sqrt(t);
     }
     return r;

@@ -57,34 +57,87 @@ __global__ void k_scatter_csr(int64_t dim, const int32_t* __restrict__ Dptr, con
   for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < dim; r += (int64_t)gridDim.x * blockDim.x)
     for (int32_t j = Dptr[r]; j < Dptr[r + 1]; ++j) C[(int64_t)Dcol[j] * dim + r] += Dval[j];
 }
-// W^T dense (dim x n_rec, column-major): column i = record i's design row
-__global__ void k_build_wt(int64_t n_rec, int64_t p, int64_t q, int64_t dim, const int32_t* __restrict__ aid,
-                           const int32_t* __restrict__ xp, const int32_t* __restrict__ xc,
-                           const double* __restrict__ xv, double* __restrict__ Wt) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_rec; i += (int64_t)gridDim.x * blockDim.x) {
-    double* col = Wt + i * dim;
-    for (int32_t j = xp[i]; j < xp[i + 1]; ++j)
-      if (xc[j] < p) col[xc[j]] += xv[j];
-    const int32_t a = aid[i];
-    if (a > 0 && a <= q) col[p + a - 1] += 1.0;
-  }
-}
-// P[i, j] = (delta_ij - (W CinvWt)[i, j]) / ve   (gather over the records' design rows)
-__global__ void k_build_P(int64_t n_rec, int64_t p, int64_t q, int64_t dim, const int32_t* __restrict__ aid,
-                          const int32_t* __restrict__ xp, const int32_t* __restrict__ xc,
-                          const double* __restrict__ xv, const double* __restrict__ CiWt, double ve,
-                          double* __restrict__ P) {
+// P[i, j] = (delta_ij - (W C^-1 W^T)[i, j]) / ve from the explicit C^-1 (dim x
+// dim, column-major, symmetric): a gather over the two records' design rows
+// (their fixed-effect entries and their animal).
+__global__ void k_build_P_ci(int64_t n_rec, int64_t p, int64_t q, int64_t dim, const int32_t* __restrict__ aid,
+                             const int32_t* __restrict__ xp, const int32_t* __restrict__ xc,
+                             const double* __restrict__ xv, const double* __restrict__ Ci, double ve,
+                             double* __restrict__ P) {
   const int64_t total = n_rec * n_rec;
   for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
        idx += (int64_t)gridDim.x * blockDim.x) {
     const int64_t i = idx % n_rec, j = idx / n_rec;
-    const double* cj = CiWt + j * dim;
-    double h = 0.0;
-    for (int32_t k = xp[i]; k < xp[i + 1]; ++k)
-      if (xc[k] < p) h += xv[k] * cj[xc[k]];
-    const int32_t a = aid[i];
-    if (a > 0 && a <= q) h += cj[p + a - 1];
-    P[idx] = ((i == j ? 1.0 : 0.0) - h) / ve;
+    // column (W C^-1)[i, :] restricted to record j's entries: sum_b w_jb (sum_a w_ia Ci[b, a])
+    auto row_i_dot = [&](int64_t b) {
+      const double* cb = Ci + b * dim;
+      double t = 0.0;
+      for (int32_t k = xp[i]; k < xp[i + 1]; ++k)
+        if (xc[k] < p) t += xv[k] * cb[xc[k]];
+      const int32_t a = aid[i];
+      if (a > 0 && a <= q) t += cb[p + a - 1];
+      return t;
+    };
+    double hsum = 0.0;
+    for (int32_t k = xp[j]; k < xp[j + 1]; ++k)
+      if (xc[k] < p) hsum += xv[k] * row_i_dot(xc[k]);
+    const int32_t bj = aid[j];
+    if (bj > 0 && bj <= q) hsum += row_i_dot(p + bj - 1);
+    P[idx] = ((i == j ? 1.0 : 0.0) - hsum) / ve;
+  }
+}
+// C = A B for n x n column-major FP64 matrices: 64 x 64 output tiles per
+// block, 4 x 4 per thread, K in steps of 16 staged in shared memory; every
+// output sums its K terms in index order.  FP64 multiply-add issue bounds it
+// (GB300 runs FP64 at 1/64 of the FP32 rate).
+__global__ void __launch_bounds__(256) k_dgemm_nn(int64_t n, const double* __restrict__ A,
+                                                  const double* __restrict__ B, double* __restrict__ C) {
+  __shared__ double As[16][65];
+  __shared__ double Bs[16][65];
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  const int64_t row0 = (int64_t)blockIdx.x * 64, col0 = (int64_t)blockIdx.y * 64;
+  double acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
+  for (int64_t k0 = 0; k0 < n; k0 += 16) {
+    for (int t = threadIdx.x; t < 1024; t += 256) {
+      const int r = t & 63, kk = t >> 6;
+      As[kk][r] = (row0 + r < n && k0 + kk < n) ? A[(k0 + kk) * n + row0 + r] : 0.0;
+      const int kb = t & 15, c = t >> 4;
+      Bs[kb][c] = (col0 + c < n && k0 + kb < n) ? B[(col0 + c) * n + k0 + kb] : 0.0;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < 16; ++kk) {
+      double a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = As[kk][ty * 4 + i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) b[j] = Bs[kk][tx * 4 + j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int64_t r = row0 + ty * 4 + i, c = col0 + tx * 4 + j;
+      if (r < n && c < n) C[c * n + r] = acc[i][j];
+    }
+}
+// y = A x for an n x n column-major FP64 matrix (one thread per row, K in order)
+__global__ void k_dgemv_n(int64_t n, const double* __restrict__ A, const double* __restrict__ x,
+                          double* __restrict__ y) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    double t = 0.0;
+    for (int64_t k = 0; k < n; ++k) t = fma(A[k * n + r], x[k], t);
+    y[r] = t;
   }
 }
 // ZAZt[i, j] = A[aid_i - 1, aid_j - 1] (0 for records without an animal)
@@ -724,7 +777,7 @@ static void reml_gradient(cbx_handle* h, double vu, double ve, int nprobe, int s
 struct DenseExact {
   bool init = false;
   int64_t n = 0, dim = 0;
-  DevBuf<double> ZAZt, Wt;
+  DevBuf<double> ZAZt;
   double log_det_A = 0;
 };
 static DenseExact& dense_state(cbx_handle* h) {
@@ -760,11 +813,6 @@ static void dense_init(cbx_handle* h, DenseExact& D) {
   D.ZAZt.resize((size_t)n * n);
   k_build_zazt<<<gridn(n * n, 256, 8 * h->num_sms), 256, 0, s>>>(n, q, m.aid.p, A.p, D.ZAZt.p);
   h->launched("k_build_zazt");
-  D.Wt.resize((size_t)dim * n);
-  D.Wt.zero(s);
-  k_build_wt<<<gridn(n, 256, 4 * h->num_sms), 256, 0, s>>>(n, m.p, q, dim, m.aid.p, m.x_ptr.p, m.x_col.p, m.x_val.p,
-                                                            D.Wt.p);
-  h->launched("k_build_wt");
   CBX_CUDA(cudaStreamSynchronize(s));
   D.n = n;
   D.dim = dim;
@@ -845,20 +893,30 @@ static bool dense_exact_step(cbx_handle* h, double& vu_io, double& ve_io, IterIn
   const double cur0 = dense_logL(h, D, vu, ve, C, sol);
   if (cur0 <= -1e18) return false;
   double cur = cur0;
-  // C^-1 W^T, P = (I - W C^-1 W^T) / ve
-  DevBuf<double> CiWt;
-  CiWt.resize((size_t)dim * n);
-  CBX_CUDA(cudaMemcpyAsync(CiWt.p, D.Wt.p, (size_t)dim * n * sizeof(double), cudaMemcpyDeviceToDevice, s));
-  potrs(h, C.p, dim, CiWt.p, n);
+  // P = (I - W C^-1 W^T) / ve from the explicit C^-1 (inverse of the factor),
+  // then M_u = P ZAZ^T: the FP64 products on this library's kernels
+  DevBuf<double> Ci;
+  Ci.resize((size_t)dim * dim);
+  CBX_CUDA(cudaMemcpyAsync(Ci.p, C.p, (size_t)dim * dim * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  {
+    int lw = 0;
+    CBX_SOLVER(cusolverDnDpotri_bufferSize(L.sol, CUBLAS_FILL_MODE_LOWER, (int)dim, Ci.p, (int)dim, &lw));
+    DevBuf<double> work;
+    work.resize(std::max(lw, 1));
+    DevBuf<int> info;
+    info.resize(1);
+    CBX_SOLVER(cusolverDnDpotri(L.sol, CUBLAS_FILL_MODE_LOWER, (int)dim, Ci.p, (int)dim, work.p, lw, info.p));
+    k_symmetrize_lower<<<gridn(dim * dim, 256, 8 * h->num_sms), 256, 0, s>>>(Ci.p, dim);
+    h->launched("k_symmetrize_lower");
+  }
   DevBuf<double> P, Mu;
   P.resize((size_t)n * n);
   Mu.resize((size_t)n * n);
-  k_build_P<<<gridn(n * n, 256, 8 * h->num_sms), 256, 0, s>>>(n, m.p, m.q, dim, m.aid.p, m.x_ptr.p, m.x_col.p,
-                                                               m.x_val.p, CiWt.p, ve, P.p);
-  h->launched("k_build_P");
-  const double one = 1.0, zero = 0.0;
-  CBX_BLAS(cublasDgemm(L.blas, CUBLAS_OP_N, CUBLAS_OP_N, (int)n, (int)n, (int)n, &one, P.p, (int)n, D.ZAZt.p, (int)n,
-                       &zero, Mu.p, (int)n));
+  k_build_P_ci<<<gridn(n * n, 256, 8 * h->num_sms), 256, 0, s>>>(n, m.p, m.q, dim, m.aid.p, m.x_ptr.p, m.x_col.p,
+                                                                  m.x_val.p, Ci.p, ve, P.p);
+  h->launched("k_build_P_ci");
+  k_dgemm_nn<<<dim3((unsigned)((n + 63) / 64), (unsigned)((n + 63) / 64)), 256, 0, s>>>(n, P.p, D.ZAZt.p, Mu.p);
+  h->launched("k_dgemm_nn");
   const unsigned g = gridn(n * n, 256, 4 * h->num_sms);
   DevBuf<double> part;
   part.resize((size_t)g * 5);
@@ -878,7 +936,8 @@ static bool dense_exact_step(cbx_handle* h, double& vu_io, double& ve_io, IterIn
   DevBuf<double> dPy;
   dPy.resize(n);
   CBX_CUDA(cudaMemcpyAsync(dPy.p, Py.data(), n * sizeof(double), cudaMemcpyHostToDevice, s));
-  CBX_BLAS(cublasDgemv(L.blas, CUBLAS_OP_N, (int)n, (int)n, &one, D.ZAZt.p, (int)n, dPy.p, 1, &zero, ZPy.p, 1));
+  k_dgemv_n<<<gridn(n, 256, 4 * h->num_sms), 256, 0, s>>>(n, D.ZAZt.p, dPy.p, ZPy.p);
+  h->launched("k_dgemv_n");
   const auto ZPyh = d2h(h, ZPy.p, n);
   const double score_u = dot_h(Py, ZPyh), score_e = dot_h(Py, Py);
   const double grad_u = -0.5 * sums[3] + 0.5 * score_u;
@@ -1287,8 +1346,47 @@ extern "C" int cbx_reml_solve(cbx_handle* h, const cbx_reml_config* cfg, double*
 
 namespace cbx {
 
-// Eigen-bending inverse of a device matrix into out_dev (both n x n, column-major).
-void invert_psd_device(cbx_handle* h, const double* M_dev, int64_t n, double ridge, double* out_dev) {
+// Absolute column sums of a symmetric n x n matrix (= its row sums), one block
+// per column: their maximum bounds every |eigenvalue|.
+__global__ void k_col_abs_sum(const double* __restrict__ M, int64_t n, double* __restrict__ out) {
+  __shared__ double red[256];
+  const int64_t c = blockIdx.x;
+  double a = 0.0;
+  for (int64_t r = threadIdx.x; r < n; r += blockDim.x) a += fabs(M[c * n + r]);
+  red[threadIdx.x] = a;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[c] = red[0];
+}
+// A += sum_i w_i u_i u_i^T (U: n x k column-major)
+__global__ void k_add_lowrank(double* __restrict__ A, int64_t n, const double* __restrict__ U, const double* __restrict__ w,
+                              int k) {
+  const int64_t total = n * n;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = idx % n, c = idx / n;
+    double a = 0.0;
+    for (int i = 0; i < k; ++i) a += w[i] * U[(int64_t)i * n + r] * U[(int64_t)i * n + c];
+    A[idx] += a;
+  }
+}
+
+// Eigen-bending inverse of a device matrix into out_dev (both n x n, column-major):
+// invert_psd_matrix (matrix_io.cpp:488-501) raises every eigenvalue below
+// eps = max(1e-12 lambda_max, 1e-6) to eps and returns U diag(1 / lambda) U^T.
+// The same matrix is formed without the full eigendecomposition:
+//  * lambda_max <= ||M||_inf, so eps = 1e-6 whenever 1e-12 ||M||_inf <= 1e-6;
+//  * if M - eps I has a Cholesky factor, no eigenvalue is raised and the result
+//    is M^-1 (Cholesky inverse);
+//  * otherwise only the eigenpairs below eps are computed (syevdx), M is raised
+//    to M + sum (eps - lambda_i) u_i u_i^T, whose eigenvalues are all >= eps,
+//    and that is inverted by Cholesky.
+// The full eigendecomposition (syevd, scaled columns, GEMM) remains for the
+// other cases.  The three forms are the same matrix in exact arithmetic.
+static void invert_psd_full(cbx_handle* h, const double* M_dev, int64_t n, double ridge, double* out_dev) {
   cudaStream_t s = h->stream;
   Libs& L = libs(h);
   DevBuf<double> U, w;
@@ -1324,6 +1422,70 @@ void invert_psd_device(cbx_handle* h, const double* M_dev, int64_t n, double rid
   const double one = 1.0, zero = 0.0;
   CBX_BLAS(cublasDgemm(L.blas, CUBLAS_OP_N, CUBLAS_OP_T, (int)n, (int)n, (int)n, &one, V.p, (int)n, U.p, (int)n,
                        &zero, out_dev, (int)n));
+}
+
+void invert_psd_device(cbx_handle* h, const double* M_dev, int64_t n, double ridge, double* out_dev) {
+  cudaStream_t s = h->stream;
+  const double r = ridge > 0 ? ridge : 0.0;
+  // M + ridge I into out_dev (the working copy)
+  k_add_ridge_copy<<<gridn(n * n, 256, 8 * h->num_sms), 256, 0, s>>>(M_dev, n, r, out_dev);
+  h->launched("k_add_ridge_copy");
+  double rinf = 0.0;
+  {
+    DevBuf<double> cs;
+    cs.resize(n);
+    k_col_abs_sum<<<(unsigned)n, 256, 0, s>>>(out_dev, n, cs.p);
+    h->launched("k_col_abs_sum");
+    for (double v : d2h(h, cs.p, n)) rinf = std::max(rinf, v);
+  }
+  if (!(std::isfinite(rinf)) || 1e-12 * rinf > 1e-6) {
+    invert_psd_full(h, M_dev, n, ridge, out_dev);
+    return;
+  }
+  const double eps = 1e-6;
+  DevBuf<double> T;
+  T.resize((size_t)n * n);
+  // no eigenvalue below eps: M - eps I is positive definite
+  k_add_ridge_copy<<<gridn(n * n, 256, 8 * h->num_sms), 256, 0, s>>>(out_dev, n, -eps, T.p);
+  h->launched("k_add_ridge_copy");
+  if (potrf(h, T.p, n)) {
+    if (chol_inverse_device(h, out_dev, n)) return;
+    invert_psd_full(h, M_dev, n, ridge, out_dev);
+    return;
+  }
+  // the eigenpairs below eps: lambda in (-||M||_inf - 1, eps)
+  Libs& L = libs(h);
+  CBX_CUDA(cudaMemcpyAsync(T.p, out_dev, (size_t)n * n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  DevBuf<double> w;
+  w.resize(n);
+  const double vl = -rinf - 1.0, vu = std::nextafter(eps, 0.0);
+  int meig = 0, lw = 0;
+  CBX_SOLVER(cusolverDnDsyevdx_bufferSize(L.sol, CUSOLVER_EIG_MODE_VECTOR, CUSOLVER_EIG_RANGE_V,
+                                          CUBLAS_FILL_MODE_LOWER, (int)n, T.p, (int)n, vl, vu, 0, 0, &meig, w.p,
+                                          &lw));
+  {
+    DevBuf<double> work;
+    work.resize(std::max(lw, 1));
+    DevBuf<int> info;
+    info.resize(1);
+    CBX_SOLVER(cusolverDnDsyevdx(L.sol, CUSOLVER_EIG_MODE_VECTOR, CUSOLVER_EIG_RANGE_V, CUBLAS_FILL_MODE_LOWER,
+                                 (int)n, T.p, (int)n, vl, vu, 0, 0, &meig, w.p, work.p, lw, info.p));
+    int hi = 0;
+    CBX_CUDA(cudaMemcpyAsync(&hi, info.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CBX_CUDA(cudaStreamSynchronize(s));
+    if (hi != 0 || meig < 0 || meig > n) {
+      invert_psd_full(h, M_dev, n, ridge, out_dev);
+      return;
+    }
+  }
+  if (meig > 0) {
+    std::vector<double> wh = d2h(h, w.p, meig);
+    for (auto& v : wh) v = eps - v;
+    CBX_CUDA(cudaMemcpyAsync(w.p, wh.data(), meig * sizeof(double), cudaMemcpyHostToDevice, s));
+    k_add_lowrank<<<gridn(n * n, 256, 8 * h->num_sms), 256, 0, s>>>(out_dev, n, T.p, w.p, meig);
+    h->launched("k_add_lowrank");
+  }
+  if (!chol_inverse_device(h, out_dev, n)) invert_psd_full(h, M_dev, n, ridge, out_dev);
 }
 
 // In-place inverse of an SPD device matrix by Cholesky; false if not PD.

@@ -208,6 +208,10 @@ int cbx_profile_read(cbx_handle* h, int32_t bucket, int64_t* launches, double* t
                      double* total_bytes);
 int cbx_timer_start(cbx_handle* h);
 int cbx_timer_stop(cbx_handle* h, double* ms);
+/* Named NVTX range around a sequence of calls on this thread, so that a profiler
+ * can select the kernels launched inside it; no effect without a profiler. */
+int cbx_range_push(const char* name);
+int cbx_range_pop(void);
 
 /* ---- Pinned host buffers (no reference counterpart) ------------------------
  * Page-locks / releases a caller's host buffer (cudaHostRegister), so that the

@@ -109,6 +109,12 @@ def test_breakdown_restart_returns_iterate(handle, prob, precision):
         assert rr[c] == relo  # 1 along the singular direction, 0 for b = 0
         if precision == FP64:
             assert it[c] == maxit
-    # column 0 in the same block runs its own recurrence, as a solve alone does
+    # column 0 in the same block runs its own recurrence: it converges as a solve
+    # alone does (same iterations; the block and single-column products sum in
+    # different orders, and this LHS is singular, so the iterates are compared
+    # through their true residuals)
     x0, it0, rr0 = dm.pcg_solve(0.0, B[:, 0], maxit=maxit, precision=precision)
-    assert it[0] == it0[0] and np.array_equal(X[:, 0], x0)
+    b0 = B[:, 0]
+    assert it[0] == it0[0]
+    for x in (X[:, 0], x0):
+        assert np.linalg.norm(b0 - A @ x) <= 1e-9 * np.linalg.norm(b0)
