@@ -40,7 +40,8 @@ constexpr int NRAW = 4;       // raw 2-bit stages
 constexpr int CHUNK_STEPS = 64;  // 2048 SNPs per exact FP32 chunk
 constexpr int NVAR = 11;      // B-side operand variants
 constexpr int NDIG = 7;       // digits per SNP (3 for a_j, 4 for e_j)
-constexpr int THREADS = 320;  // 10 warps
+constexpr int THREADS = 448;  // 14 warps: MMA, loader, 8 producers, 4 epilogue
+constexpr int NPROD = 256;    // producer threads
 
 constexpr int A_TILE_BYTES = TILE_M * KSTEP * 2;                   // 8192
 constexpr int B_VAR_BYTES = TILE_N * KSTEP * 2;                    // 2048
@@ -89,6 +90,10 @@ __device__ __forceinline__ void fail(Bars* b, int* status) {
   atomicExch(status, DEV_TIMEOUT);
 }
 
+__device__ __forceinline__ void st_shared_v2(uint32_t addr, uint32_t a, uint32_t b) {
+  asm volatile("st.shared.v2.b32 [%0], {%1,%2};" ::"r"(addr), "r"(a), "r"(b) : "memory");
+}
+
 __device__ __forceinline__ void st_shared_v4(uint32_t addr, uint32_t a, uint32_t b, uint32_t c,
                                              uint32_t d) {
   asm volatile("st.shared.v4.b32 [%0], {%1,%2,%3,%4};" ::"r"(addr), "r"(a), "r"(b), "r"(c),
@@ -128,12 +133,12 @@ __global__ void __launch_bounds__(THREADS, 1) k_grm_tc(Args args) {
 
   if (tid == 0) {
     for (int i = 0; i < NSTAGE; ++i) {
-      mbar_init(&bars->op_full[i], 128);
+      mbar_init(&bars->op_full[i], NPROD);
       mbar_init(&bars->op_empty[i], 1);
     }
     for (int i = 0; i < NRAW; ++i) {
       mbar_init(&bars->raw_full[i], 32);
-      mbar_init(&bars->raw_empty[i], 128);
+      mbar_init(&bars->raw_empty[i], NPROD);
     }
     for (int i = 0; i < 2; ++i) {
       mbar_init(&bars->acc_full[i], 1);
@@ -230,13 +235,18 @@ __global__ void __launch_bounds__(THREADS, 1) k_grm_tc(Args args) {
     }
     if (!ok) fail(bars, args.status);
     cp_async_wait_all();
-  } else if (warp < 6) {
+  } else if (warp < 2 + NPROD / 32) {
     // ---------------- producers: 2-bit codes -> f16 operand tiles ----------------
+    // Eight warps: A side, thread = (row, half of the 32 SNPs); B side, thread =
+    // (row, k-group of 8 SNPs, half of it).  Every warp's 16-byte (A) and 8-byte
+    // (B) stores cover whole 128-byte lines.
     const int pt = tid - 64;
     uint32_t g = 0;
     bool ok = true;
-    const int br = pt & 31;   // B-side row
-    const int bkg = pt >> 5;  // B-side k-group (8 SNPs)
+    const int arow = pt >> 1, ahalf = pt & 1;         // A-side row, SNPs 16*ahalf .. +15
+    const int unit = pt >> 1, bhalf = pt & 1;
+    const int br = unit & 31;                         // B-side row
+    const int bkg = unit >> 5;                        // B-side k-group (8 SNPs)
     for (int t = blockIdx.x; t < args.ntiles && ok; t += gridDim.x) {
       for (int s = 0; s < nsteps; ++s, ++g) {
         const uint32_t rslot = g % NRAW, oslot = g % NSTAGE;
@@ -244,15 +254,15 @@ __global__ void __launch_bounds__(THREADS, 1) k_grm_tc(Args args) {
         if (!mbar_wait(&bars->op_empty[oslot], ((g / NSTAGE) & 1) ^ 1, abort_flag)) { ok = false; break; }
         const uint8_t* raw = smem + OFF_RAW + rslot * RAW_BYTES;
         const uint32_t st = smem_addr(smem + OFF_STAGE + oslot * STAGE_BYTES);
-        // A side: row pt, 32 SNPs
+        // A side: row arow, SNPs 16*ahalf .. 16*ahalf+15 (k-groups 2*ahalf, 2*ahalf+1)
         {
-          const uint2 w = *reinterpret_cast<const uint2*>(raw + pt * 8);
-          const uint32_t base = (pt >> 3) * 512 + (pt & 7) * 16;
+          const uint32_t word = *reinterpret_cast<const uint32_t*>(raw + arow * 8 + ahalf * 4);
+          const uint32_t base = (arow >> 3) * 512 + (arow & 7) * 16;
 #pragma unroll
-          for (int kg = 0; kg < 4; ++kg) {
-            const uint32_t word = kg < 2 ? w.x : w.y;
-            const uint32_t b0 = (word >> (16 * (kg & 1))) & 0xFF;
-            const uint32_t b1 = (word >> (16 * (kg & 1) + 8)) & 0xFF;
+          for (int kk = 0; kk < 2; ++kk) {
+            const int kg = 2 * ahalf + kk;
+            const uint32_t b0 = (word >> (16 * kk)) & 0xFF;
+            const uint32_t b1 = (word >> (16 * kk + 8)) & 0xFF;
             uint32_t x0, x1, x2, x3, o0, o1, o2, o3;
             decode_byte(b0, x0, x1, o0, o1);
             decode_byte(b1, x2, x3, o2, o3);
@@ -260,30 +270,25 @@ __global__ void __launch_bounds__(THREADS, 1) k_grm_tc(Args args) {
             st_shared_v4(st + A_TILE_BYTES + base + kg * 128, o0, o1, o2, o3);
           }
         }
-        // B side: row br, SNPs 8*bkg .. 8*bkg+7, 11 variants
+        // B side: row br, SNPs 8*bkg + 4*bhalf .. +3, 11 variants
         {
-          const uint32_t b0 = raw[RAW_A + br * 8 + 2 * bkg];
-          const uint32_t b1 = raw[RAW_A + br * 8 + 2 * bkg + 1];
-          uint32_t X[4], O[4];
-          decode_byte(b0, X[0], X[1], O[0], O[1]);
-          decode_byte(b1, X[2], X[3], O[2], O[3]);
-          const uint8_t* dg = raw + RAW_A + RAW_B + bkg * 16;
-          const uint32_t vbase = st + 2 * A_TILE_BYTES + (br >> 3) * 512 + (br & 7) * 16 + bkg * 128;
-          st_shared_v4(vbase, X[0], X[1], X[2], X[3]);  // variant 0: X
+          const uint32_t b = raw[RAW_A + br * 8 + 2 * bkg + bhalf];
+          uint32_t X[2], O[2];
+          decode_byte(b, X[0], X[1], O[0], O[1]);
+          const uint8_t* dg = raw + RAW_A + RAW_B + bkg * 16 + bhalf * 8;
+          const uint32_t vbase =
+              st + 2 * A_TILE_BYTES + (br >> 3) * 512 + (br & 7) * 16 + bkg * 128 + bhalf * 8;
+          st_shared_v2(vbase, X[0], X[1]);  // variant 0: X
 #pragma unroll
           for (int d = 0; d < NDIG; ++d) {
-            const uint4 dv = *reinterpret_cast<const uint4*>(dg + d * 64);
-            const uint32_t D[4] = {dv.x, dv.y, dv.z, dv.w};
+            const uint2 dv = *reinterpret_cast<const uint2*>(dg + d * 64);
             if (d < 3) {
               // variants 1..3: O*d, variants 4..6: X*d
-              st_shared_v4(vbase + (1 + d) * B_VAR_BYTES, hmul2u(O[0], D[0]), hmul2u(O[1], D[1]),
-                           hmul2u(O[2], D[2]), hmul2u(O[3], D[3]));
-              st_shared_v4(vbase + (4 + d) * B_VAR_BYTES, hmul2u(X[0], D[0]), hmul2u(X[1], D[1]),
-                           hmul2u(X[2], D[2]), hmul2u(X[3], D[3]));
+              st_shared_v2(vbase + (1 + d) * B_VAR_BYTES, hmul2u(O[0], dv.x), hmul2u(O[1], dv.y));
+              st_shared_v2(vbase + (4 + d) * B_VAR_BYTES, hmul2u(X[0], dv.x), hmul2u(X[1], dv.y));
             } else {
               // variants 7..10: O*e
-              st_shared_v4(vbase + (4 + d) * B_VAR_BYTES, hmul2u(O[0], D[0]), hmul2u(O[1], D[1]),
-                           hmul2u(O[2], D[2]), hmul2u(O[3], D[3]));
+              st_shared_v2(vbase + (4 + d) * B_VAR_BYTES, hmul2u(O[0], dv.x), hmul2u(O[1], dv.y));
             }
           }
         }

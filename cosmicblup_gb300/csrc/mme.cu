@@ -247,6 +247,7 @@ struct Workspace {
   DevBuf<T> seg_part;
   DevBuf<sv::Col> col;
   DevBuf<int> active;
+  DevBuf<unsigned> done;  // arrival counter of k_scalar_beta_c (reset by its last block)
   int nblk_vec = 0, nblk_spmv = 0;
   int64_t dim = -1;
   void alloc(const Mme& m, int num_sms) {
@@ -264,6 +265,8 @@ struct Workspace {
     tol.resize(S);
     col.resize(S);
     active.resize(1);
+    done.resize(1);
+    CBX_CUDA(cudaMemset(done.p, 0, sizeof(unsigned)));
     seg_part.resize((size_t)std::max<int32_t>(m.nseg, 1) * S);
     dim = m.dim;
     nb_fused = 0;
@@ -718,7 +721,7 @@ void run_pcg(cbx_handle* h, Mme& m, const sv::OpView<T>& op, Workspace<T, S>& w,
     }
     for (int j = 0; j < CHECK; ++j) {
       matvec<T, S>(h, op, w, w.P.p, w.Q.p, lam, 1, w.P.p, w.pq_part.p, w.active.p, false, ncols);
-      sv::k_scalar_alpha<S><<<1, sv::NTS, 0, s>>>(w.col.p, w.pq_part.p, w.nblk_spmv);
+      sv::k_scalar_alpha_c<S><<<S, sv::NTC, 0, s>>>(w.col.p, w.pq_part.p, w.nblk_spmv);
       h->launched(sizeof(T) == 4 ? "k_scalar_alpha<f32>" : "k_scalar_alpha<f64>");
       sv::k_update<T, S><<<w.nblk_vec, sv::NT, 0, s>>>(op, w.col.p, X, Xlo, w.R.p, w.Z.p, w.P.p, w.Q.p, w.part.p);
       h->launched(sizeof(T) == 4 ? "k_update<f32>" : "k_update<f64>");
@@ -726,8 +729,8 @@ void run_pcg(cbx_handle* h, Mme& m, const sv::OpView<T>& op, Workspace<T, S>& w,
         sv::k_fixed<T, S><<<(unsigned)m.p, sv::NT, 0, s>>>(op, w.R.p, w.Z.p, w.col.p, w.rz_fix.p);
         h->launched(sizeof(T) == 4 ? "k_fixed<f32>" : "k_fixed<f64>");
       }
-      sv::k_scalar_beta<S><<<1, sv::NTS, 0, s>>>(w.col.p, w.part.p, w.nblk_vec, w.rz_fix.p, m.p, w.tol.p, abs_tol,
-                                                 maxit, w.active.p);
+      sv::k_scalar_beta_c<S><<<S, sv::NTC, 0, s>>>(w.col.p, w.part.p, w.nblk_vec, w.rz_fix.p, m.p, w.tol.p, abs_tol,
+                                                   maxit, w.active.p, w.done.p);
       h->launched(sizeof(T) == 4 ? "k_scalar_beta<f32>" : "k_scalar_beta<f64>");
       sv::k_pupdate<T, S><<<grid_for(m.dim * S, sv::NT, 16 * h->num_sms), sv::NT, 0, s>>>(m.dim, w.col.p, w.Z.p,
                                                                                            w.P.p);

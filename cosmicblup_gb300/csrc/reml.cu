@@ -1523,10 +1523,20 @@ extern "C" int cbx_reml_logl_dense(cbx_handle* h, double var_u, double var_e, do
   return cbx_guard(h, [&] {
     CBX_REQUIRE(h->mme && logL, CBX_ERR_STATE, "call cbx_mme_create and cbx_mme_set_qinv_dense first");
     CBX_CUDA(cudaSetDevice(h->device));
-    cbx::DenseExact& D = cbx::dense_state(h);
-    if (!D.init || D.n != h->mme->n_rec || D.dim != h->mme->dim) cbx::dense_init(h, D);
-    cbx::DevBuf<double> C, sol;
-    *logL = cbx::dense_logL(h, D, var_u, var_e, C, sol);
+    const cbx::Mme& m = *h->mme;
+    if (m.has_dense && !m.has_sparse && m.ng == m.q) {
+      cbx::DenseExact& D = cbx::dense_state(h);
+      if (!D.init || D.n != m.n_rec || D.dim != m.dim) cbx::dense_init(h, D);
+      cbx::DevBuf<double> C, sol;
+      *logL = cbx::dense_logL(h, D, var_u, var_e, C, sol);
+    } else {
+      // a split Qinv: calc_logL_internal, without the constant log|A|
+      CBX_REQUIRE(m.dim <= cbx::kAiDenseMax, CBX_ERR_UNSUPPORTED, "LHS too large for a dense factorization");
+      cbx::DevBuf<double> Q, C;
+      cbx::dense_qinv(h, Q);
+      std::vector<double> sol;
+      *logL = cbx::ai_logl(h, Q.p, var_u, var_e, C, sol);
+    }
   });
 }
 

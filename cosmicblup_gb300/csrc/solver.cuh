@@ -1090,6 +1090,112 @@ __global__ void k_scalar_beta(Col* col, const double* part, int nblk, const doub
   if (c == 0) *active_count = n_act;
 }
 
+// Per-column forms of the two scalar steps of every iteration: one block of
+// NTC threads per column sums that column's block partials (in a fixed order:
+// strided per thread, then a tree), then thread 0 updates the column.  With
+// eight vector blocks per SM the single-block forms above spent ~80 us per
+// call reading ~10^5 partials through one SM.
+constexpr int NTC = 256;
+
+__device__ __forceinline__ double col_total_c(const double* __restrict__ part, int nblk, int64_t stride, int c,
+                                              double* red /*[NTC]*/) {
+  double a = 0.0;
+  for (int b = threadIdx.x; b < nblk; b += NTC) a += part[(int64_t)b * stride + c];
+  red[threadIdx.x] = a;
+  __syncthreads();
+  for (int o = NTC / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  const double t = red[0];
+  __syncthreads();
+  return t;
+}
+
+// alpha = rz / p'Ap per column (grid = S blocks), breakdown handling as k_scalar_alpha.
+template <int S>
+__global__ void __launch_bounds__(NTC) k_scalar_alpha_c(Col* col, const double* pq_part, int nblk) {
+  __shared__ double red[NTC];
+  const int c = blockIdx.x;
+  const double pq = col_total_c(pq_part, nblk, S, c, red);
+  if (threadIdx.x != 0) return;
+  Col s = col[c];
+  s.skip = 0;
+  if (s.active) {
+    s.pq = pq;
+    if (fabs(pq) < 1e-300) {
+      if (!s.restarted) {
+        s.restarted = 1;
+        s.skip = 1;
+      } else {
+        s.active = 0;
+        s.status = COL_BREAKDOWN;
+      }
+    } else {
+      s.alpha = s.rz / pq;
+    }
+  }
+  col[c] = s;
+}
+
+// The convergence test and beta per column (grid = S blocks), as k_scalar_beta;
+// the block that finishes last counts the active columns into *active_count and
+// resets the arrival counter *done (zero before the first launch).
+template <int S>
+__global__ void __launch_bounds__(NTC) k_scalar_beta_c(Col* col, const double* part, int nblk,
+                                                       const double* rz_fix, int64_t p, const double* tol_col,
+                                                       int abs_tol, int maxit, int* active_count,
+                                                       unsigned* done) {
+  __shared__ double red[NTC];
+  __shared__ int last;
+  const int c = blockIdx.x;
+  const double rr = col_total_c(part, nblk, 2 * S, c, red);
+  const double rzr = col_total_c(part + S, nblk, 2 * S, c, red);
+  const double rzf = p > 0 ? col_total_c(rz_fix, (int)p, S, c, red) : 0.0;
+  if (threadIdx.x == 0) {
+    Col s = col[c];
+    if (s.active) {
+      const double rz = rzr + rzf;
+      s.rr = rr;
+      if (s.skip) {
+        s.beta = 0.0;
+        s.rz = rz;
+      } else {
+        s.iters += 1;
+        const double bn = s.bnorm2 > 0 ? sqrt(s.bnorm2) : 1.0;
+        const double res = sqrt(rr);
+        const double tol = tol_col[c];
+        const bool conv = abs_tol ? (res < tol) : (res / bn < tol);
+        if (conv) {
+          s.active = 0;
+          s.status = COL_CONVERGED;
+        } else if (!isfinite(rr) || !isfinite(rz)) {
+          s.active = 0;
+          s.status = COL_NONFINITE;
+        } else if (s.iters >= maxit) {
+          s.active = 0;
+          s.status = COL_MAXIT;
+        } else {
+          s.beta = rz / s.rz;
+          s.rz = rz;
+        }
+      }
+    }
+    col[c] = s;
+    __threadfence();
+    last = atomicAdd(done, 1u) == (unsigned)(S - 1);
+  }
+  __syncthreads();
+  if (last && threadIdx.x == 0) {
+    __threadfence();
+    int n_act = 0;
+    for (int k = 0; k < S; ++k) n_act += __ldcg(&col[k].active);
+    *active_count = n_act;
+    *done = 0u;
+  }
+}
+
+
 // Partial sums of squares per column (interleaved layout).
 template <int S>
 __global__ void __launch_bounds__(NT) k_colnorm2(const double* __restrict__ V, int64_t dim,

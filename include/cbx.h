@@ -408,8 +408,10 @@ int cbx_mt_solve(cbx_handle* h, int64_t n, int32_t t, int64_t p, const double* Y
 int cbx_reml_gradient(cbx_handle* h, double var_u, double var_e, int32_t nprobe, int32_t seed,
                       int32_t exact_trace, int32_t precision, double pcg_tol, int32_t pcg_maxit,
                       double* grad, double* trace, int64_t* pcg_iters);
-/* REML log-likelihood of run_dense_exact_step's compute_logL (src/core/vce.cpp:
- * 2974-3007) by dense Cholesky of the LHS: small problems with a dense Qinv. */
+/* REML log-likelihood by dense Cholesky of the LHS (dim <= 24,576): with a dense
+ * Qinv, run_dense_exact_step's compute_logL (src/core/vce.cpp:2974-3007); with a
+ * split Qinv (ssGBLUP), calc_logL_internal (:3533-3588), which omits the constant
+ * log|A| (it does not depend on the variances). */
 int cbx_reml_logl_dense(cbx_handle* h, double var_u, double var_e, double* logL);
 
 /* ---- Dense Qinv product without device allocation -------------------------
