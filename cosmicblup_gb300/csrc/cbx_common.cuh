@@ -68,14 +68,32 @@ __device__ __forceinline__ bool mbar_try(uint64_t* bar, uint32_t parity) {
 }
 // Wait until the phase with the given parity has completed.  Gives up after
 // limit_ns or when *abort becomes non-zero; returns false in that case.
+// The abort word (shared memory) and the clock are read every 16th try only: a
+// poll is a shared-memory access, and the warps that poll share that pipe with
+// the operand stores and the MMAs' operand reads.
 __device__ __forceinline__ bool mbar_wait_for(uint64_t* bar, uint32_t parity,
                                               volatile int* abort, uint64_t limit_ns) {
   if (mbar_try(bar, parity)) return true;
   const uint64_t t0 = global_ns();
+  for (uint32_t i = 1;; ++i) {
+    if (mbar_try(bar, parity)) return true;
+    if ((i & 15u) == 0) {
+      if (*abort) return false;
+      if (global_ns() - t0 > limit_ns) return false;
+    }
+  }
+}
+// The same wait for a consumer that idles through a whole accumulation (an
+// epilogue waiting for a chunk or a tile): sleeps sleep_ns between tries.
+__device__ __forceinline__ bool mbar_wait_idle(uint64_t* bar, uint32_t parity, volatile int* abort,
+                                               uint32_t sleep_ns) {
+  if (mbar_try(bar, parity)) return true;
+  const uint64_t t0 = global_ns();
   while (true) {
+    __nanosleep(sleep_ns);
     if (mbar_try(bar, parity)) return true;
     if (*abort) return false;
-    if (global_ns() - t0 > limit_ns) return false;
+    if (global_ns() - t0 > kWaitLimitNs) return false;
   }
 }
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity,

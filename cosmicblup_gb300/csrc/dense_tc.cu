@@ -288,7 +288,7 @@ __global__ void __launch_bounds__(THREADS, 1)
       // slot: this CTA's rank among the CTAs that cover the tile
       const int ks = (int)blockIdx.x - (mt * ksteps) / per;
       const uint32_t b = c & 1;
-      if (!mbar_wait(&bars->acc_full[b], (c >> 1) & 1, abort_flag)) { ok = false; break; }
+      if (!mbar_wait_idle(&bars->acc_full[b], (c >> 1) & 1, abort_flag, 64)) { ok = false; break; }
       tc_fence_after();
       // columns [0, nc): A B_hi; [nc, 2 nc): A B_lo + A_lo B_hi; nc <= S
       float out[S];

@@ -311,7 +311,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_grm_tc(Args args) {
       const int2 tl = args.tiles[t];
       for (int ch = 0; ch < nchunks; ++ch, ++c) {
         const uint32_t b = c & 1;
-        if (!mbar_wait(&bars->acc_full[b], (c >> 1) & 1, abort_flag)) { ok = false; break; }
+        if (!mbar_wait_idle(&bars->acc_full[b], (c >> 1) & 1, abort_flag, 1000)) { ok = false; break; }
         tc_fence_after();
         const uint32_t ta = tmem_base + (uint32_t(q * 32) << 16) + b * 256;
 #pragma unroll 1

@@ -27,6 +27,10 @@ struct cbx_handle {
   int64_t G_n = 0;
   cbx::DevBuf<double> Ginv;
   int64_t Ginv_n = 0;
+  // dense block of the single-step H^-1 (G_blend^-1 - A22^-1, ng x ng) left on
+  // the device by cbx_ssgblup_qinv
+  cbx::DevBuf<double> Hd;
+  int64_t Hd_n = 0;
   // mixed-model equations and REML state
   std::unique_ptr<cbx::Mme> mme;
   // library handles (cuSOLVER / cuBLAS) and dense exact AI state, owned here

@@ -1185,10 +1185,24 @@ static void upload_csr(cudaStream_t s, int64_t rows, const std::vector<int32_t>&
   }
 }
 
-// Sort triplets by (row, col) keeping insertion order among duplicates, then sum duplicates.
+// Triplets to CSR, duplicates summed in their insertion order: a stable counting
+// sort by row, then a stable sort of each row by column (the same order as one
+// stable sort by (row, column), in linear time for the many short rows).
 static void triplets_to_csr(int64_t rows, std::vector<Trip>& t, std::vector<int32_t>& ptr, std::vector<int32_t>& col,
                             std::vector<double>& val) {
-  std::stable_sort(t.begin(), t.end(), [](const Trip& a, const Trip& b) { return a.r != b.r ? a.r < b.r : a.c < b.c; });
+  {
+    std::vector<int64_t> start(rows + 1, 0);
+    for (const Trip& x : t) start[x.r + 1]++;
+    for (int64_t i = 0; i < rows; ++i) start[i + 1] += start[i];
+    std::vector<Trip> by_row(t.size());
+    std::vector<int64_t> pos(start.begin(), start.end() - 1);
+    for (const Trip& x : t) by_row[pos[x.r]++] = x;
+    for (int64_t i = 0; i < rows; ++i)
+      if (start[i + 1] - start[i] > 1)
+        std::stable_sort(by_row.begin() + start[i], by_row.begin() + start[i + 1],
+                         [](const Trip& a, const Trip& b) { return a.c < b.c; });
+    t.swap(by_row);
+  }
   ptr.assign(rows + 1, 0);
   col.clear();
   val.clear();
@@ -1202,39 +1216,6 @@ static void triplets_to_csr(int64_t rows, std::vector<Trip>& t, std::vector<int3
     k = e;
   }
   for (int64_t i = 0; i < rows; ++i) ptr[i + 1] += ptr[i];
-}
-
-// In-place Cholesky inverse of an SPD matrix (row-major n x n); false if not SPD.
-static bool spd_inverse(std::vector<double>& A, int64_t n) {
-  std::vector<double> L(A);
-  for (int64_t j = 0; j < n; ++j) {
-    double d = L[j * n + j];
-    for (int64_t k = 0; k < j; ++k) d -= L[j * n + k] * L[j * n + k];
-    if (!(d > 0)) return false;
-    d = std::sqrt(d);
-    L[j * n + j] = d;
-    for (int64_t i = j + 1; i < n; ++i) {
-      double v = L[i * n + j];
-      for (int64_t k = 0; k < j; ++k) v -= L[i * n + k] * L[j * n + k];
-      L[i * n + j] = v / d;
-    }
-  }
-  // inverse via solves with identity columns
-  std::vector<double> inv(n * n, 0.0), y(n);
-  for (int64_t c = 0; c < n; ++c) {
-    for (int64_t i = 0; i < n; ++i) {
-      double v = (i == c) ? 1.0 : 0.0;
-      for (int64_t k = 0; k < i; ++k) v -= L[i * n + k] * y[k];
-      y[i] = v / L[i * n + i];
-    }
-    for (int64_t i = n - 1; i >= 0; --i) {
-      double v = y[i];
-      for (int64_t k = i + 1; k < n; ++k) v -= L[k * n + i] * inv[k * n + c];
-      inv[i * n + c] = v / L[i * n + i];
-    }
-  }
-  A.swap(inv);
-  return true;
 }
 
 }  // namespace cbx
@@ -1329,13 +1310,31 @@ extern "C" int cbx_mme_create(cbx_handle* h, int64_t n_rec, int64_t p, int64_t q
       const double ridge = std::max(1e-8 * maxd, 1e-6);
       std::vector<double> M(A11);
       for (int64_t i = 0; i < p; ++i) M[i * p + i] += ridge;
-      if (!spd_inverse(M, p)) {
+      bool diagonal = true;
+      for (int64_t i = 0; i < p && diagonal; ++i)
+        for (int64_t j = 0; j < p; ++j)
+          if (j != i && M[i * p + j] != 0.0) { diagonal = false; break; }
+      m->A11inv64.resize((size_t)p * p);
+      bool ok = true;
+      if (diagonal) {
+        // one fixed factor: X'X is diagonal and so is its inverse
+        for (int64_t i = 0; i < p; ++i) {
+          ok = ok && M[i * p + i] > 0.0;
+          M[i * p + i] = 1.0 / M[i * p + i];
+        }
+        if (ok)
+          CBX_CUDA(cudaMemcpyAsync(m->A11inv64.p, M.data(), M.size() * sizeof(double), cudaMemcpyHostToDevice, s));
+      } else {
+        // Cholesky inverse on the device (cuSOLVER potrf / potri)
+        CBX_CUDA(cudaMemcpyAsync(m->A11inv64.p, M.data(), M.size() * sizeof(double), cudaMemcpyHostToDevice, s));
+        ok = chol_inverse_device(h, m->A11inv64.p, p);
+      }
+      if (!ok) {
         // reference fallback: diagonal scaling of the fixed block (pcg_solver.h:108-116)
         M.assign((size_t)p * p, 0.0);
         for (int64_t i = 0; i < p; ++i) M[i * p + i] = std::fabs(diag[i]) > 1e-14 ? 1.0 / diag[i] : 1.0;
+        CBX_CUDA(cudaMemcpyAsync(m->A11inv64.p, M.data(), M.size() * sizeof(double), cudaMemcpyHostToDevice, s));
       }
-      m->A11inv64.resize((size_t)p * p);
-      CBX_CUDA(cudaMemcpyAsync(m->A11inv64.p, M.data(), M.size() * sizeof(double), cudaMemcpyHostToDevice, s));
       m->A11inv32.resize((size_t)p * p);
       k_convert<double, float><<<grid_for(p * p, 256, 1024), 256, 0, s>>>(m->A11inv64.p, m->A11inv32.p, p * p);
       h->launched("k_convert");
@@ -1439,7 +1438,8 @@ extern "C" int cbx_mme_set_qinv_dense(cbx_handle* h, const double* Qinv, int64_t
 }
 
 // Split Qinv = A (CSR, q x q) + S Gd S^T with Gd dense ng x ng (row-major) and
-// gmap[k] the u-index of dense row k (SplitMatrixAdapter::operator*).
+// gmap[k] the u-index of dense row k (SplitMatrixAdapter::operator*).  Gd ==
+// NULL with ng > 0 uses the block cbx_ssgblup_qinv left on the device.
 extern "C" int cbx_mme_set_qinv_split(cbx_handle* h, const int64_t* a_ptr, const int32_t* a_col,
                                       const double* a_val, const double* Gd, int64_t ng,
                                       const int32_t* gmap) {
@@ -1466,18 +1466,29 @@ extern "C" int cbx_mme_set_qinv_split(cbx_handle* h, const int64_t* a_ptr, const
     m.has_dense = ng > 0;
     m.drop_carry();
     if (ng > 0) {
-      CBX_REQUIRE(Gd && gmap, CBX_ERR_ARG, "dense block or map missing");
+      CBX_REQUIRE(gmap, CBX_ERR_ARG, "genotyped map missing");
+      CBX_REQUIRE(Gd || (h->Hd.p && h->Hd_n == ng), CBX_ERR_STATE,
+                  "no dense block: pass Gd or run cbx_ssgblup_qinv with this ng first");
       std::vector<int32_t> inv(q, -1);
       for (int64_t k = 0; k < ng; ++k) {
         CBX_REQUIRE(gmap[k] >= 0 && gmap[k] < q, CBX_ERR_ARG, "genotyped map out of range");
         CBX_REQUIRE(inv[gmap[k]] < 0, CBX_ERR_ARG, "genotyped map has duplicates");
         inv[gmap[k]] = (int32_t)k;
-        diag[gmap[k]] += Gd[k * ng + k];
       }
       DevBuf<double> tmp;
-      tmp.resize((size_t)ng * ng);
-      CBX_CUDA(cudaMemcpyAsync(tmp.p, Gd, (size_t)ng * ng * sizeof(double), cudaMemcpyHostToDevice, s));
-      upload_dense(h, m, tmp.p, ng);
+      const double* src = h->Hd.p;
+      if (Gd) {
+        tmp.resize((size_t)ng * ng);
+        CBX_CUDA(cudaMemcpyAsync(tmp.p, Gd, (size_t)ng * ng * sizeof(double), cudaMemcpyHostToDevice, s));
+        src = tmp.p;
+      }
+      // diagonal of the dense block, for diag(Qinv)
+      std::vector<double> dd(ng);
+      CBX_CUDA(cudaMemcpy2DAsync(dd.data(), sizeof(double), src, (ng + 1) * sizeof(double), sizeof(double), ng,
+                                 cudaMemcpyDeviceToHost, s));
+      CBX_CUDA(cudaStreamSynchronize(s));
+      for (int64_t k = 0; k < ng; ++k) diag[gmap[k]] += dd[k];
+      upload_dense(h, m, src, ng);
       m.gmap.resize(ng);
       m.ginv.resize(q);
       CBX_CUDA(cudaMemcpyAsync(m.gmap.p, gmap, ng * sizeof(int32_t), cudaMemcpyHostToDevice, s));

@@ -389,10 +389,11 @@ extern "C" int cbx_ssgblup_qinv(cbx_handle* h, int64_t n, const int64_t* dam, co
     ped::k_combine<<<ped::gridn(ng * ng, 256, 8 * h->num_sms), 256, 0, s>>>(Gbi.p, A22.p, ng * ng, tau, omega, Gd.p);
     h->launched("k_combine");
     if (Gd_out) CBX_CUDA(cudaMemcpyAsync(Gd_out, Gd.p, (size_t)ng * ng * 8, cudaMemcpyDeviceToHost, s));
-    std::vector<double> Gd_h((size_t)ng * ng);
-    CBX_CUDA(cudaMemcpyAsync(Gd_h.data(), Gd.p, (size_t)ng * ng * 8, cudaMemcpyDeviceToHost, s));
     CBX_CUDA(cudaStreamSynchronize(s));
-    if (int rc = cbx_mme_set_qinv_split(h, ap.data(), ac.data(), av.data(), Gd_h.data(), ng, gmap); rc != CBX_OK)
+    // the block stays on the device for later MMEs of this handle
+    h->Hd = std::move(Gd);
+    h->Hd_n = ng;
+    if (int rc = cbx_mme_set_qinv_split(h, ap.data(), ac.data(), av.data(), nullptr, ng, gmap); rc != CBX_OK)
       throw Error(rc, h->last_error);
   });
 }

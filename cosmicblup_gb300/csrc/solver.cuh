@@ -294,24 +294,27 @@ static __global__ void __launch_bounds__(256) k_colsum_x(const double* __restric
   if (tid == 0) out[c] = __dadd_rn(rs[0], re[0]);
 }
 
-// out[c] = sum_k Vt[c * ld + k] (k < ng) in FP64: the column sums of the
-// gathered vectors of an FP32 product with the shifted block (FP64 holds the
-// sum of FP32 values with 29 spare bits, so cancellation costs nothing that
-// the FP32 solve can see).  One block of 256 threads per column, fixed order.
+// out[c] = sum_k Vt[c * ld + k] (k < ng): the column sums of the gathered
+// vectors of an FP32 product with the shifted block.  Each thread sums with
+// Kahan compensation (error about one rounding of its sum plus n eps^2 of the
+// magnitudes, far below the FP32 product's), the threads' sums are combined in
+// FP64.  One block of 1024 threads per column, fixed order.
 template <typename T>
 __global__ void __launch_bounds__(1024) k_colsum_vt(const T* __restrict__ Vt, int64_t ld, int64_t ng,
                                                     double* __restrict__ out) {
   __shared__ double red[1024];
   const int c = blockIdx.x, tid = threadIdx.x;
-  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  // per-thread sums compensated in the vectors' own precision (no FP64
+  // arithmetic per element), combined in FP64
+  DotAcc<T> acc[4];
   const T* col = Vt + (int64_t)c * ld;
   int64_t k = tid;
   for (; k + 3 * 1024 < ng; k += 4 * 1024) {
 #pragma unroll
-    for (int u = 0; u < 4; ++u) acc[u] += (double)col[k + u * 1024];
+    for (int u = 0; u < 4; ++u) acc[u].add(col[k + u * 1024], T(1));
   }
-  for (; k < ng; k += 1024) acc[0] += (double)col[k];
-  red[tid] = (acc[0] + acc[1]) + (acc[2] + acc[3]);
+  for (; k < ng; k += 1024) acc[0].add(col[k], T(1));
+  red[tid] = (acc[0].value() + acc[1].value()) + (acc[2].value() + acc[3].value());
   __syncthreads();
   for (int o = 512; o > 0; o >>= 1) {
     if (tid < o) red[tid] += red[tid + o];
@@ -696,14 +699,28 @@ __device__ __forceinline__ void spmv_random_row(const OpView<T>& op, int64_t i, 
   } else {
     constexpr int G = 32 / S;
     const int c = lane % S, g = lane / S;
+    // this lane's entries j = start + g, + G, ... in batches of 4 (loads first,
+    // then the multiply-adds in the same order as one entry at a time)
+    auto rowsum1 = [&](const int32_t* __restrict__ cidx, const T* __restrict__ val, int32_t j, int32_t e1,
+                       int64_t off) {
+      T a = T(0);
+      for (; j + 3 * G < e1; j += 4 * G) {
+        T dv[4], xv[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          dv[k] = val[j + k * G];
+          xv[k] = X[(off + cidx[j + k * G]) * S + c];
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) a += dv[k] * xv[k];
+      }
+      for (; j < e1; j += G) a += val[j] * X[(off + cidx[j]) * S + c];
+      return a;
+    };
     T acc = T(0);
-    if (use_D) {
-      for (int32_t j = op.Dptr[i] + g; j < op.Dptr[i + 1]; j += G) acc += op.Dval[j] * X[(int64_t)op.Dcol[j] * S + c];
-    }
+    if (use_D) acc = rowsum1(op.Dcol, op.Dval, op.Dptr[i] + g, op.Dptr[i + 1], 0);
     T qv = T(0);
-    if (op.Sptr) {
-      for (int32_t j = op.Sptr[u] + g; j < op.Sptr[u + 1]; j += G) qv += op.Sval[j] * X[(p + op.Scol[j]) * S + c];
-    }
+    if (op.Sptr) qv = rowsum1(op.Scol, op.Sval, op.Sptr[u] + g, op.Sptr[u + 1], p);
 #pragma unroll
     for (int off = 16; off >= S; off >>= 1) {
       acc += __shfl_xor_sync(0xffffffffu, acc, off);
@@ -915,10 +932,12 @@ __global__ void __launch_bounds__(NT) k_update(OpView<T> op, const Col* __restri
     }
     arr.add(r, r);
     if (i >= op.p) {
-      T z = Z[idx];
+      T z;
       if (upd) {
         z = op.dinv[i - op.p] * r;
         Z[idx] = z;
+      } else {
+        z = Z[idx];
       }
       arz.add(r, z);
     }

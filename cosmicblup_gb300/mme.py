@@ -46,12 +46,14 @@ class DeviceMME:
             self.h.check(lib().cbx_mme_set_qinv_dense(self.h.raw, ptr(Q), self.q))
 
     def set_qinv_split(self, a_ptr, a_col, a_val, Gd=None, gmap=None):
+        """Qinv = A^-1 (CSR) + S Gd S^T.  Gd None with a gmap uses the dense block
+        that ssgblup_qinv left on the device (order len(gmap))."""
         a_ptr = np.ascontiguousarray(a_ptr, dtype=np.int64)
         a_col = np.ascontiguousarray(a_col, dtype=np.int32)
         a_val = np.ascontiguousarray(a_val, dtype=np.float64)
-        ng = 0 if Gd is None else Gd.shape[0]
-        Gd = None if Gd is None else np.ascontiguousarray(Gd, dtype=np.float64)
         gmap = None if gmap is None else np.ascontiguousarray(gmap, dtype=np.int32)
+        ng = Gd.shape[0] if Gd is not None else (0 if gmap is None else gmap.size)
+        Gd = None if Gd is None else np.ascontiguousarray(Gd, dtype=np.float64)
         self.h.check(lib().cbx_mme_set_qinv_split(self.h.raw, ptr(a_ptr), ptr(a_col), ptr(a_val),
                                                   ptr(Gd), ng, ptr(gmap)))
 

@@ -165,7 +165,9 @@ int cbx_mme_set_qinv_dense(cbx_handle* h, const double* Qinv, int64_t q);
 /* Qinv = A + S Gd S^T: A sparse q x q in CSR (a_ptr[q+1] int64, a_col int32,
  * a_val), Gd dense ng x ng, gmap[k] = row of Qinv for dense row k
  * (SplitMatrixAdapter, src/core/matrix_adapter.h:232-373, with the G^-1 and
- * A22^-1 blocks pre-combined into Gd = G^-1 - A22^-1). */
+ * A22^-1 blocks pre-combined into Gd = G^-1 - A22^-1).  Gd == NULL with ng > 0
+ * uses the block that cbx_ssgblup_qinv left on the device of this handle
+ * (CBX_ERR_STATE when there is none of order ng). */
 int cbx_mme_set_qinv_split(cbx_handle* h, const int64_t* a_ptr, const int32_t* a_col,
                            const double* a_val, const double* Gd, int64_t ng,
                            const int32_t* gmap);
@@ -260,7 +262,8 @@ int cbx_ainv_henderson(cbx_handle* h, int64_t n, const int64_t* dam, const int64
  * Gd = tau Gb^-1 (eigen-bending) - omega A22^-1, and installs
  * Qinv = A^-1 + S Gd S' on the MME (q = n) as cbx_mme_set_qinv_split would.
  * G == NULL uses the device GRM of this handle (order ng).  A22_out / Gd_out
- * (ng x ng) may be NULL. */
+ * (ng x ng) may be NULL.  Gd stays on the device for later MMEs of the handle
+ * (cbx_mme_set_qinv_split with Gd == NULL). */
 int cbx_ssgblup_qinv(cbx_handle* h, int64_t n, const int64_t* dam, const int64_t* sire, int64_t ng,
                      const int32_t* gmap, const double* G, double alpha, int32_t tune_g, double tau,
                      double omega, double ridge, double* A22_out, double* Gd_out);

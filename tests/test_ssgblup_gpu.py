@@ -75,3 +75,21 @@ def test_pcg_and_em_on_hinv(handle, ss):
     assert info["probes"] == ores["samples"]
     assert abs(r.var_u - o.var_u) <= 1e-6 * o.var_u
     assert abs(r.var_e - o.var_e) <= 1e-6 * o.var_e
+
+
+def test_split_with_device_block_equals_host_block(handle, ss):
+    """A later MME of the handle takes the dense H^-1 block that ssgblup_qinv left on
+    the device (Gd omitted): the same operator as the block passed from the host."""
+    dm = DeviceMME(handle, ss["rec"]["y"], ss["rec"]["aid"], ss["rows"], ss["p"], ss["n"])
+    _, Gd = ssgblup_qinv(dm, ss["dam"], ss["sire"], ss["gmap"], G=ss["G"], return_blocks=True)
+    Ainv = ainv_henderson(handle, ss["dam"], ss["sire"])
+    X = np.random.default_rng(2).normal(size=(ss["n"], 3))
+    dm_host = DeviceMME(handle, ss["rec"]["y"], ss["rec"]["aid"], ss["rows"], ss["p"], ss["n"])
+    dm_host.set_qinv_split(*Ainv, Gd=Gd, gmap=ss["gmap"])
+    Y_host = dm_host.qinv_apply(X)
+    x_host, _, _ = dm_host.pcg_solve(1.4, ss["mme"].rhs())
+    dm_dev = DeviceMME(handle, ss["rec"]["y"], ss["rec"]["aid"], ss["rows"], ss["p"], ss["n"])
+    dm_dev.set_qinv_split(*Ainv, gmap=ss["gmap"])
+    np.testing.assert_array_equal(dm_dev.qinv_apply(X), Y_host)
+    x_dev, _, _ = dm_dev.pcg_solve(1.4, ss["mme"].rhs())
+    np.testing.assert_array_equal(x_dev, x_host)
