@@ -106,6 +106,8 @@ SIGNATURES = [
                                         C.c_int32, C.c_int32, C.c_void_p, C.POINTER(C.c_double)]),
     ("cbx_selftest_dense_tc", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_void_p, C.c_int32,
                                         C.c_void_p]),
+    ("cbx_selftest_dense_fx", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_void_p, C.c_int32,
+                                        C.c_int32, C.c_void_p, C.POINTER(C.c_double)]),
     ("cbx_selftest_wait_timeout", C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_double)]),
 ]
 

@@ -27,6 +27,7 @@
 #include <vector>
 #include "handle.h"
 #include "dense_tc.h"
+#include "tma.cuh"
 
 namespace cbx {
 namespace dtc {
@@ -61,16 +62,6 @@ struct Bars {
   int abort;
 };
 
-__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
-          dst),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_addr(bar))
-      : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
-}
 __device__ __forceinline__ void umma_tf32(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
   asm volatile(
       "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
@@ -334,35 +325,6 @@ __global__ void __launch_bounds__(THREADS, 1)
   if (warp == 1) tmem_dealloc(tmem, TMEM_ALLOC);
 }
 
-typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
-                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
-                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
-static EncodeTiledFn encode_fn() {
-  static EncodeTiledFn fn = nullptr;
-  if (!fn) {
-    void* p = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    CBX_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q));
-    CBX_REQUIRE(p && q == cudaDriverEntryPointSuccess, CBX_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
-    fn = reinterpret_cast<EncodeTiledFn>(p);
-  }
-  return fn;
-}
-
-static CUtensorMap make_map(const float* base, int64_t cols, int64_t rows, int box_rows) {
-  CUtensorMap m;
-  const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
-  const cuuint64_t strides[1] = {(cuuint64_t)cols * 4};
-  const cuuint32_t box[2] = {(cuuint32_t)KB, (cuuint32_t)box_rows};
-  const cuuint32_t es[2] = {1, 1};
-  CUresult r = encode_fn()(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides, box, es,
-                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
-                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-  CBX_REQUIRE(r == CUDA_SUCCESS, CBX_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
-  return m;
-}
-
 }  // namespace dtc
 
 // Stream-K split of the (tile, K step) space: CTA b takes steps [b per,
@@ -387,6 +349,9 @@ static int stream_k(int64_t ng, int64_t ld, int num_sms, int* grid_out, int* per
 }
 
 int dense_tc_ksplit(int64_t ng, int64_t ld, int num_sms) { return stream_k(ng, ld, num_sms, nullptr, nullptr); }
+int dense_tc_stream_k(int64_t ng, int64_t ld, int num_sms, int* grid, int* per) {
+  return stream_k(ng, ld, num_sms, grid, per);
+}
 
 void dense_tc(cbx_handle* h, const float* Qd, int64_t ng, int64_t ld, const float* Vt, int S, int ksplit, float* Tpart,
               const int* active, int ncols) {
@@ -395,8 +360,8 @@ void dense_tc(cbx_handle* h, const float* Qd, int64_t ng, int64_t ld, const floa
   // to the MMA granularity of 16; the output's other columns are written as 0
   const int nc = std::min(S, std::max(16, (ncols + 15) / 16 * 16));
   CBX_REQUIRE(ld % 4 == 0, CBX_ERR_ARG, "row pitch must be a multiple of 4");
-  const CUtensorMap ma = dtc::make_map(Qd, ld, ng, 128);
-  const CUtensorMap mb = dtc::make_map(Vt, ld, S, nc);
+  const CUtensorMap ma = make_map_f32(Qd, ld, ng, 128);
+  const CUtensorMap mb = make_map_f32(Vt, ld, S, nc);
   const int ksteps = (int)((ld + dtc::KB - 1) / dtc::KB);
   const int mtiles = (int)((ng + 127) / 128);
   const int total = mtiles * ksteps;

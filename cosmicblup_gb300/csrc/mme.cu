@@ -367,6 +367,14 @@ static bool use_xff() {
   return v != 0;
 }
 
+// FP64-accurate refinement products of 16 or more columns on the tensor cores
+// (exact fixed-point digits, dense_fx.cu) instead of the CUDA-core float-float
+// kernels; CBX_FX=0 selects the float-float kernels.
+static bool use_fx() {
+  static int v = env_int("CBX_FX", 1);
+  return v != 0;
+}
+
 // Diagnostics: the environment CBX_LOG_REFINE=1 prints every refinement step
 // of the mixed solver (inner iterations, worst relative true residual) to stderr.
 static bool log_refine() {
@@ -485,6 +493,26 @@ static void dense64(cbx_handle* h, const sv::OpView<double>& op, const double* X
     // the compensated FP64 column sums that restore the block's shift
     sv::k_colsum_x<<<ncols, 256, 0, h->stream>>>(X, S, op.p, op.ng, op.gmap, colsum);
     h->launched("k_colsum_x<f64>");
+    if (use_fx() && ncols >= 16) {
+      // tensor-core fixed-point product, 32 columns at a time; fewer than 16
+      // columns left over go to the float-float kernels below
+      Mme& mm = *h->mme;
+      if (!mm.fx_rows_ok) {
+        mm.fx_rowexp.resize(op.ng);
+        fx_row_scales(h, mm.Qd32.p, op.ng, op.ld, mm.fx_rowexp.p);
+        mm.fx_rows_ok = true;
+      }
+      int c0 = 0;
+      for (; ncols - c0 >= 16; c0 += 32) {
+        const int nc = std::min(32, ncols - c0);
+        fx_product(h, mm.Qd32.p, mm.Qlo32.p, mm.fx_rowexp.p, op.ng, op.ld, X + c0, S, op.p, op.gmap, nc, mm.fx_bdig,
+                   mm.fx_cexp, mm.fx_part, Tout + c0, S, active);
+      }
+      if (c0 >= ncols) return;
+      X += c0;
+      Tout += c0;
+      ncols -= c0;
+    }
     // the launch shape is tuned per block order (two 16-column passes with 2 rows
     // per warp measured best at n = 20,000: register pressure, not the second read
     // of the block, limits the wider pieces)
@@ -1397,6 +1425,7 @@ static void upload_dense(cbx_handle* h, Mme& m, const double* src, int64_t ng) {
   k_lowp_block<<<grid_for(ng * m.ld, 256, 8 * h->num_sms), 256, 0, s>>>(src, ng, m.ld, m.qshift, m.Qd32.p,
                                                                        m.Qlo32.p);
   h->launched("k_lowp_block");
+  m.fx_rows_ok = false;
 }
 
 // Dense Qinv (q x q, symmetric, row- or column-major alike).  Qinv == NULL uses

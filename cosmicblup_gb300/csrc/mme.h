@@ -54,6 +54,13 @@ struct Mme {
   DevBuf<float> Qd32;              // fl32(Qd - qshift)
   DevBuf<float> Qlo32;             // fl32(Qd - qshift - Qd32): with Qd32 the float-float block
   double qshift = 0.0;
+  // row scales of the Qd32 / Qlo32 planes for the fixed-point tensor-core
+  // refinement product (valid while fx_rows_ok), and its scratch
+  DevBuf<int32_t> fx_rowexp;
+  bool fx_rows_ok = false;
+  DevBuf<uint16_t> fx_bdig;
+  DevBuf<int32_t> fx_cexp;
+  DevBuf<double> fx_part;
   DevBuf<int32_t> gmap;            // ng -> u index
   DevBuf<int32_t> ginv;            // q -> dense index or -1
   Csr<double> Qs64;

@@ -249,3 +249,73 @@ extern "C" int cbx_selftest_dense_ff(cbx_handle* h, const double* Q, int64_t ng,
     CBX_CUDA(cudaStreamSynchronize(h->stream));
   });
 }
+
+// The fixed-point tensor-core product alone: Y (ng x S, row-major FP64) = Q V^T
+// with Q (ng x ld, row-major FP64, ld % 4 == 0) held as FP32 hi / lo planes and V
+// (S x ld, row-major FP64, S <= 32); reps > 0 also times that many products
+// (ms_out, mean, including the column-digit and reduce kernels).
+namespace {
+__global__ void k_transpose_cols(const double* __restrict__ V, int S, int64_t ld, int64_t ng, double* __restrict__ X) {
+  const int64_t total = ng * S;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t k = i / S;
+    const int c = (int)(i - k * S);
+    X[i] = V[(int64_t)c * ld + k];
+  }
+}
+__global__ void k_iota(int32_t* __restrict__ g, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    g[i] = (int32_t)i;
+}
+}  // namespace
+
+extern "C" int cbx_selftest_dense_fx(cbx_handle* h, const double* Q, int64_t ng, int64_t ld, const double* V,
+                                     int32_t S, int32_t reps, double* Y, double* ms_out) {
+  return cbx_guard(h, [&] {
+    CBX_REQUIRE(ng > 0 && ld >= ng && ld % 4 == 0 && S >= 1 && S <= 32, CBX_ERR_ARG, "bad shape");
+    CBX_CUDA(cudaSetDevice(h->device));
+    cbx::DevBuf<double> dQ, dV, dX, dY, part;
+    cbx::DevBuf<float> qh, ql;
+    cbx::DevBuf<int32_t> rowexp, gmap, cexp;
+    cbx::DevBuf<uint16_t> bdig;
+    dQ.resize((size_t)ng * ld);
+    dV.resize((size_t)S * ld);
+    dX.resize((size_t)ng * S);
+    dY.resize((size_t)ng * S);
+    qh.resize((size_t)ng * ld);
+    ql.resize((size_t)ng * ld);
+    rowexp.resize(ng);
+    gmap.resize(ng);
+    CBX_CUDA(cudaMemcpyAsync(dQ.p, Q, (size_t)ng * ld * 8, cudaMemcpyHostToDevice, h->stream));
+    CBX_CUDA(cudaMemcpyAsync(dV.p, V, (size_t)S * ld * 8, cudaMemcpyHostToDevice, h->stream));
+    k_split_hilo<<<1024, 256, 0, h->stream>>>(dQ.p, ng * ld, qh.p, ql.p);
+    h->launched("k_split_hilo");
+    k_transpose_cols<<<256, 256, 0, h->stream>>>(dV.p, S, ld, ng, dX.p);
+    h->launched("k_transpose_cols");
+    k_iota<<<64, 256, 0, h->stream>>>(gmap.p, ng);
+    h->launched("k_iota");
+    cbx::fx_row_scales(h, qh.p, ng, ld, rowexp.p);
+    auto run = [&] {
+      cbx::fx_product(h, qh.p, ql.p, rowexp.p, ng, ld, dX.p, S, 0, gmap.p, S, bdig, cexp, part, dY.p, S, nullptr);
+    };
+    run();
+    h->check_status("cbx_selftest_dense_fx");
+    if (reps > 0) {
+      cudaEvent_t a, b;
+      CBX_CUDA(cudaEventCreate(&a));
+      CBX_CUDA(cudaEventCreate(&b));
+      CBX_CUDA(cudaEventRecord(a, h->stream));
+      for (int i = 0; i < reps; ++i) run();
+      CBX_CUDA(cudaEventRecord(b, h->stream));
+      CBX_CUDA(cudaEventSynchronize(b));
+      float ms = 0;
+      CBX_CUDA(cudaEventElapsedTime(&ms, a, b));
+      if (ms_out) *ms_out = ms / reps;
+      cudaEventDestroy(a);
+      cudaEventDestroy(b);
+      h->check_status("cbx_selftest_dense_fx");
+    }
+    CBX_CUDA(cudaMemcpyAsync(Y, dY.p, (size_t)ng * S * 8, cudaMemcpyDeviceToHost, h->stream));
+    CBX_CUDA(cudaStreamSynchronize(h->stream));
+  });
+}

@@ -1,6 +1,8 @@
 """GPU test of the launch-shape autotuner: every candidate shape of every tuned
 kernel gives the same bits, so a run with tuning on reproduces one with tuning off
 exactly, and the decisions are reported."""
+import os
+
 import numpy as np
 import pytest
 
@@ -56,7 +58,10 @@ def test_tuning_changes_no_bits(handle, problem):
         assert np.array_equal(a, b)
         assert np.array_equal(a, c)
     kernels = {ln.split()[0] for ln in rep}
-    assert {"k_dense_ff", "k_gemv", "k_geno_zt", "k_geno_z"} <= kernels, rep
+    # the float-float refinement product is tuned when it takes the 16-column
+    # pieces, i.e. with the tensor-core fixed-point product switched off (CBX_FX=0)
+    tuned = {"k_gemv", "k_geno_zt", "k_geno_z"} | ({"k_dense_ff"} if os.environ.get("CBX_FX") == "0" else set())
+    assert tuned <= kernels, rep
     for ln in rep:
         ms = [float(t) for t in ln.split(" ms ")[1].split()]
         choice = int(ln.split(" choice ")[1].split()[0])
