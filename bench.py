@@ -67,7 +67,7 @@ CONFIGS = {
     # [5000, 40000], h2 ~ U(0.1, 0.6), mean + 10-level group; each one GRM +
     # eigen-bent G^-1 + REML (3 EM iterations), the batch sharing the GPU
     "c5": dict(name="batch96_gblup_n500-8000_m5000-40000", kind="batch", nprob=96, n_lo=500, n_hi=8000,
-               m_lo=5000, m_hi=40000, levels=10, max_iter=3, workers=16, seed=5000),
+               m_lo=5000, m_hi=40000, levels=10, max_iter=3, workers=16, seed=5000, mt_n=10000, mt_m=20000),
 }
 # DRAM bytes per launch of k_dense_tf32<64> from an ncu capture at n = 8,192
 # (1.0125 x the algorithmic bytes), scaled to a 20,000-row block by the block's bytes
@@ -362,6 +362,7 @@ def run_batch(args, cfg):
                       "sum_problem_s": reps.sum(sum(r.seconds for r in res))}
     if reps.rank != 0:
         return
+    mtr = run_multi_trait(cfg, reps.local_rank)
     line = {"metric": METRIC, "value": out["mixed"]["reml_iter_per_s_incl_setup"],
             "unit": "REML iter/s (batch, GRM + G^-1 + REML per problem)", "n_gpus": reps.world,
             "scaling": "strong",
@@ -370,10 +371,53 @@ def run_batch(args, cfg):
                        "n_range": [min(p.n for p in all_probs), max(p.n for p in all_probs)],
                        "m_range": [min(p.m for p in all_probs), max(p.m for p in all_probs)],
                        "parallelism": f"problems sharded round robin over {reps.world} GPU(s)"},
-            "batch": out, "mixed_vs_fp64": out["fp64"]["wall_s"] / out["mixed"]["wall_s"],
+            "batch": out, "multi_trait": mtr,
+            "mixed_vs_fp64": out["fp64"]["wall_s"] / out["mixed"]["wall_s"],
             "workers_speedup": out["mixed_1worker"]["wall_s"] / out["mixed"]["wall_s"],
             "setup": {"synthetic_data_s": gen_s}}
     print(json.dumps(line))
+
+
+def run_multi_trait(cfg, device) -> dict:
+    """The batch config's dense 3-trait GBLUP: n = 10,000 genotyped animals (m = 20,000
+    SNPs), genetic correlations (0.5, -0.3, 0.2), residual correlations 0.1, mean + sex.
+    GRM and eigen-bent G^-1 on the device, then MvEigenVce (projection, eigen-EM) and
+    the Kronecker multi-trait MME solve, all FP64; host-clock seconds of each call."""
+    import ctypes as C
+    from cosmicblup_gb300 import Handle, MvEigenVce, MvOptions, invert_psd, solve_multi_trait
+    from cosmicblup_gb300._lib import lib, ptr
+    from cosmicblup_gb300.synth import simulate_bed, simulate_mt_records
+    n, m, seed = cfg["mt_n"], cfg["mt_m"], cfg["seed"] + 7000
+    rg = np.array([[1.0, 0.5, -0.3], [0.5, 1.0, 0.2], [-0.3, 0.2, 1.0]])
+    sg, se = np.sqrt([0.3, 0.4, 0.5]), np.sqrt([0.7, 0.6, 0.5])
+    Vg = rg * np.outer(sg, sg)
+    Ve = (np.full((3, 3), 0.1) + 0.9 * np.eye(3)) * np.outer(se, se)
+    t0 = time.perf_counter()
+    bed, _ = simulate_bed(n, m, seed=seed, p_lo=0.01, miss=0.02)
+    rec = simulate_mt_records(bed, n, m, seed=seed + 1, Vg=Vg, Ve=Ve)
+    gen_s = time.perf_counter() - t0
+    h = Handle(device)
+    bedarr = np.frombuffer(bed, dtype=np.uint8)
+    s2pq, nval = C.c_double(0), C.c_int64(0)
+    t0 = time.perf_counter()
+    h.check(lib().cbx_grm_bed(h.raw, ptr(bedarr), bedarr.size, n, m, C.c_float(0.01), 1, 2048, None, None,
+                              None, C.byref(s2pq), C.byref(nval)))
+    invert_psd(h, None, n, download=False)
+    h.sync()
+    ginv_s = time.perf_counter() - t0
+    v = MvEigenVce(h, MvOptions())
+    t0 = time.perf_counter()
+    v.prepare(rec["Y"], rec["X"], None)
+    v.runNullModel()
+    vce_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    sol = solve_multi_trait(h, rec["Y"], rec["X"], v.getVg(), v.getVe(), Ginv=None)
+    solve_s = time.perf_counter() - t0
+    return {"n": n, "m": m, "traits": 3, "synthetic_data_s": gen_s, "grm_and_ginv_s": ginv_s,
+            "vce_s": vce_s, "em_iterations": v.iterations, "converged": v.converged, "solve_s": solve_s,
+            "Vg": v.getVg().tolist(), "Ve": v.getVe().tolist(), "Vg_true": Vg.tolist(), "Ve_true": Ve.tolist(),
+            "u_abs_max": float(np.abs(sol["u"]).max()),
+            "precision": "fp64 (eigen-EM and dense Cholesky of the Kronecker MME, as the reference)"}
 
 
 def run_geno(h, bed, n, m, seed, hbm_peak, want_host, reps: int = 5) -> dict:
@@ -435,7 +479,7 @@ def run_gpu(args, cfg):
     world, rank, local = reps.world, reps.rank, reps.local_rank
     hbm_peak, bf16_peak, peak_src = peaks()
     n, m = cfg["n"], cfg["m"]
-    G_PROBES = cfg.get("grad_probes", 0)
+    G_PROBES = cfg.get("grad_probes", 0) if args.grad_probes is None else args.grad_probes
     dense = bool(cfg.get("dense"))
     mode = MODE_DENSE if dense else MODE_EM
     phases = {}
@@ -487,11 +531,12 @@ def run_gpu(args, cfg):
     d2h_bytes = 8 * (p + q) + 16 + (16 if G_PROBES else 0)
 
     def step(r, prec):
-        """One REML iteration, then the gradient at its starting point."""
-        vu0, ve0 = r.var_u, r.var_e
-        info = r.run_iteration()
-        g = reml_gradient(r.mme, vu0, ve0, nprobe=G_PROBES, precision=prec) if G_PROBES else None
-        return info, g
+        """One REML iteration, then the gradient at its starting point (one call:
+        the gradient's probes join the iteration's data + probe block)."""
+        if not G_PROBES:
+            return r.run_iteration(), None
+        info = r.run_iteration(grad_probes=G_PROBES)
+        return info, {"grad": info["grad"], "trace": info["grad_trace"], "pcg_iters": info["grad_pcg_iters"]}
 
     # ---- mixed-precision steps (the headline) ----
     r = AIREML(dm, 0.5, 0.5, RemlConfig.default(mode=mode, precision=MIXED))
@@ -664,8 +709,9 @@ def run_gpu(args, cfg):
         l2_note = f"dense exact step on {p + q}-order FP64 matrices (32 MB each); cache-resident"
     step_desc = ("one dense exact AI-REML step (FP64 Cholesky, P, AI traces, logL-checked halving)" if dense else
                  "one EM+Hutchinson AI-REML iteration (data solve + adaptive probe solves, relres 1e-10)"
-                 + (f", then the REML gradient at its starting point from {G_PROBES} probes (the iteration's "
-                    f"probe solves reused)" if G_PROBES else ""))
+                 + (f", then the REML gradient at its starting point from {G_PROBES} probes (cbx_reml_iterate_grad: "
+                    f"the gradient's first probes, up to 79, solved in the iteration's data + probe block, the "
+                    f"iteration's estimator using only the probes its stopping rule selects)" if G_PROBES else ""))
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
@@ -692,13 +738,14 @@ def run_gpu(args, cfg):
         "e2e": e2e,
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm",
-                     "kernel": "k_dense_tf32<64> (tcgen05 3xTF32, dense H^-1 / G^-1 block x up to 64 columns)",
+                     "kernel": ("k_dense_tf32 (tcgen05 3xTF32, dense H^-1 / G^-1 block x the populated columns of "
+                                "the block, up to 80 of a 128-wide block)"),
                      "achieved": ach, "peak": hbm_peak, "unit": "GB/s",
                      "frac": (ach / hbm_peak) if ach else None, "traffic": TRAFFIC_BYTES.get(n),
                      "peak_source": peak_src, "launches": dl, "avg_launch_ms": dms / dl if dl else None,
                      "step_dense_bytes_GBps": (dbytes + ffbytes) / (ms_local * 1e-3) / 1e9,
                      "step_hbm_frac": (dbytes + ffbytes) / (ms_local * 1e-3) / 1e9 / hbm_peak,
-                     "step_note": "the step's dense-block bytes (FP32 products and float-float "
+                     "step_note": "the step's dense-block bytes (FP32 products and FP64-accurate "
                                   "refinement products) over the whole step time; sparse and vector "
                                   "traffic not counted"},
         "cpu_baseline": cpu,
@@ -718,6 +765,8 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=None,
                     help="FP64 comparison steps (default: --steps)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--grad-probes", type=int, default=None,
+                    help="probes of the gradient in each step (default: the config's)")
     args = ap.parse_args()
     cfg = CONFIGS[args.config]
     if args.impl == "reference":

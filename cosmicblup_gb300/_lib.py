@@ -61,6 +61,9 @@ SIGNATURES = [
     ("cbx_reml_config_default", None, [C.c_void_p]),
     ("cbx_reml_iterate", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_double),
                                    C.POINTER(C.c_double), C.c_void_p]),
+    ("cbx_reml_iterate_grad", C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(C.c_double),
+                                        C.POINTER(C.c_double), C.c_void_p, C.c_void_p, C.POINTER(C.c_double),
+                                        C.POINTER(C.c_int64)]),
     ("cbx_reml_solve", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                  C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_void_p, C.c_void_p]),
     ("cbx_profile_enable", C.c_int, [C.c_void_p, C.c_int32]),

@@ -37,9 +37,12 @@ constexpr int A_BYTES = 128 * KB * 4;  // 16 KB
 constexpr int THREADS = 320;
 constexpr uint32_t TMEM_ALLOC = 512;
 
-template <int S>
+// S: the output row stride (the solver's block width); NCM: the most populated
+// columns one launch multiplies (S, or 80 for the 128-wide block, whose TMEM
+// budget holds two 2 x 80-column accumulators beside the A_lo stages).
+template <int S, int NCM = S>
 struct Layout {
-  static constexpr int B_BYTES = S * KB * 4;             // S rows of 128 bytes
+  static constexpr int B_BYTES = NCM * KB * 4;           // NCM rows of 128 bytes
   // stage: the Qd tile (its tf32 lo part goes to TMEM), then the vector tile
   // as B_hi rows followed by B_lo rows (one N = 2 nc descriptor covers both)
   static constexpr int OFF_B = A_BYTES;
@@ -48,9 +51,9 @@ struct Layout {
   static_assert(STAGE % 1024 == 0, "stages must stay 1024-byte aligned for SWIZZLE_128B");
   static constexpr int OFF_BAR = NSTAGE * STAGE;
   static constexpr int SMEM = OFF_BAR + 256 + 1024;     // + alignment slack
-  // TMEM: two accumulator buffers of 2S columns, then 32 columns (one K step
+  // TMEM: two accumulator buffers of 2 NCM columns, then 32 columns (one K step
   // of tf32 lo values) per stage
-  static constexpr uint32_t ALO_COL = 4 * S;
+  static constexpr uint32_t ALO_COL = 4 * NCM;
   static_assert(ALO_COL + 32 * NSTAGE <= TMEM_ALLOC, "tensor memory budget");
   static_assert(NSTAGE <= 12, "barrier arrays");
 };
@@ -129,13 +132,13 @@ __device__ __forceinline__ float4 lo4(const float4& v) {
   return lo;
 }
 
-template <int S>
+template <int S, int NCM = S>
 __global__ void __launch_bounds__(THREADS, 1)
     k_dense_tf32(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int ng,
                  int ksteps, int total, int per, int nslot, float* __restrict__ Tpart, const int* active,
                  int* status, int nc) {
   if (active && *active == 0) return;
-  using LY = Layout<S>;
+  using LY = Layout<S, NCM>;
   constexpr int NSTAGE = LY::NSTAGE;
   extern __shared__ uint8_t dsm_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(dsm_raw) + 1023) & ~uintptr_t(1023));
@@ -202,7 +205,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         const uint32_t b = c & 1;
         if (!mbar_wait(&bars->acc_empty[b], ((c >> 1) & 1) ^ 1, abort_flag)) { ok = false; break; }
         tc_fence_after();
-        const uint32_t d = tmem + b * 2 * S;
+        const uint32_t d = tmem + b * 2 * NCM;
         for (int k = k0; k < k1; ++k, ++g) {
           const uint32_t s = g % NSTAGE;
           if (!mbar_wait(&bars->conv[s], (g / NSTAGE) & 1, abort_flag)) { ok = false; break; }
@@ -281,37 +284,37 @@ __global__ void __launch_bounds__(THREADS, 1)
       const uint32_t b = c & 1;
       if (!mbar_wait_idle(&bars->acc_full[b], (c >> 1) & 1, abort_flag, 64)) { ok = false; break; }
       tc_fence_after();
-      // columns [0, nc): A B_hi; [nc, 2 nc): A B_lo + A_lo B_hi; nc <= S
-      float out[S];
-      const uint32_t ta = tmem + (uint32_t(q * 32) << 16) + b * 2 * S;
+      // columns [0, nc): A B_hi; [nc, 2 nc): A B_lo + A_lo B_hi; nc <= NCM.  Each
+      // 16-column group is stored as it is read; columns nc .. S - 1 are zero.
+      const uint32_t ta = tmem + (uint32_t(q * 32) << 16) + b * 2 * NCM;
+      const int row = mt * 128 + q * 32 + lane;
+      float4* dst = reinterpret_cast<float4*>(Tpart + ((int64_t)ks * ng + (row < ng ? row : 0)) * S);
 #pragma unroll
-      for (int j0 = 0; j0 < S; j0 += 16) {
+      for (int j0 = 0; j0 < NCM; j0 += 16) {
         if (j0 < nc) {
           uint32_t r1[16], r2[16];
           tmem_ld16(ta + j0, r1);
           tmem_ld16(ta + nc + j0, r2);
           tmem_ld_wait();
+          if (row < ng) {
 #pragma unroll
-          for (int j = 0; j < 16; ++j) out[j0 + j] = __uint_as_float(r1[j]) + __uint_as_float(r2[j]);
-        } else {
-#pragma unroll
-          for (int j = 0; j < 16; ++j) out[j0 + j] = 0.0f;
+            for (int j = 0; j < 4; ++j)
+              dst[j0 / 4 + j] = make_float4(__uint_as_float(r1[4 * j]) + __uint_as_float(r2[4 * j]),
+                                            __uint_as_float(r1[4 * j + 1]) + __uint_as_float(r2[4 * j + 1]),
+                                            __uint_as_float(r1[4 * j + 2]) + __uint_as_float(r2[4 * j + 2]),
+                                            __uint_as_float(r1[4 * j + 3]) + __uint_as_float(r2[4 * j + 3]));
+          }
         }
       }
       tc_fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(&bars->acc_empty[b]);
-      const int row = mt * 128 + q * 32 + lane;
       if (row < ng) {
-        float4* dst = reinterpret_cast<float4*>(Tpart + ((int64_t)ks * ng + row) * S);
-#pragma unroll
-        for (int j = 0; j < S / 4; ++j)
-          dst[j] = make_float4(out[4 * j], out[4 * j + 1], out[4 * j + 2], out[4 * j + 3]);
+        for (int j = nc / 4; j < S / 4; ++j) dst[j] = make_float4(0.f, 0.f, 0.f, 0.f);
         if (k1 == ksteps) {
           // the tile ends here: its slots after this one hold nothing
           for (int z = ks + 1; z < nslot; ++z) {
             float4* zd = reinterpret_cast<float4*>(Tpart + ((int64_t)z * ng + row) * S);
-#pragma unroll
             for (int j = 0; j < S / 4; ++j) zd[j] = make_float4(0.f, 0.f, 0.f, 0.f);
           }
         }
@@ -355,10 +358,11 @@ int dense_tc_stream_k(int64_t ng, int64_t ld, int num_sms, int* grid, int* per) 
 
 void dense_tc(cbx_handle* h, const float* Qd, int64_t ng, int64_t ld, const float* Vt, int S, int ksplit, float* Tpart,
               const int* active, int ncols) {
-  CBX_REQUIRE(S == 16 || S == 32 || S == 64, CBX_ERR_ARG, "dense_tc supports 16, 32 or 64 columns");
+  CBX_REQUIRE(S == 16 || S == 32 || S == 64 || S == 128, CBX_ERR_ARG, "dense_tc supports 16, 32, 64 or 128 columns");
   // the MMAs and the lo conversion run on the populated columns, rounded up
   // to the MMA granularity of 16; the output's other columns are written as 0
   const int nc = std::min(S, std::max(16, (ncols + 15) / 16 * 16));
+  CBX_REQUIRE(S != 128 || nc <= 80, CBX_ERR_ARG, "the 128-wide block product takes at most 80 populated columns");
   CBX_REQUIRE(ld % 4 == 0, CBX_ERR_ARG, "row pitch must be a multiple of 4");
   const CUtensorMap ma = make_map_f32(Qd, ld, ng, 128);
   const CUtensorMap mb = make_map_f32(Vt, ld, S, nc);
@@ -368,7 +372,12 @@ void dense_tc(cbx_handle* h, const float* Qd, int64_t ng, int64_t ld, const floa
   int grid = 0, per = 0;
   const int nslot = stream_k(ng, ld, h->num_sms, &grid, &per);
   CBX_REQUIRE(nslot == ksplit, CBX_ERR_ARG, "partial slot count does not match dense_tc_ksplit");
-  if (S == 64) {
+  if (S == 128) {
+    constexpr int SM = dtc::Layout<128, 80>::SMEM;
+    ensure_smem((const void*)dtc::k_dense_tf32<128, 80>, SM, h->device);
+    dtc::k_dense_tf32<128, 80><<<grid, dtc::THREADS, SM, h->stream>>>(ma, mb, (int)ng, ksteps, total, per, nslot,
+                                                                      Tpart, active, h->status.p, nc);
+  } else if (S == 64) {
     constexpr int SM = dtc::Layout<64>::SMEM;
     ensure_smem((const void*)dtc::k_dense_tf32<64>, SM, h->device);
     dtc::k_dense_tf32<64><<<grid, dtc::THREADS, SM, h->stream>>>(ma, mb, (int)ng, ksteps, total, per, nslot, Tpart,

@@ -556,10 +556,12 @@ int product_from_vt(cbx_handle* h, const sv::OpView<T>& op, Workspace<T, S>& w, 
     CBX_CUDA(cudaEventCreate(&pr.b));
     CBX_CUDA(cudaEventRecord(pr.a, s));
   }
-  if ((S == 16 || S == 32 || S == 64) && use_dense_tc()) {
+  if ((S == 16 || S == 32 || S == 64 || S == 128) && use_dense_tc()) {
     tsplit = dense_tc_ksplit(op.ng, op.ld, h->num_sms);
     dense_tc(h, reinterpret_cast<const float*>(op.Qd), op.ng, op.ld, reinterpret_cast<const float*>(w.Vt.p), S,
              tsplit, reinterpret_cast<float*>(w.Tout.p), active, ncols);
+  } else if constexpr (S == 128) {
+    throw Error(CBX_ERR_UNSUPPORTED, "the 128-wide block needs the tensor-core product (CBX_DENSE_TC=1)");
   } else if (S == 1) {
     // rows per warp x loads in flight per lane, tuned per block order (all shapes
     // accumulate each row in the same order)
@@ -1028,7 +1030,7 @@ struct Solver : public SolverBase {
 
 template <int S>
 static Solver<S>& solver_for(Mme& m) {
-  constexpr int idx = S == 1 ? 0 : S == 2 ? 1 : S == 4 ? 2 : S == 8 ? 3 : S == 16 ? 4 : S == 32 ? 5 : 6;
+  constexpr int idx = S == 1 ? 0 : S == 2 ? 1 : S == 4 ? 2 : S == 8 ? 3 : S == 16 ? 4 : S == 32 ? 5 : S == 64 ? 6 : 7;
   if (!m.solvers[idx]) m.solvers[idx].reset(new Solver<S>());
   return *static_cast<Solver<S>*>(m.solvers[idx].get());
 }
@@ -1073,11 +1075,13 @@ void pcg_solve(cbx_handle* h, double lam, int ncols, const double* B_cm, double*
   Mme& m = *h->mme;
   CBX_REQUIRE(m.has_dense || m.has_sparse, CBX_ERR_STATE, "Qinv not set (cbx_mme_set_qinv_*)");
   res = PcgResult{};
-  // Mixed precision takes up to 64 columns per block: its PCG bulk reads the
-  // FP32 block once per iteration for all of them, and the FP64-class
-  // refinement products run on the populated columns only.  The FP64 solver's
-  // product is FP64-bound, so it stays at 32.
-  const int chunk = precision != 0 ? 64 : 32;
+  // Mixed precision takes up to 64 columns per block, or up to 80 in a
+  // 128-wide block when there are more than 64: its PCG bulk reads the FP32
+  // block once per iteration for all of them (the tensor-core product takes at
+  // most 80 populated columns), and the FP64-class refinement products run on
+  // the populated columns only.  The FP64 solver's product is FP64-bound, so it
+  // stays at 32.
+  const int chunk = precision != 0 ? (ncols > 64 ? 80 : 64) : 32;
   for (int c0 = 0; c0 < ncols; c0 += chunk) {
     const int nc = std::min(chunk, ncols - c0);
     PcgResult r;
@@ -1087,14 +1091,15 @@ void pcg_solve(cbx_handle* h, double lam, int ncols, const double* B_cm, double*
     double* ro = carry && carry->r_out ? carry->r_out + (int64_t)c0 * m.dim : nullptr;
     const double dl = carry ? carry->dlam : 0.0;
 #define CBX_CHUNK(W) solve_chunk<W>(h, m, lam, nc, B, X, use_x0, tol, maxit, abs_tol, precision, r, rp, dl, ro)
-    switch (block_width(nc, chunk)) {
+    switch (block_width(nc, 128)) {
       case 1: CBX_CHUNK(1); break;
       case 2: CBX_CHUNK(2); break;
       case 4: CBX_CHUNK(4); break;
       case 8: CBX_CHUNK(8); break;
       case 16: CBX_CHUNK(16); break;
       case 32: CBX_CHUNK(32); break;
-      default: CBX_CHUNK(64); break;
+      case 64: CBX_CHUNK(64); break;
+      default: CBX_CHUNK(128); break;
     }
 #undef CBX_CHUNK
     res.iters.insert(res.iters.end(), r.iters.begin(), r.iters.end());

@@ -116,7 +116,7 @@ struct Mme {
     fwd.valid = false;
   }
   // persistent solver workspaces, indexed by log2 of the RHS block width
-  std::unique_ptr<SolverBase> solvers[7];
+  std::unique_ptr<SolverBase> solvers[8];
   // scratch column-major buffers of the C ABI
   DevBuf<double> io_b, io_x;
 };

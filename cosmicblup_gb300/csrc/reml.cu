@@ -428,8 +428,13 @@ static void probe_values(cbx_handle* h, Mme& m, double lam, int c0, int k, bool 
 // systems share the matrix, so one read of the dense block per PCG iteration
 // serves them all).  Results per column are those of separate solves: every
 // column runs its own CG recurrence and refinement.  The iteration leaves its
-// forward state (m.fwd) for a gradient at its starting point.
-static void em_iteration(cbx_handle* h, const RemlConfigI& cfg, double& vu, double& ve, IterInfo& info) {
+// forward state (m.fwd) for a gradient at its starting point.  `extra` > 0 (a
+// gradient from that many probes follows at this point) widens the block to
+// the first `extra` probes, up to 79 (16-probe batches; the block's tensor-core
+// product takes 80 columns), so that the gradient reuses their solves; the
+// estimator still uses exactly the probes its stopping rule selects.
+static void em_iteration(cbx_handle* h, const RemlConfigI& cfg, double& vu, double& ve, IterInfo& info,
+                         int extra = 0) {
   Mme& m = *h->mme;
   cudaStream_t s = h->stream;
   const int64_t p = m.p, q = m.q, dim = m.dim, n = m.n_rec;
@@ -449,7 +454,7 @@ static void em_iteration(cbx_handle* h, const RemlConfigI& cfg, double& vu, doub
   if (min_s <= 0) min_s = 10;
   if (max_s < min_s) max_s = min_s;
   const int batch = 16;  // max(16, 4 * threads) with one thread
-  probe_store(h, m, cfg.seed, max_s);
+  probe_store(h, m, cfg.seed, std::max(max_s, extra));
   // column 0 of em_B: W'y
   CBX_CUDA(cudaMemcpyAsync(m.em_B.p, m.rhs.p, dim * sizeof(double), cudaMemcpyDeviceToDevice, s));
 
@@ -479,11 +484,15 @@ static void em_iteration(cbx_handle* h, const RemlConfigI& cfg, double& vu, doub
 
   int done = 0;
   Group g0 = make_group(0);
+  // probes solved in the data block: the first group, or the gradient's first
+  // `extra` probes when they are more (whole batches, 79 at most)
+  const int kx = std::max(g0.k, std::min(extra, 79) / batch * batch);
+  for (int b = g0.k; b < kx; b += batch) probe_batch(h, m, cfg.seed, b, std::min(batch, kx - b));
   // --- 1. the data solve (with the first probe group in mixed precision)
   const bool data_warm = m.has_last;
-  const bool merge = mixed && data_warm == probes_warm(m, 0, g0.k);
+  const bool merge = mixed && data_warm == probes_warm(m, 0, kx);
   if (merge) {
-    const int k = g0.k, nc = 1 + k;
+    const int k = kx, nc = 1 + k;
     DevBuf<double> X, R;
     X.resize((size_t)dim * nc);
     R.resize((size_t)dim * nc);
@@ -549,7 +558,8 @@ static void em_iteration(cbx_handle* h, const RemlConfigI& cfg, double& vu, doub
   while (done < max_s && !stop) {
     Group g = first ? std::move(g0) : make_group(done);
     const int k = g.k;
-    if (!(first && merge)) {
+    // groups inside the data block were solved there
+    if (!(merge && done + k <= kx)) {
       PcgResult pr;
       probe_solve(h, m, lam, done, k, cfg.precision, cfg.pcg_tol, cfg.pcg_max_iter, pr);
       if (h->trace_on) h->trace_mark("#em: probe solve");
@@ -578,6 +588,11 @@ static void em_iteration(cbx_handle* h, const RemlConfigI& cfg, double& vu, doub
         if (std::abs(mean) > 1e-12 && (se / std::abs(mean)) < 0.05) { stop = true; break; }
       }
     }
+  }
+  if (merge && kx > solved) {
+    // the probes solved for a following gradient: their values too
+    probe_values(h, m, lam, solved, kx - solved, mixed);
+    solved = kx;
   }
   const double tr = tsum / done;
   // --- 5. updates (vce.cpp:1554-1569)
@@ -1251,7 +1266,8 @@ static bool ai_data_step(cbx_handle* h, double& vu_io, double& ve_io, IterInfo& 
   return false;
 }
 
-static void reml_iterate(cbx_handle* h, const RemlConfigI& cfg, double& vu, double& ve, IterInfo& info) {
+static void reml_iterate(cbx_handle* h, const RemlConfigI& cfg, double& vu, double& ve, IterInfo& info,
+                         int extra = 0) {
   Mme& m = *h->mme;
   if (cfg.mode == 3) {
     if (ai_data_step(h, vu, ve, info)) return;
@@ -1259,7 +1275,7 @@ static void reml_iterate(cbx_handle* h, const RemlConfigI& cfg, double& vu, doub
     const bool dense = cfg.mode == 2 || (cfg.mode == 0 && m.dim < 5000);
     if (dense && dense_exact_step(h, vu, ve, info)) return;
   }
-  em_iteration(h, cfg, vu, ve, info);
+  em_iteration(h, cfg, vu, ve, info, extra);
 }
 
 }  // namespace cbx
@@ -1316,6 +1332,24 @@ extern "C" int cbx_reml_iterate(cbx_handle* h, const cbx_reml_config* cfg, doubl
     IterInfo it;
     reml_iterate(h, to_cfg(cfg), *var_u, *var_e, it);
     to_info(it, info);
+  });
+}
+
+extern "C" int cbx_reml_iterate_grad(cbx_handle* h, const cbx_reml_config* cfg, int32_t nprobe, double* var_u,
+                                     double* var_e, cbx_reml_iter_info* info, double* grad, double* trace,
+                                     int64_t* grad_pcg_iters) {
+  return cbx_guard(h, [&] {
+    CBX_REQUIRE(h->mme, CBX_ERR_STATE, "call cbx_mme_create and cbx_mme_set_qinv_* first");
+    CBX_REQUIRE(var_u && var_e && *var_u > 0 && *var_e > 0, CBX_ERR_ARG, "variances must be positive");
+    CBX_REQUIRE(nprobe > 0 && grad, CBX_ERR_ARG, "nprobe must be positive and grad non-null");
+    CBX_CUDA(cudaSetDevice(h->device));
+    const RemlConfigI c = to_cfg(cfg);
+    const double vu0 = *var_u, ve0 = *var_e;
+    IterInfo it;
+    reml_iterate(h, c, *var_u, *var_e, it, nprobe);
+    to_info(it, info);
+    cbx::reml_gradient(h, vu0, ve0, nprobe, c.seed, 0, c.precision, c.pcg_tol, c.pcg_max_iter, grad, trace,
+                       grad_pcg_iters);
   });
 }
 

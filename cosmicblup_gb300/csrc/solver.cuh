@@ -932,12 +932,12 @@ __global__ void __launch_bounds__(NT) k_update(OpView<T> op, const Col* __restri
     }
     arr.add(r, r);
     if (i >= op.p) {
-      T z;
+      // z is loaded for every column (a load on one side of a branch that differs
+      // between the lanes of a warp measured twice as slow)
+      T z = Z[idx];
       if (upd) {
         z = op.dinv[i - op.p] * r;
         Z[idx] = z;
-      } else {
-        z = Z[idx];
       }
       arz.add(r, z);
     }

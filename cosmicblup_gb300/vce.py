@@ -60,13 +60,25 @@ class AIREML:
         self.var_e = float(var_e)
         self.var_u = float(vars_u[0] if np.ndim(vars_u) else vars_u)
 
-    def run_iteration(self) -> dict:
+    def run_iteration(self, grad_probes: int = 0) -> dict:
+        """One REML iteration.  grad_probes > 0 also returns the REML gradient at
+        the iteration's starting point from that many probes (cbx_reml_iterate_grad:
+        one block solve serves both) as d["grad"], d["grad_trace"], d["grad_pcg_iters"]."""
         vu, ve = C.c_double(self.var_u), C.c_double(self.var_e)
         info = RemlIterInfo()
-        self.mme.h.check(lib().cbx_reml_iterate(self.mme.h.raw, C.byref(self.config), C.byref(vu),
-                                                C.byref(ve), C.byref(info)))
+        if grad_probes > 0:
+            g = np.zeros(2)
+            tr, it = C.c_double(0), C.c_int64(0)
+            self.mme.h.check(lib().cbx_reml_iterate_grad(self.mme.h.raw, C.byref(self.config), int(grad_probes),
+                                                         C.byref(vu), C.byref(ve), C.byref(info), ptr(g),
+                                                         C.byref(tr), C.byref(it)))
+        else:
+            self.mme.h.check(lib().cbx_reml_iterate(self.mme.h.raw, C.byref(self.config), C.byref(vu),
+                                                    C.byref(ve), C.byref(info)))
         self.var_u, self.var_e = vu.value, ve.value
         d = info.as_dict()
+        if grad_probes > 0:
+            d.update(grad=g, grad_trace=tr.value, grad_pcg_iters=it.value)
         self.history.append(d)
         return d
 

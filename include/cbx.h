@@ -411,6 +411,17 @@ int cbx_mt_solve(cbx_handle* h, int64_t n, int32_t t, int64_t p, const double* Y
 int cbx_reml_gradient(cbx_handle* h, double var_u, double var_e, int32_t nprobe, int32_t seed,
                       int32_t exact_trace, int32_t precision, double pcg_tol, int32_t pcg_maxit,
                       double* grad, double* trace, int64_t* pcg_iters);
+/* One REML iteration (as cbx_reml_iterate) followed by the REML gradient at its
+ * starting point from nprobe probes (as cbx_reml_gradient with cfg's seed,
+ * precision and PCG settings).  In the EM branch with mixed precision the
+ * gradient's first probes (up to 79, whole 16-probe batches) join the
+ * iteration's data + probe block, so one multi-RHS solve serves both; the
+ * iteration's estimator still uses exactly the probes its stopping rule
+ * selects.  grad (2) gets the score; info, trace and grad_pcg_iters (CG
+ * iterations of the gradient's own solves) may be NULL. */
+int cbx_reml_iterate_grad(cbx_handle* h, const cbx_reml_config* cfg, int32_t nprobe, double* var_u,
+                          double* var_e, cbx_reml_iter_info* info, double* grad, double* trace,
+                          int64_t* grad_pcg_iters);
 /* REML log-likelihood by dense Cholesky of the LHS (dim <= 24,576): with a dense
  * Qinv, run_dense_exact_step's compute_logL (src/core/vce.cpp:2974-3007); with a
  * split Qinv (ssGBLUP), calc_logL_internal (:3533-3588), which omits the constant

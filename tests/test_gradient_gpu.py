@@ -147,3 +147,36 @@ def test_exact_gradient_matches_finite_differences_ssgblup(handle):
         fd.append((lp - lm) / (2 * hk))
     fd = np.array(fd)
     np.testing.assert_allclose(g, fd, rtol=1e-5, atol=1e-6 * np.abs(fd).max())
+
+
+@pytest.mark.parametrize("precision", [0, MIXED])
+def test_iteration_with_gradient_in_one_block(handle, prob, precision):
+    """cbx_reml_iterate_grad: in mixed precision the gradient's 64 probes join the
+    iteration's data + probe block (65 columns, the 128-wide solver), so the
+    gradient solves nothing; the iteration (same probes selected by its
+    estimator) and the gradient equal those of the separate calls to the
+    tolerance of their solves, and the iteration matches the oracle."""
+    from cosmicblup_gb300 import AIREML, RemlConfig
+    from cosmicblup_gb300.vce import MODE_EM
+    vu, ve = 0.45, 0.55
+    scale = max(prob["n"] / (2 * vu), prob["n"] / (2 * ve))
+    r1 = AIREML(dev(handle, prob), vu, ve, RemlConfig.default(mode=MODE_EM, precision=precision))
+    d1 = r1.run_iteration(grad_probes=64)
+    if precision == MIXED:
+        assert d1["grad_pcg_iters"] == 0
+    dm2 = dev(handle, prob)
+    r2 = AIREML(dm2, vu, ve, RemlConfig.default(mode=MODE_EM, precision=precision))
+    d2 = r2.run_iteration()
+    g2 = reml_gradient(dm2, vu, ve, nprobe=64, seed=42, precision=precision)
+    assert d1["probes"] == d2["probes"]
+    assert abs(r1.var_u - r2.var_u) <= 1e-9 * r2.var_u and abs(r1.var_e - r2.var_e) <= 1e-9 * r2.var_e
+    np.testing.assert_allclose(d1["grad"], g2["grad"], rtol=1e-8, atol=1e-8 * scale)
+    assert abs(d1["grad_trace"] - g2["trace"]) <= 1e-8 * abs(g2["trace"])
+    o = OracleREML(prob["mme"], prob["Gi"], vu, ve)
+    o.em_iteration()
+    assert abs(r1.var_u - o.var_u) <= 1e-6 * o.var_u and abs(r1.var_e - o.var_e) <= 1e-6 * o.var_e
+    # a second combined call continues warm from the 65-column block
+    d3 = r1.run_iteration(grad_probes=64)
+    if precision == MIXED:
+        assert d3["grad_pcg_iters"] == 0
+    assert np.all(np.isfinite(d3["grad"]))
