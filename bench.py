@@ -637,9 +637,11 @@ def run_gpu(args, cfg):
             else:
                 dm2.set_qinv_dense(None)
             r2 = AIREML(dm2, *state, RemlConfig.default(mode=mode, precision=MIXED, max_iter=1))
-            r2.solve()
             if G_PROBES:
-                reml_gradient(dm2, *state, nprobe=G_PROBES, precision=MIXED)
+                # the iteration and its gradient in one call; the data solve comes back
+                r2.run_iteration(grad_probes=G_PROBES, solution=True)
+            else:
+                r2.solve()
         e2e_rate, _ = job_rate(e2e_steps, h.timer_stop(), reps)
     e2e = {"value": e2e_rate, "unit": UNIT,
            "h2d_bytes_per_step": int(h2d_bytes), "d2h_bytes_per_step": int(d2h_bytes)}

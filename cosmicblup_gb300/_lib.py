@@ -63,7 +63,7 @@ SIGNATURES = [
                                    C.POINTER(C.c_double), C.c_void_p]),
     ("cbx_reml_iterate_grad", C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(C.c_double),
                                         C.POINTER(C.c_double), C.c_void_p, C.c_void_p, C.POINTER(C.c_double),
-                                        C.POINTER(C.c_int64)]),
+                                        C.POINTER(C.c_int64), C.c_void_p]),
     ("cbx_reml_solve", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                  C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_void_p, C.c_void_p]),
     ("cbx_profile_enable", C.c_int, [C.c_void_p, C.c_int32]),

@@ -606,6 +606,10 @@ void matvec(cbx_handle* h, const sv::OpView<T>& op, Workspace<T, S>& w, const T*
             const T* P, double* pq_part, const int* active, bool ff = false, int ncols = S) {
   cudaStream_t s = h->stream;
   int tsplit = 1;
+  // columns computed: the populated ones rounded up to whole 32-column groups
+  // (the 128-wide block computes three groups)
+  const int ncp = std::min(S, (ncols + 31) / 32 * 32);
+  CBX_REQUIRE(S != 128 || ncols <= 96, CBX_ERR_ARG, "the 128-wide block takes at most 96 populated columns");
   // The FP32 and float-float products use the shifted copies and add
   // qshift * (column sums) back; the FP64 product uses the block itself.
   const double* colsum = op.Qd ? w.colsum.p : nullptr;
@@ -633,21 +637,23 @@ void matvec(cbx_handle* h, const sv::OpView<T>& op, Workspace<T, S>& w, const T*
     }
   } else {
     // FP32: gather the dense-block rows, their FP64 column sums, the product
-    sv::k_gather_t<T, S><<<grid_for(S * op.ld, 256, 16 * h->num_sms), 256, 0, s>>>(X, w.Vt.p, op.p, op.ng, op.ld,
-                                                                               op.gmap, active);
+    // (the populated 32-column groups only)
+    sv::k_gather_t<T, S><<<grid_for(ncp * op.ld, 256, 16 * h->num_sms), 256, 0, s>>>(X, w.Vt.p, op.p, op.ng, op.ld,
+                                                                                 op.gmap, active, S, ncp);
     h->launched("k_gather_t<f32>");
-    sv::k_colsum_vt<T><<<S, 1024, 0, s>>>(w.Vt.p, op.ld, op.ng, w.colsum.p);
+    sv::k_colsum_vt<T><<<ncp, 1024, 0, s>>>(w.Vt.p, op.ld, op.ng, w.colsum.p);
     h->launched("k_colsum_vt<f32>");
     tsplit = product_from_vt<T, S>(h, op, w, active, ncols);
   }
   if (use_D && h->mme->nseg > 0) {
     const Mme& mm = *h->mme;
-    sv::k_fix_seg<T, S><<<mm.nseg, sv::NT, 0, s>>>(op, mm.seg_row.p, mm.seg_lo.p, mm.seg_hi.p, X, w.seg_part.p, active);
+    sv::k_fix_seg<T, S><<<mm.nseg, sv::NT, 0, s>>>(op, mm.seg_row.p, mm.seg_lo.p, mm.seg_hi.p, X, w.seg_part.p, active,
+                                                   ncp);
     h->launched(sizeof(T) == 4 ? "k_fix_seg<f32>" : "k_fix_seg<f64>");
   }
   sv::k_spmv<T, S><<<w.nblk_spmv, sv::NT, 0, s>>>(op, X, w.Tout.p, tsplit, colsum, tshift, h->mme->fix_seg_ptr.p,
                                                   w.seg_part.p,
-                                                  (T)lam, use_D, Y, P, pq_part, active);
+                                                  (T)lam, use_D, Y, P, pq_part, active, ncp);
   h->launched(sizeof(T) == 4 ? "k_spmv<f32>" : "k_spmv<f64>");
 }
 

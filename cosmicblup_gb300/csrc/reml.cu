@@ -1337,7 +1337,7 @@ extern "C" int cbx_reml_iterate(cbx_handle* h, const cbx_reml_config* cfg, doubl
 
 extern "C" int cbx_reml_iterate_grad(cbx_handle* h, const cbx_reml_config* cfg, int32_t nprobe, double* var_u,
                                      double* var_e, cbx_reml_iter_info* info, double* grad, double* trace,
-                                     int64_t* grad_pcg_iters) {
+                                     int64_t* grad_pcg_iters, double* solution) {
   return cbx_guard(h, [&] {
     CBX_REQUIRE(h->mme, CBX_ERR_STATE, "call cbx_mme_create and cbx_mme_set_qinv_* first");
     CBX_REQUIRE(var_u && var_e && *var_u > 0 && *var_e > 0, CBX_ERR_ARG, "variances must be positive");
@@ -1350,6 +1350,8 @@ extern "C" int cbx_reml_iterate_grad(cbx_handle* h, const cbx_reml_config* cfg, 
     to_info(it, info);
     cbx::reml_gradient(h, vu0, ve0, nprobe, c.seed, 0, c.precision, c.pcg_tol, c.pcg_max_iter, grad, trace,
                        grad_pcg_iters);
+    if (solution && h->mme->has_last)
+      CBX_CUDA(cudaMemcpy(solution, h->mme->last_solution.p, h->mme->dim * sizeof(double), cudaMemcpyDeviceToHost));
   });
 }
 

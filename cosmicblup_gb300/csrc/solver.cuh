@@ -75,9 +75,9 @@ __device__ __forceinline__ double dot16(const double2& a, const double2& b) {
 template <typename T, int S>
 __global__ void k_gather_t(const T* __restrict__ X, T* __restrict__ Vt, int64_t p, int64_t ng,
                            int64_t ld, const int32_t* __restrict__ gmap,
-                           const int* __restrict__ active, int xs = S) {
+                           const int* __restrict__ active, int xs = S, int nc = S) {
   if (active && *active == 0) return;
-  const int64_t total = (int64_t)S * ld;
+  const int64_t total = (int64_t)nc * ld;  // the first nc columns (the populated ones)
   for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
        idx += (int64_t)gridDim.x * blockDim.x) {
     const int64_t c = idx / ld, k = idx - c * ld;
@@ -603,14 +603,15 @@ template <typename T, int S>
 __global__ void __launch_bounds__(NT) k_fix_seg(OpView<T> op, const int32_t* __restrict__ seg_row,
                                                 const int32_t* __restrict__ seg_lo, const int32_t* __restrict__ seg_hi,
                                                 const T* __restrict__ X, T* __restrict__ seg_part,
-                                                const int* __restrict__ active) {
+                                                const int* __restrict__ active, int ncp = S) {
   if (active && *active == 0) return;
   __shared__ T redT[NT];
   const int sg = blockIdx.x;
   constexpr int G = NT / S;
   const int tid = threadIdx.x, c = tid % S, g = tid / S;
   T acc[4] = {T(0), T(0), T(0), T(0)};
-  const int32_t hi = seg_hi[sg];
+  // columns past the populated ones (ncp) are not computed
+  const int32_t hi = c < ncp ? seg_hi[sg] : 0;
   int32_t j = seg_lo[sg] + g;
   for (; j + 3 * G < hi; j += 4 * G) {
 #pragma unroll
@@ -645,7 +646,11 @@ __device__ __forceinline__ void spmv_random_row(const OpView<T>& op, int64_t i, 
                                                 DotAcc<T> (&pq)[RowLayout<S>::CPL], int lane) {
   const int64_t p = op.p, u = i - p;
   if constexpr (S > 32) {
+    // column groups of 32; the 128-wide block holds at most 80 populated
+    // columns (its tensor-core product's limit), so only its first three groups
+    // are computed and the fourth is written as zero
     constexpr int CPL = S / 32;
+    constexpr int NG = S == 128 ? 3 : CPL;
     T acc[CPL], qv[CPL];
 #pragma unroll
     for (int j = 0; j < CPL; ++j) acc[j] = qv[j] = T(0);
@@ -654,24 +659,24 @@ __device__ __forceinline__ void spmv_random_row(const OpView<T>& op, int64_t i, 
     auto rowsum = [&](const int32_t* __restrict__ cidx, const T* __restrict__ val, int32_t e, int32_t e1,
                       int64_t off, T (&out)[CPL]) {
       for (; e + 3 < e1; e += 4) {
-        T dv[4], xv[4][CPL];
+        T dv[4], xv[4][NG];
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
           dv[k] = val[e + k];
           const T* xr = X + (off + cidx[e + k]) * S + lane;
 #pragma unroll
-          for (int j = 0; j < CPL; ++j) xv[k][j] = xr[32 * j];
+          for (int j = 0; j < NG; ++j) xv[k][j] = xr[32 * j];
         }
 #pragma unroll
         for (int k = 0; k < 4; ++k)
 #pragma unroll
-          for (int j = 0; j < CPL; ++j) out[j] += dv[k] * xv[k][j];
+          for (int j = 0; j < NG; ++j) out[j] += dv[k] * xv[k][j];
       }
       for (; e < e1; ++e) {
         const T dv = val[e];
         const T* xr = X + (off + cidx[e]) * S + lane;
 #pragma unroll
-        for (int j = 0; j < CPL; ++j) out[j] += dv * xr[32 * j];
+        for (int j = 0; j < NG; ++j) out[j] += dv * xr[32 * j];
       }
     };
     if (use_D) rowsum(op.Dcol, op.Dval, op.Dptr[i], op.Dptr[i + 1], 0, acc);
@@ -682,19 +687,23 @@ __device__ __forceinline__ void spmv_random_row(const OpView<T>& op, int64_t i, 
         for (int t = 0; t < tsplit; ++t) {
           const T* tr = Tout + ((int64_t)t * op.ng + k) * S + lane;
 #pragma unroll
-          for (int j = 0; j < CPL; ++j) qv[j] += tr[32 * j];
+          for (int j = 0; j < NG; ++j) qv[j] += tr[32 * j];
         }
         if (colsum) {
 #pragma unroll
-          for (int j = 0; j < CPL; ++j) qv[j] += (T)(tshift * colsum[lane + 32 * j]);
+          for (int j = 0; j < NG; ++j) qv[j] += (T)(tshift * colsum[lane + 32 * j]);
         }
       }
     }
 #pragma unroll
     for (int j = 0; j < CPL; ++j) {
-      const T yv = acc[j] + lam * qv[j];
-      Y[i * S + lane + 32 * j] = yv;
-      if (P) pq[j].add(P[i * S + lane + 32 * j], yv);
+      if (j < NG) {
+        const T yv = acc[j] + lam * qv[j];
+        Y[i * S + lane + 32 * j] = yv;
+        if (P) pq[j].add(P[i * S + lane + 32 * j], yv);
+      } else {
+        Y[i * S + lane + 32 * j] = T(0);  // defined, never read
+      }
     }
   } else {
     constexpr int G = 32 / S;
@@ -781,7 +790,7 @@ __global__ void __launch_bounds__(NT) k_spmv(OpView<T> op, const T* __restrict__
                                              const T* __restrict__ seg_part, T lam, int use_D,
                                              T* __restrict__ Y, const T* __restrict__ P,
                                              double* __restrict__ pq_part,
-                                             const int* __restrict__ active) {
+                                             const int* __restrict__ active, int ncp = S) {
   if (active && *active == 0) return;
   __shared__ double red[NT];
   __shared__ T redT[NT];
@@ -796,11 +805,12 @@ __global__ void __launch_bounds__(NT) k_spmv(OpView<T> op, const T* __restrict__
     constexpr int GS = NT / S;
     const int c = tid % S, g = tid / S;
     T s = T(0);
-    if (use_D)
+    if (use_D && c < ncp)
       for (int32_t k = fix_seg_ptr[i] + g; k < fix_seg_ptr[i + 1]; k += GS) s += seg_part[(int64_t)k * S + c];
     redT[tid] = s;
     __syncthreads();
-    if (tid < S) {
+    if (tid >= ncp && tid < S) Y[i * S + tid] = T(0);  // defined, never read
+    if (tid < ncp) {
       T t = T(0);
       for (int gg = 0; gg < GS; ++gg) t += redT[gg * S + tid];
       Y[i * S + tid] = t;
@@ -870,7 +880,8 @@ __global__ void __launch_bounds__(NT) k_fixed(OpView<T> op, const T* __restrict_
   constexpr int G = NT / S;
   const int tid = threadIdx.x, c = tid % S, g = tid / S;
   T acc = T(0);
-  for (int64_t k = g; k < op.p; k += G) acc += op.A11inv[f * op.p + k] * R[k * S + c];
+  const int64_t kend = (col == nullptr || col[c].active) ? op.p : 0;  // inactive columns: nothing to do
+  for (int64_t k = g; k < kend; k += G) acc += op.A11inv[f * op.p + k] * R[k * S + c];
   redT[tid] = acc;
   __syncthreads();
   if (tid < S) {
@@ -1136,6 +1147,7 @@ template <int S>
 __global__ void __launch_bounds__(NTC) k_scalar_alpha_c(Col* col, const double* pq_part, int nblk) {
   __shared__ double red[NTC];
   const int c = blockIdx.x;
+  if (!col[c].active) return;  // uniform over the block
   const double pq = col_total_c(pq_part, nblk, S, c, red);
   if (threadIdx.x != 0) return;
   Col s = col[c];
@@ -1168,9 +1180,11 @@ __global__ void __launch_bounds__(NTC) k_scalar_beta_c(Col* col, const double* p
   __shared__ double red[NTC];
   __shared__ int last;
   const int c = blockIdx.x;
-  const double rr = col_total_c(part, nblk, 2 * S, c, red);
-  const double rzr = col_total_c(part + S, nblk, 2 * S, c, red);
-  const double rzf = p > 0 ? col_total_c(rz_fix, (int)p, S, c, red) : 0.0;
+  // an inactive column's partials are not read (uniform over the block)
+  const bool was_active = col[c].active != 0;
+  const double rr = was_active ? col_total_c(part, nblk, 2 * S, c, red) : 0.0;
+  const double rzr = was_active ? col_total_c(part + S, nblk, 2 * S, c, red) : 0.0;
+  const double rzf = (was_active && p > 0) ? col_total_c(rz_fix, (int)p, S, c, red) : 0.0;
   if (threadIdx.x == 0) {
     Col s = col[c];
     if (s.active) {

@@ -60,18 +60,22 @@ class AIREML:
         self.var_e = float(var_e)
         self.var_u = float(vars_u[0] if np.ndim(vars_u) else vars_u)
 
-    def run_iteration(self, grad_probes: int = 0) -> dict:
+    def run_iteration(self, grad_probes: int = 0, solution: bool = False) -> dict:
         """One REML iteration.  grad_probes > 0 also returns the REML gradient at
         the iteration's starting point from that many probes (cbx_reml_iterate_grad:
-        one block solve serves both) as d["grad"], d["grad_trace"], d["grad_pcg_iters"]."""
+        one block solve serves both) as d["grad"], d["grad_trace"], d["grad_pcg_iters"],
+        and with solution=True the data solve as self.solution."""
         vu, ve = C.c_double(self.var_u), C.c_double(self.var_e)
         info = RemlIterInfo()
         if grad_probes > 0:
             g = np.zeros(2)
             tr, it = C.c_double(0), C.c_int64(0)
+            sol = np.zeros(self.mme.dim) if solution else None
             self.mme.h.check(lib().cbx_reml_iterate_grad(self.mme.h.raw, C.byref(self.config), int(grad_probes),
                                                          C.byref(vu), C.byref(ve), C.byref(info), ptr(g),
-                                                         C.byref(tr), C.byref(it)))
+                                                         C.byref(tr), C.byref(it), ptr(sol)))
+            if solution:
+                self.solution = sol
         else:
             self.mme.h.check(lib().cbx_reml_iterate(self.mme.h.raw, C.byref(self.config), C.byref(vu),
                                                     C.byref(ve), C.byref(info)))

@@ -417,11 +417,12 @@ int cbx_reml_gradient(cbx_handle* h, double var_u, double var_e, int32_t nprobe,
  * gradient's first probes (up to 79, whole 16-probe batches) join the
  * iteration's data + probe block, so one multi-RHS solve serves both; the
  * iteration's estimator still uses exactly the probes its stopping rule
- * selects.  grad (2) gets the score; info, trace and grad_pcg_iters (CG
- * iterations of the gradient's own solves) may be NULL. */
+ * selects.  grad (2) gets the score; info, trace, grad_pcg_iters (CG
+ * iterations of the gradient's own solves) and solution (dim: the last data
+ * solve, as cbx_reml_solve returns it) may be NULL. */
 int cbx_reml_iterate_grad(cbx_handle* h, const cbx_reml_config* cfg, int32_t nprobe, double* var_u,
                           double* var_e, cbx_reml_iter_info* info, double* grad, double* trace,
-                          int64_t* grad_pcg_iters);
+                          int64_t* grad_pcg_iters, double* solution);
 /* REML log-likelihood by dense Cholesky of the LHS (dim <= 24,576): with a dense
  * Qinv, run_dense_exact_step's compute_logL (src/core/vce.cpp:2974-3007); with a
  * split Qinv (ssGBLUP), calc_logL_internal (:3533-3588), which omits the constant
