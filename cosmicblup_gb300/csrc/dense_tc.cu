@@ -72,16 +72,6 @@ __device__ __forceinline__ void umma_tf32(uint32_t d, uint64_t a, uint64_t b, ui
       "l"(a), "l"(b), "r"(idesc), "r"(acc)
       : "memory");
 }
-// K-major SWIZZLE_128B descriptor: 8-row groups 1024 bytes apart.
-__device__ __forceinline__ uint64_t sdesc_sw128(uint32_t saddr) {
-  uint64_t d = 0;
-  d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
-  d |= (uint64_t)1 << 16;              // leading byte offset (unused for swizzled K-major)
-  d |= (uint64_t)(1024 >> 4) << 32;    // stride byte offset
-  d |= (uint64_t)1 << 46;              // descriptor version
-  d |= (uint64_t)2 << 61;              // SWIZZLE_128B
-  return d;
-}
 __host__ __device__ constexpr uint32_t idesc_tf32(uint32_t M, uint32_t N) {
   return (1u << 4) | (2u << 7) | (2u << 10) | ((N >> 3) << 17) | ((M >> 4) << 24);
 }
@@ -352,6 +342,10 @@ static int stream_k(int64_t ng, int64_t ld, int num_sms, int* grid_out, int* per
 }
 
 int dense_tc_ksplit(int64_t ng, int64_t ld, int num_sms) { return stream_k(ng, ld, num_sms, nullptr, nullptr); }
+// bf16 tiles are 64 elements wide: the same split over ld / 2
+int dense_bf_stream_k(int64_t ng, int64_t ld, int num_sms, int* grid, int* per) {
+  return stream_k(ng, (ld + 1) / 2, num_sms, grid, per);
+}
 int dense_tc_stream_k(int64_t ng, int64_t ld, int num_sms, int* grid, int* per) {
   return stream_k(ng, ld, num_sms, grid, per);
 }

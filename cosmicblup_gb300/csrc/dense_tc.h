@@ -10,6 +10,13 @@ int dense_tc_stream_k(int64_t ng, int64_t ld, int num_sms, int* grid, int* per);
 // Tpart[ks][i][c] = sum over split ks of Qd[i][k] Vt[c][k]; S = 16 or 32.
 void dense_tc(cbx_handle* h, const float* Qd, int64_t ng, int64_t ld, const float* Vt, int S, int ksplit,
               float* Tpart, const int* active, int ncols);
+// The bf16 block product (dense_bf.cu): the same split over 64-element K steps,
+// the bf16 copy of Qd - shift, and Tpart as dense_tc for the first ncols of the
+// S gathered FP32 rows Vt (Vhl: 2 S ld bf16 scratch); returns the partial count.
+int dense_bf_stream_k(int64_t ng, int64_t ld, int num_sms, int* grid, int* per);
+void dense_bf_block(cbx_handle* h, const double* Qd64, int64_t ng, int64_t ld, double shift, uint16_t* Qbf);
+int dense_bf(cbx_handle* h, const uint16_t* Qbf, int64_t ng, int64_t ld, const float* Vt, int S, uint16_t* Vhl,
+             float* Tpart, const int* active, int ncols);
 // FP64-accurate block product on the tensor cores by exact fixed-point digits
 // (dense_fx.cu): Tout[i * os + c] = sum_k (qh + ql)[i][k] v[k][c] for c < ncols <= 32,
 // v[k][c] = X[(p + gmap[k]) * xs + c] (k < ng), the block an ng x ld row-major pair of

@@ -239,6 +239,7 @@ static int env_int(const char* name, int def) {
 template <typename T, int S>
 struct Workspace {
   DevBuf<T> R, Z, P, Q, Vt, Tout, X;
+  DevBuf<uint16_t> Vbf;   // bf16 hi / lo rows of the gathered vectors (CBX_BF16=1)
   DevBuf<T> Pn;           // second direction buffer of the fused iteration
   DevBuf<double> part, pq_part, rz_fix, tol, colsum;
   DevBuf<double> fpart;   // per-block partials of the fused iteration (nb_fused x 4 x S)
@@ -287,6 +288,14 @@ struct Workspace {
 
 // FP32 probe blocks of 16 or 32 columns use the tcgen05 3xTF32 product unless
 // the environment sets CBX_DENSE_TC=0.
+// The FP32 PCG bulk's block product from a bf16 copy of the block (half the
+// bytes; the inner operator is then perturbed by the block's rounding, so the
+// refinement takes more outer steps) when the environment sets CBX_BF16=1.
+static bool use_bf16() {
+  static int v = env_int("CBX_BF16", 0);
+  return v != 0;
+}
+
 static bool use_dense_tc() {
   static int v = -1;
   if (v < 0) {
@@ -556,7 +565,13 @@ int product_from_vt(cbx_handle* h, const sv::OpView<T>& op, Workspace<T, S>& w, 
     CBX_CUDA(cudaEventCreate(&pr.b));
     CBX_CUDA(cudaEventRecord(pr.a, s));
   }
-  if ((S == 16 || S == 32 || S == 64 || S == 128) && use_dense_tc()) {
+  bool bf = false;
+  if ((S == 16 || S == 32 || S == 64 || S == 128) && sizeof(T) == 4 && h->mme->Qbf.p && use_dense_tc()) {
+    w.Vbf.resize((size_t)2 * S * op.ld);
+    tsplit = dense_bf(h, h->mme->Qbf.p, op.ng, op.ld, reinterpret_cast<const float*>(w.Vt.p), S, w.Vbf.p,
+                      reinterpret_cast<float*>(w.Tout.p), active, ncols);
+    bf = true;
+  } else if ((S == 16 || S == 32 || S == 64 || S == 128) && use_dense_tc()) {
     tsplit = dense_tc_ksplit(op.ng, op.ld, h->num_sms);
     dense_tc(h, reinterpret_cast<const float*>(op.Qd), op.ng, op.ld, reinterpret_cast<const float*>(w.Vt.p), S,
              tsplit, reinterpret_cast<float*>(w.Tout.p), active, ncols);
@@ -591,8 +606,8 @@ int product_from_vt(cbx_handle* h, const sv::OpView<T>& op, Workspace<T, S>& w, 
   if (h->prof_on) {
     CBX_CUDA(cudaEventRecord(pr.b, s));
     pr.bucket = 0;
-    // algorithmic bytes: the dense block once, the S gathered vectors, the outputs
-    pr.bytes = 4.0 * ((double)op.ng * op.ld + (double)S * op.ld + (double)op.ng * S * tsplit);
+    // algorithmic bytes: the dense block once (bf16 or FP32), the S gathered vectors, the outputs
+    pr.bytes = (bf ? 2.0 : 4.0) * (double)op.ng * op.ld + 4.0 * ((double)S * op.ld + (double)op.ng * S * tsplit);
     h->prof.push_back(pr);
   }
   return tsplit;
@@ -1437,6 +1452,12 @@ static void upload_dense(cbx_handle* h, Mme& m, const double* src, int64_t ng) {
                                                                        m.Qlo32.p);
   h->launched("k_lowp_block");
   m.fx_rows_ok = false;
+  if (use_bf16() && m.ld % 8 == 0) {
+    m.Qbf.resize((size_t)ng * m.ld);
+    dense_bf_block(h, m.Qd64.p, ng, m.ld, m.qshift, m.Qbf.p);
+  } else {
+    m.Qbf.release();
+  }
 }
 
 // Dense Qinv (q x q, symmetric, row- or column-major alike).  Qinv == NULL uses

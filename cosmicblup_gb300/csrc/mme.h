@@ -54,6 +54,7 @@ struct Mme {
   DevBuf<float> Qd32;              // fl32(Qd - qshift)
   DevBuf<float> Qlo32;             // fl32(Qd - qshift - Qd32): with Qd32 the float-float block
   double qshift = 0.0;
+  DevBuf<uint16_t> Qbf;            // bf16(Qd - qshift), ng x ld (only with CBX_BF16=1)
   // row scales of the Qd32 / Qlo32 planes for the fixed-point tensor-core
   // refinement product (valid while fx_rows_ok), and its scratch
   DevBuf<int32_t> fx_rowexp;
