@@ -31,6 +31,14 @@ struct cbx_handle {
   // the device by cbx_ssgblup_qinv
   cbx::DevBuf<double> Hd;
   int64_t Hd_n = 0;
+  // Rademacher probe vectors of the trace estimator's stream (q x count,
+  // column-major) for seed probe_z_seed and order probe_z_q: deterministic, so
+  // each 16-probe batch is drawn on the host once and later MMEs of the handle
+  // copy it on the device
+  cbx::DevBuf<double> probe_z;
+  std::vector<char> probe_z_have;
+  int probe_z_seed = -1;
+  int64_t probe_z_q = -1;
   // mixed-model equations and REML state
   std::unique_ptr<cbx::Mme> mme;
   // library handles (cuSOLVER / cuBLAS) and dense exact AI state, owned here

@@ -16,6 +16,7 @@
 #include <cmath>
 #include <memory>
 #include <random>
+#include <thread>
 #include <vector>
 #include <cublas_v2.h>
 #include <cusolverDn.h>
@@ -340,22 +341,66 @@ static void probe_store(cbx_handle* h, Mme& m, int seed, int cap) {
   m.probe_cap = cap;
 }
 
-// Upload the batch of probes [start, start + size) (rows p.. of em_B columns
-// 1 + start ..; the fixed rows stay zero) unless every column is there.
-static void probe_batch(cbx_handle* h, Mme& m, int seed, int start, int size) {
-  bool all = true;
-  for (int j = 0; j < size; ++j) all = all && m.probe_have[start + j];
-  if (all) return;
-  const int64_t q = m.q, dim = m.dim, p = m.p;
-  std::vector<double> Zb((size_t)q * size);
+// Probes [start, start + size) of the stream: a batch of the reference's
+// estimator, drawn from mt19937_64(seed + start) with uniform_int_distribution
+// <int>(0, 1) (0 -> -1, 1 -> +1), probe by probe, q values each.
+static void probe_draw(int seed, int start, int size, int64_t q, double* out) {
   std::mt19937_64 gen((unsigned long)(seed + start));
   std::uniform_int_distribution<int> dist(0, 1);
   for (int j = 0; j < size; ++j)
-    for (int64_t i = 0; i < q; ++i) Zb[(size_t)j * q + i] = dist(gen) == 0 ? -1.0 : 1.0;
-  CBX_CUDA(cudaMemcpy2DAsync(m.em_B.p + (size_t)(1 + start) * dim + p, dim * sizeof(double), Zb.data(),
-                             q * sizeof(double), q * sizeof(double), size, cudaMemcpyHostToDevice, h->stream));
-  CBX_CUDA(cudaStreamSynchronize(h->stream));
-  for (int j = 0; j < size; ++j) m.probe_have[start + j] = 1;
+    for (int64_t i = 0; i < q; ++i) out[(size_t)j * q + i] = dist(gen) == 0 ? -1.0 : 1.0;
+}
+
+// Put the probe batches (start, size) into rows p.. of em_B columns 1 + start ..
+// (the fixed rows stay zero).  Batches the handle has not drawn yet for this seed
+// and q are drawn on host threads (one per batch: each batch is its own
+// generator) and kept on the device; the others are copied there.
+static void probe_batches(cbx_handle* h, Mme& m, int seed, const std::vector<std::pair<int, int>>& batches) {
+  const int64_t q = m.q, dim = m.dim, p = m.p;
+  cudaStream_t s = h->stream;
+  if (h->probe_z_seed != seed || h->probe_z_q != q) {
+    h->probe_z_have.clear();
+    h->probe_z_seed = seed;
+    h->probe_z_q = q;
+  }
+  int hi = 0;
+  std::vector<std::pair<int, int>> need, draw;
+  for (const auto& bt : batches) {
+    bool have = true;
+    for (int j = 0; j < bt.second; ++j) have = have && m.probe_have[bt.first + j];
+    if (have) continue;
+    need.push_back(bt);
+    hi = std::max(hi, bt.first + bt.second);
+    bool cached = (int)h->probe_z_have.size() >= bt.first + bt.second;
+    for (int j = 0; cached && j < bt.second; ++j) cached = h->probe_z_have[bt.first + j] != 0;
+    if (!cached) draw.push_back(bt);
+  }
+  if (need.empty()) return;
+  if ((int)h->probe_z_have.size() < hi) {
+    grow_keep(h, h->probe_z, (size_t)q * h->probe_z_have.size(), (size_t)q * hi);
+    h->probe_z_have.resize(hi, 0);
+  }
+  if (!draw.empty()) {
+    std::vector<std::vector<double>> buf(draw.size());
+    std::vector<std::thread> pool;
+    for (size_t t = 0; t < draw.size(); ++t) {
+      buf[t].resize((size_t)q * draw[t].second);
+      pool.emplace_back(probe_draw, seed, draw[t].first, draw[t].second, q, buf[t].data());
+    }
+    for (auto& th : pool) th.join();
+    for (size_t t = 0; t < draw.size(); ++t) {
+      CBX_CUDA(cudaMemcpyAsync(h->probe_z.p + (size_t)draw[t].first * q, buf[t].data(),
+                               buf[t].size() * sizeof(double), cudaMemcpyHostToDevice, s));
+      for (int j = 0; j < draw[t].second; ++j) h->probe_z_have[draw[t].first + j] = 1;
+    }
+    CBX_CUDA(cudaStreamSynchronize(s));  // the host buffers go out of scope
+  }
+  for (const auto& bt : need) {
+    CBX_CUDA(cudaMemcpy2DAsync(m.em_B.p + (size_t)(1 + bt.first) * dim + p, dim * sizeof(double),
+                               h->probe_z.p + (size_t)bt.first * q, q * sizeof(double), q * sizeof(double),
+                               bt.second, cudaMemcpyDeviceToDevice, s));
+    for (int j = 0; j < bt.second; ++j) m.probe_have[bt.first + j] = 1;
+  }
 }
 
 // The stored solutions of probes [c0, c0 + k) are a warm start when every one
@@ -472,7 +517,7 @@ static void em_iteration(cbx_handle* h, const RemlConfigI& cfg, double& vu, doub
       next += sz;
     } while (next < min_s && next < max_s);
     g.k = next - done;
-    for (auto& bt : g.batches) probe_batch(h, m, cfg.seed, bt.first, bt.second);
+    probe_batches(h, m, cfg.seed, g.batches);
     return g;
   };
   auto count = [&](const PcgResult& pr, int c0, int k, const char* what) {
@@ -487,7 +532,11 @@ static void em_iteration(cbx_handle* h, const RemlConfigI& cfg, double& vu, doub
   // probes solved in the data block: the first group, or the gradient's first
   // `extra` probes when they are more (whole batches, 79 at most)
   const int kx = std::max(g0.k, std::min(extra, 79) / batch * batch);
-  for (int b = g0.k; b < kx; b += batch) probe_batch(h, m, cfg.seed, b, std::min(batch, kx - b));
+  {
+    std::vector<std::pair<int, int>> bts;
+    for (int b = g0.k; b < kx; b += batch) bts.push_back({b, std::min(batch, kx - b)});
+    probe_batches(h, m, cfg.seed, bts);
+  }
   // --- 1. the data solve (with the first probe group in mixed precision)
   const bool data_warm = m.has_last;
   const bool merge = mixed && data_warm == probes_warm(m, 0, kx);
@@ -759,7 +808,9 @@ static void reml_gradient(cbx_handle* h, double vu, double ve, int nprobe, int s
     const int blk = mixed ? 64 : 32;
     for (int c0 = have; c0 < nprobe;) {
       const int k = std::min(blk - (c0 % 16), nprobe - c0);
-      for (int b = c0 - c0 % 16; b < c0 + k; b += 16) probe_batch(h, m, seed, b, std::min(16, m.probe_cap - b));
+      std::vector<std::pair<int, int>> bts;
+      for (int b = c0 - c0 % 16; b < c0 + k; b += 16) bts.push_back({b, std::min(16, m.probe_cap - b)});
+      probe_batches(h, m, seed, bts);
       PcgResult pr;
       probe_solve(h, m, lam, c0, k, precision, pcg_tol, pcg_maxit, pr);
       for (int c = 0; c < k; ++c) iters += pr.iters[c];
