@@ -13,6 +13,8 @@
 #include <algorithm>
 #include <cstdio>
 #include <cmath>
+#include <exception>
+#include <thread>
 #include <vector>
 #include "handle.h"
 #include "pcg.h"
@@ -250,9 +252,12 @@ struct Workspace {
   DevBuf<int> active;
   DevBuf<unsigned> done;  // arrival counter of k_scalar_beta_c (reset by its last block)
   int nblk_vec = 0, nblk_spmv = 0;
-  int64_t dim = -1;
+  int64_t dim = -1, p_ = -1, ng_ = -1, ld_ = -1;
+  int nseg_ = -1;
   void alloc(const Mme& m, int num_sms) {
-    if (dim == m.dim && (!m.has_dense || Vt.n == (size_t)S * m.ld)) return;
+    if (dim == m.dim && p_ == m.p && nseg_ == m.nseg && ng_ == m.ng && ld_ == m.ld &&
+        (!m.has_dense || Vt.n == (size_t)S * m.ld))
+      return;
     const int64_t n = m.dim * S;
     R.resize(n); Z.resize(n); P.resize(n); Q.resize(n); X.resize(n);
     if (m.has_dense) { Vt.resize((size_t)S * m.ld); Tout.resize((size_t)m.ng * S * 8); colsum.resize(S); }
@@ -270,6 +275,10 @@ struct Workspace {
     CBX_CUDA(cudaMemset(done.p, 0, sizeof(unsigned)));
     seg_part.resize((size_t)std::max<int32_t>(m.nseg, 1) * S);
     dim = m.dim;
+    p_ = m.p;
+    nseg_ = m.nseg;
+    ng_ = m.ng;
+    ld_ = m.ld;
     nb_fused = 0;
     if constexpr (sizeof(T) == 4) {
       int per_sm = 0;
@@ -851,6 +860,11 @@ struct Solver : public SolverBase {
   DevBuf<float> dinv32, R32, D32, D32lo;
   double dinv_lam = std::nan("");
 
+  void rebind() override {
+    dinv_lam = std::nan("");
+    w64.dim = w32.dim = -1;  // the next prepare re-checks every size and clears the counters
+  }
+
   void prepare(cbx_handle* h, Mme& m, double lam, bool need32) {
     cudaStream_t s = h->stream;
     w64.alloc(m, h->num_sms);
@@ -1217,11 +1231,6 @@ double record_residual(cbx_handle* h, const double* sol_dev, double* e_dev) {
 
 // ---------------------------------------------------------------------------
 // host assembly helpers
-struct Trip {
-  int64_t r, c;
-  double v;
-};
-
 template <typename T>
 static void upload_csr(cudaStream_t s, int64_t rows, const std::vector<int32_t>& ptr, const std::vector<int32_t>& col,
                        const std::vector<double>& val, Csr<T>& out) {
@@ -1239,37 +1248,188 @@ static void upload_csr(cudaStream_t s, int64_t rows, const std::vector<int32_t>&
   }
 }
 
-// Triplets to CSR, duplicates summed in their insertion order: a stable counting
-// sort by row, then a stable sort of each row by column (the same order as one
-// stable sort by (row, column), in linear time for the many short rows).
-static void triplets_to_csr(int64_t rows, std::vector<Trip>& t, std::vector<int32_t>& ptr, std::vector<int32_t>& col,
-                            std::vector<double>& val) {
-  {
-    std::vector<int64_t> start(rows + 1, 0);
-    for (const Trip& x : t) start[x.r + 1]++;
-    for (int64_t i = 0; i < rows; ++i) start[i + 1] += start[i];
-    std::vector<Trip> by_row(t.size());
-    std::vector<int64_t> pos(start.begin(), start.end() - 1);
-    for (const Trip& x : t) by_row[pos[x.r]++] = x;
-    for (int64_t i = 0; i < rows; ++i)
-      if (start[i + 1] - start[i] > 1)
-        std::stable_sort(by_row.begin() + start[i], by_row.begin() + start[i + 1],
-                         [](const Trip& a, const Trip& b) { return a.c < b.c; });
-    t.swap(by_row);
+// W'W as CSR and W'y from the records (mme_builder.cpp:107-176, 321-387) on
+// host threads: every record emits its triplets (fixed x fixed pairs, fixed x
+// animal, animal x animal) in record order; the threads take contiguous record
+// ranges, count their triplets per row, and place them at offsets that keep the
+// record order within each row, so each row's entries come out as from one
+// sequential pass (a stable counting sort).  Each row is then sorted stably by
+// column and its duplicates summed in that order, so W'W does not depend on the
+// number of threads.  W'y and y'y are summed in record order.
+struct WtW {
+  std::vector<int32_t> ptr, col;
+  std::vector<double> val, rhs;
+  double yty = 0.0;
+};
+
+static void assemble_wtw(int64_t n_rec, int64_t p, int64_t q, const double* y, const int32_t* aid,
+                         const int64_t* fx_ptr, const int32_t* fx_col, const double* fx_val, WtW& out) {
+  const int64_t dim = p + q;
+  const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
+  const int T = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)std::min(hw, 16), n_rec / 2000));
+  struct Part {
+    int64_t r0 = 0, r1 = 0;
+    std::vector<int64_t> cnt;   // triplets per row, then the running placement offsets
+    int err = CBX_OK;
+    const char* what = nullptr;
+  };
+  std::vector<Part> part(T);
+  for (int t = 0; t < T; ++t) {
+    part[t].r0 = n_rec * t / T;
+    part[t].r1 = n_rec * (t + 1) / T;
   }
-  ptr.assign(rows + 1, 0);
-  col.clear();
-  val.clear();
-  for (size_t k = 0; k < t.size();) {
-    size_t e = k;
-    double v = 0.0;
-    while (e < t.size() && t[e].r == t[k].r && t[e].c == t[k].c) v += t[e++].v;
-    col.push_back((int32_t)t[k].c);
-    val.push_back(v);
-    ptr[t[k].r + 1]++;
-    k = e;
+  // fn(t) on T threads; an exception in a thread is rethrown after the join
+  auto run = [&](auto&& fn) {
+    std::vector<std::exception_ptr> fail(T);
+    auto body = [&](int t) {
+      try {
+        fn(t);
+      } catch (...) {
+        fail[t] = std::current_exception();
+      }
+    };
+    std::vector<std::thread> pool;
+    for (int t = 1; t < T; ++t) pool.emplace_back(body, t);
+    body(0);
+    for (auto& th : pool) th.join();
+    for (auto& f : fail)
+      if (f) std::rethrow_exception(f);
+  };
+  // the triplets of record i, in order, to emit(row, col, value)
+  auto record = [&](int64_t i, auto&& emit) {
+    const int64_t a0 = fx_ptr[i], a1 = fx_ptr[i + 1];
+    for (int64_t a = a0; a < a1; ++a)
+      for (int64_t b = a; b < a1; ++b) {
+        const double v = fx_val[a] * fx_val[b];
+        emit(fx_col[a], fx_col[b], v);
+        if (fx_col[a] != fx_col[b]) emit(fx_col[b], fx_col[a], v);
+      }
+    const int32_t an = aid[i];
+    if (an > 0 && an <= q) {
+      const int64_t ck = p + an - 1;
+      for (int64_t a = a0; a < a1; ++a) {
+        emit(fx_col[a], ck, fx_val[a]);
+        emit(ck, (int64_t)fx_col[a], fx_val[a]);
+      }
+      emit(ck, ck, 1.0);
+    }
+  };
+  // 1. per thread: checks and triplet counts per row
+  run([&](int t) {
+    Part& pt = part[t];
+    pt.cnt.assign(dim, 0);
+    for (int64_t i = pt.r0; i < pt.r1; ++i) {
+      if (fx_ptr[i + 1] < fx_ptr[i]) { pt.err = CBX_ERR_ARG; pt.what = "fx_ptr not monotone"; return; }
+      if (!std::isfinite(y[i])) { pt.err = CBX_ERR_NONFINITE; pt.what = "non-finite phenotype"; return; }
+      for (int64_t a = fx_ptr[i]; a < fx_ptr[i + 1]; ++a) {
+        if (fx_col[a] < 0 || fx_col[a] >= p) {
+          pt.err = CBX_ERR_ARG;
+          pt.what = "fixed-effect column out of range";
+          return;
+        }
+      }
+      record(i, [&](int64_t r, int64_t, double) { pt.cnt[r]++; });
+    }
+  });
+  for (const Part& pt : part) CBX_REQUIRE(pt.err == CBX_OK, pt.err, pt.what);
+  out.rhs.assign(dim, 0.0);
+  out.yty = 0.0;
+  for (int64_t i = 0; i < n_rec; ++i) {
+    for (int64_t a = fx_ptr[i]; a < fx_ptr[i + 1]; ++a) out.rhs[fx_col[a]] += fx_val[a] * y[i];
+    const int32_t an = aid[i];
+    if (an > 0 && an <= q) out.rhs[p + an - 1] += y[i];
+    out.yty += y[i] * y[i];
   }
-  for (int64_t i = 0; i < rows; ++i) ptr[i + 1] += ptr[i];
+  // 2. row starts; each thread's offsets in a row follow the earlier threads'
+  // (row ranges in parallel: offsets within the range, then the range bases)
+  std::vector<int64_t> start(dim + 1, 0), base(T + 1, 0);
+  run([&](int t) {
+    int64_t o = 0;
+    for (int64_t r = dim * t / T; r < dim * (t + 1) / T; ++r) {
+      start[r] = o;
+      for (int k = 0; k < T; ++k) {
+        const int64_t c = part[k].cnt[r];
+        part[k].cnt[r] = o;
+        o += c;
+      }
+    }
+    base[t + 1] = o;
+  });
+  for (int t = 0; t < T; ++t) base[t + 1] += base[t];
+  start[dim] = base[T];
+  run([&](int t) {
+    const int64_t b = base[t];
+    for (int64_t r = dim * t / T; r < dim * (t + 1) / T; ++r) {
+      start[r] += b;
+      for (int k = 0; k < T; ++k) part[k].cnt[r] += b;
+    }
+  });
+  struct Ent {
+    int32_t c;
+    double v;
+  };
+  std::unique_ptr<Ent[]> ent(new Ent[(size_t)std::max<int64_t>(start[dim], 1)]);
+  // 3. placement in record order
+  run([&](int t) {
+    Part& pt = part[t];
+    for (int64_t i = pt.r0; i < pt.r1; ++i)
+      record(i, [&](int64_t r, int64_t c, double v) { ent[pt.cnt[r]++] = Ent{(int32_t)c, v}; });
+  });
+  // 4. rows sorted by column (stable), unique entries per row; the threads take
+  // row ranges of about equal numbers of entries
+  std::vector<int64_t> rb(T + 1, dim);
+  rb[0] = 0;
+  for (int t = 1; t < T; ++t)
+    rb[t] = std::lower_bound(start.begin(), start.end(), start[dim] * t / T) - start.begin();
+  for (int t = 1; t <= T; ++t) rb[t] = std::min(dim, std::max(rb[t], rb[t - 1]));
+  std::vector<int32_t> uniq(dim, 0);
+  auto rows_of = [&](int t, int64_t& r0, int64_t& r1) {
+    r0 = rb[t];
+    r1 = rb[t + 1];
+  };
+  run([&](int t) {
+    int64_t r0, r1;
+    rows_of(t, r0, r1);
+    for (int64_t r = r0; r < r1; ++r) {
+      const int64_t e0 = start[r], e1 = start[r + 1];
+      if (e1 - e0 > 32) {
+        std::stable_sort(&ent[e0], &ent[e1], [](const Ent& a, const Ent& b) { return a.c < b.c; });
+      } else {
+        for (int64_t e = e0 + 1; e < e1; ++e) {   // insertion sort: stable
+          const Ent x = ent[e];
+          int64_t k = e;
+          for (; k > e0 && ent[k - 1].c > x.c; --k) ent[k] = ent[k - 1];
+          ent[k] = x;
+        }
+      }
+      int32_t u = 0;
+      for (int64_t e = e0; e < e1; ++e) u += (e == e0 || ent[e].c != ent[e - 1].c) ? 1 : 0;
+      uniq[r] = u;
+    }
+  });
+  int64_t nnz = 0;
+  for (int64_t r = 0; r < dim; ++r) nnz += uniq[r];
+  CBX_REQUIRE(nnz < (int64_t)INT32_MAX, CBX_ERR_UNSUPPORTED, "W'W has more than 2^31 entries");
+  out.ptr.assign(dim + 1, 0);
+  for (int64_t r = 0; r < dim; ++r) out.ptr[r + 1] = out.ptr[r] + uniq[r];
+  out.col.resize(out.ptr[dim]);
+  out.val.resize(out.ptr[dim]);
+  // 5. duplicates summed in their order
+  run([&](int t) {
+    int64_t r0, r1;
+    rows_of(t, r0, r1);
+    for (int64_t r = r0; r < r1; ++r) {
+      int64_t o = out.ptr[r];
+      for (int64_t e = start[r]; e < start[r + 1];) {
+        const int32_t c = ent[e].c;
+        double v = 0.0;
+        while (e < start[r + 1] && ent[e].c == c) v += ent[e++].v;
+        out.col[o] = c;
+        out.val[o] = v;
+        ++o;
+      }
+    }
+  });
 }
 
 }  // namespace cbx
@@ -1288,41 +1448,15 @@ extern "C" int cbx_mme_create(cbx_handle* h, int64_t n_rec, int64_t p, int64_t q
     auto m = std::make_unique<Mme>();
     m->n_rec = n_rec; m->p = p; m->q = q; m->dim = p + q;
     const int64_t dim = p + q;
-    // W'W triplets in record order (mme_builder.cpp:107-176) and W'y (:321-387)
-    std::vector<Trip> t;
-    t.reserve((size_t)n_rec * 8);
-    std::vector<double> rhs(dim, 0.0);
+    // W'W and W'y (mme_builder.cpp:107-176, 321-387), assembled on host threads
+    WtW wtw;
+    assemble_wtw(n_rec, p, q, y, aid, fx_ptr, fx_col, fx_val, wtw);
+    std::vector<int32_t>& ptr = wtw.ptr;
+    std::vector<int32_t>& col = wtw.col;
+    std::vector<double>& val = wtw.val;
+    std::vector<double>& rhs = wtw.rhs;
+    const double yty = wtw.yty;
     std::vector<double> A11((size_t)p * p, 0.0);
-    double yty = 0.0;
-    for (int64_t i = 0; i < n_rec; ++i) {
-      CBX_REQUIRE(fx_ptr[i + 1] >= fx_ptr[i], CBX_ERR_ARG, "fx_ptr not monotone");
-      CBX_REQUIRE(std::isfinite(y[i]), CBX_ERR_NONFINITE, "non-finite phenotype");
-      const int64_t a0 = fx_ptr[i], a1 = fx_ptr[i + 1];
-      for (int64_t a = a0; a < a1; ++a) {
-        CBX_REQUIRE(fx_col[a] >= 0 && fx_col[a] < p, CBX_ERR_ARG, "fixed-effect column out of range");
-        for (int64_t b = a; b < a1; ++b) {
-          const double v = fx_val[a] * fx_val[b];
-          t.push_back({fx_col[a], fx_col[b], v});
-          if (fx_col[a] != fx_col[b]) t.push_back({fx_col[b], fx_col[a], v});
-        }
-        rhs[fx_col[a]] += fx_val[a] * y[i];
-      }
-      const int32_t an = aid[i];
-      if (an > 0 && an <= q) {
-        const int64_t ck = p + an - 1;
-        for (int64_t a = a0; a < a1; ++a) {
-          t.push_back({fx_col[a], ck, fx_val[a]});
-          t.push_back({ck, fx_col[a], fx_val[a]});
-        }
-        t.push_back({ck, ck, 1.0});
-        rhs[ck] += y[i];
-      }
-      yty += y[i] * y[i];
-    }
-    std::vector<int32_t> ptr, col;
-    std::vector<double> val;
-    triplets_to_csr(dim, t, ptr, col, val);
-    CBX_REQUIRE(col.size() < (size_t)INT32_MAX, CBX_ERR_UNSUPPORTED, "W'W has more than 2^31 entries");
     std::vector<double> diag(dim, 0.0);
     for (int64_t i = 0; i < dim; ++i)
       for (int32_t j = ptr[i]; j < ptr[i + 1]; ++j) {
@@ -1417,6 +1551,28 @@ extern "C" int cbx_mme_create(cbx_handle* h, int64_t n_rec, int64_t p, int64_t q
     m->xv_host.assign(fx_val, fx_val + nx);
     m->rhs_host = rhs;
     CBX_CUDA(cudaStreamSynchronize(s));
+    if (h->mme) {
+      // The device buffers whose sizes follow the shapes go to the new MME, whose
+      // set-up and solves size-check and rewrite them before use: a rebuild of
+      // the same shape (a new set of records) then neither frees nor allocates
+      // the dense planes (several GB) or the solver workspaces.
+      Mme& o = *h->mme;
+      CBX_CUDA(cudaStreamSynchronize(s));
+      m->Qd64 = std::move(o.Qd64);
+      m->Qd32 = std::move(o.Qd32);
+      m->Qlo32 = std::move(o.Qlo32);
+      m->Qbf = std::move(o.Qbf);
+      m->fx_rowexp = std::move(o.fx_rowexp);
+      m->fx_bdig = std::move(o.fx_bdig);
+      m->fx_cexp = std::move(o.fx_cexp);
+      m->fx_part = std::move(o.fx_part);
+      if (o.dim == m->dim)
+        for (int i = 0; i < 8; ++i)
+          if (o.solvers[i]) {
+            o.solvers[i]->rebind();
+            m->solvers[i] = std::move(o.solvers[i]);
+          }
+    }
     h->mme = std::move(m);
   });
 }

@@ -26,6 +26,9 @@ struct Csr {
 // Type-erased per-RHS-count solver workspace (see mme.cu).
 struct SolverBase {
   virtual ~SolverBase() = default;
+  // forget everything derived from an MME (kept buffers are re-checked and
+  // rewritten before use) when the solver moves to a rebuilt MME of the same size
+  virtual void rebind() = 0;
 };
 
 struct Mme {
