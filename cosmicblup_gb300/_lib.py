@@ -66,6 +66,7 @@ SIGNATURES = [
                                         C.POINTER(C.c_int64), C.c_void_p]),
     ("cbx_reml_solve", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                  C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_void_p, C.c_void_p]),
+    ("cbx_mme_keep_warm", C.c_int, [C.c_void_p, C.c_int32]),
     ("cbx_profile_enable", C.c_int, [C.c_void_p, C.c_int32]),
     ("cbx_profile_read", C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int64), C.POINTER(C.c_double),
                                    C.POINTER(C.c_double)]),
@@ -165,6 +166,11 @@ class Handle:
     def check(self, rc: int) -> None:
         if rc != CBX_OK:
             raise CbxError(rc, lib().cbx_last_error(self._h).decode())
+
+    def keep_warm(self, on: bool) -> None:
+        """MMEs rebuilt later with the same shape start their solves from the
+        previous MME's last data and probe solutions (cbx_mme_keep_warm)."""
+        self.check(lib().cbx_mme_keep_warm(self.raw, 1 if on else 0))
 
     def profile(self, on: bool) -> None:
         self.check(lib().cbx_profile_enable(self.raw, 1 if on else 0))

@@ -41,6 +41,10 @@ struct cbx_handle {
   int64_t probe_z_q = -1;
   // mixed-model equations and REML state
   std::unique_ptr<cbx::Mme> mme;
+  // cbx_mme_keep_warm: an MME rebuilt with the same shape starts its solves from
+  // the previous MME's last data and probe solutions (a REML run whose records
+  // are uploaded again at every iteration)
+  bool keep_warm = false;
   // library handles (cuSOLVER / cuBLAS) and dense exact AI state, owned here
   std::shared_ptr<void> libs_slot;
   std::shared_ptr<void> dense_slot;

@@ -1375,35 +1375,51 @@ static void assemble_wtw(int64_t n_rec, int64_t p, int64_t q, const double* y, c
     for (int64_t i = pt.r0; i < pt.r1; ++i)
       record(i, [&](int64_t r, int64_t c, double v) { ent[pt.cnt[r]++] = Ent{(int32_t)c, v}; });
   });
-  // 4. rows sorted by column (stable), unique entries per row; the threads take
-  // row ranges of about equal numbers of entries
+  // 4. each row's entries sorted stably by column (insertion sort for short rows,
+  // an LSD radix sort on 8-bit column digits for long ones), then each run of
+  // equal columns summed in order from 0.0 and the row compacted at its start:
+  // the result of one stable sort by (row, column) and a sequential sum.  The
+  // threads take row ranges of about equal numbers of entries.
   std::vector<int64_t> rb(T + 1, dim);
   rb[0] = 0;
   for (int t = 1; t < T; ++t)
     rb[t] = std::lower_bound(start.begin(), start.end(), start[dim] * t / T) - start.begin();
   for (int t = 1; t <= T; ++t) rb[t] = std::min(dim, std::max(rb[t], rb[t - 1]));
   std::vector<int32_t> uniq(dim, 0);
-  auto rows_of = [&](int t, int64_t& r0, int64_t& r1) {
-    r0 = rb[t];
-    r1 = rb[t + 1];
-  };
+  int key_bits = 1;
+  while (key_bits < 31 && (int64_t(1) << key_bits) < dim) ++key_bits;
   run([&](int t) {
-    int64_t r0, r1;
-    rows_of(t, r0, r1);
-    for (int64_t r = r0; r < r1; ++r) {
-      const int64_t e0 = start[r], e1 = start[r + 1];
-      if (e1 - e0 > 32) {
-        std::stable_sort(&ent[e0], &ent[e1], [](const Ent& a, const Ent& b) { return a.c < b.c; });
-      } else {
-        for (int64_t e = e0 + 1; e < e1; ++e) {   // insertion sort: stable
+    std::vector<Ent> tmp;
+    for (int64_t r = rb[t]; r < rb[t + 1]; ++r) {
+      const int64_t e0 = start[r], e1 = start[r + 1], n = e1 - e0;
+      if (n <= 48) {
+        for (int64_t e = e0 + 1; e < e1; ++e) {
           const Ent x = ent[e];
           int64_t k = e;
           for (; k > e0 && ent[k - 1].c > x.c; --k) ent[k] = ent[k - 1];
           ent[k] = x;
         }
+      } else {
+        if ((int64_t)tmp.size() < n) tmp.resize(n);
+        Ent* a = &ent[e0];
+        Ent* b = tmp.data();
+        for (int sh = 0; sh < key_bits; sh += 8) {
+          int64_t cnt[257] = {0};
+          for (int64_t i = 0; i < n; ++i) cnt[((a[i].c >> sh) & 255) + 1]++;
+          if (cnt[((a[0].c >> sh) & 255) + 1] == n) continue;  // one digit value: already in order
+          for (int d = 0; d < 256; ++d) cnt[d + 1] += cnt[d];
+          for (int64_t i = 0; i < n; ++i) b[cnt[(a[i].c >> sh) & 255]++] = a[i];
+          std::swap(a, b);
+        }
+        if (a != &ent[e0]) std::copy(a, a + n, &ent[e0]);
       }
       int32_t u = 0;
-      for (int64_t e = e0; e < e1; ++e) u += (e == e0 || ent[e].c != ent[e - 1].c) ? 1 : 0;
+      for (int64_t e = e0; e < e1;) {
+        const int32_t c = ent[e].c;
+        double v = 0.0;
+        while (e < e1 && ent[e].c == c) v += ent[e++].v;
+        ent[e0 + u++] = Ent{c, v};
+      }
       uniq[r] = u;
     }
   });
@@ -1414,21 +1430,13 @@ static void assemble_wtw(int64_t n_rec, int64_t p, int64_t q, const double* y, c
   for (int64_t r = 0; r < dim; ++r) out.ptr[r + 1] = out.ptr[r] + uniq[r];
   out.col.resize(out.ptr[dim]);
   out.val.resize(out.ptr[dim]);
-  // 5. duplicates summed in their order
+  // 5. the compacted rows into the CSR arrays
   run([&](int t) {
-    int64_t r0, r1;
-    rows_of(t, r0, r1);
-    for (int64_t r = r0; r < r1; ++r) {
-      int64_t o = out.ptr[r];
-      for (int64_t e = start[r]; e < start[r + 1];) {
-        const int32_t c = ent[e].c;
-        double v = 0.0;
-        while (e < start[r + 1] && ent[e].c == c) v += ent[e++].v;
-        out.col[o] = c;
-        out.val[o] = v;
-        ++o;
+    for (int64_t r = rb[t]; r < rb[t + 1]; ++r)
+      for (int32_t k = 0; k < uniq[r]; ++k) {
+        out.col[out.ptr[r] + k] = ent[start[r] + k].c;
+        out.val[out.ptr[r] + k] = ent[start[r] + k].v;
       }
-    }
   });
 }
 
@@ -1572,6 +1580,25 @@ extern "C" int cbx_mme_create(cbx_handle* h, int64_t n_rec, int64_t p, int64_t q
             o.solvers[i]->rebind();
             m->solvers[i] = std::move(o.solvers[i]);
           }
+      if (h->keep_warm && o.dim == m->dim && o.p == m->p && o.q == m->q) {
+        // the last data and probe solutions start the new MME's solves; the probe
+        // right-hand sides [0; z_j] depend only on the seed, p and q (column 0,
+        // W'y, is rewritten by every iteration); residual carries and the
+        // forward state belong to the old operator and are not kept
+        m->last_solution = std::move(o.last_solution);
+        m->has_last = o.has_last;
+        m->last_lam = o.last_lam;
+        m->probe_x = std::move(o.probe_x);
+        m->probe_r = std::move(o.probe_r);
+        m->probe_lam = o.probe_lam;
+        m->probe_r_ok.assign(o.probe_r_ok.size(), 0);
+        m->probe_seed = o.probe_seed;
+        m->em_B = std::move(o.em_B);
+        m->probe_have = o.probe_have;
+        m->em_B_seed = o.em_B_seed;
+        m->probe_cap = o.probe_cap;
+        m->probe_zv = std::move(o.probe_zv);
+      }
     }
     h->mme = std::move(m);
   });
@@ -1648,9 +1675,10 @@ extern "C" int cbx_mme_set_qinv_dense(cbx_handle* h, const double* Qinv, int64_t
                                cudaMemcpyDeviceToDevice, s));
     m.has_dense = true;
     m.has_sparse = false;
-    m.drop_carry();
+    m.drop_carry(h->keep_warm);
     CBX_CUDA(cudaStreamSynchronize(s));
-    for (auto& sp : m.solvers) sp.reset();
+    for (auto& sp : m.solvers)
+      if (sp) sp->rebind();  // workspaces kept; everything derived from the operator recomputed
   });
 }
 
@@ -1681,7 +1709,7 @@ extern "C" int cbx_mme_set_qinv_split(cbx_handle* h, const int64_t* a_ptr, const
     upload_csr<float>(s, q, ptr, col, val, m.Qs32);
     m.has_sparse = true;
     m.has_dense = ng > 0;
-    m.drop_carry();
+    m.drop_carry(h->keep_warm);
     if (ng > 0) {
       CBX_REQUIRE(gmap, CBX_ERR_ARG, "genotyped map missing");
       CBX_REQUIRE(Gd || (h->Hd.p && h->Hd_n == ng), CBX_ERR_STATE,
@@ -1715,7 +1743,8 @@ extern "C" int cbx_mme_set_qinv_split(cbx_handle* h, const int64_t* a_ptr, const
     m.diagQ.resize(q);
     CBX_CUDA(cudaMemcpyAsync(m.diagQ.p, diag.data(), q * sizeof(double), cudaMemcpyHostToDevice, s));
     CBX_CUDA(cudaStreamSynchronize(s));
-    for (auto& sp : m.solvers) sp.reset();
+    for (auto& sp : m.solvers)
+      if (sp) sp->rebind();  // workspaces kept; everything derived from the operator recomputed
   });
 }
 
@@ -1752,6 +1781,10 @@ extern "C" int cbx_pcg_solve(cbx_handle* h, double lambda, int32_t nrhs, const d
     for (int c = 0; c < nrhs; ++c)
       if (r.status[c] == sv::COL_NONFINITE) throw Error(CBX_ERR_NONFINITE, "non-finite PCG iterate");
   });
+}
+
+extern "C" int cbx_mme_keep_warm(cbx_handle* h, int32_t on) {
+  return cbx_guard(h, [&] { h->keep_warm = on != 0; });
 }
 
 // Kernel timing of the dense block product (see include/cbx.h).

@@ -8,6 +8,7 @@
 // FP64 copies drive refinement and the plain FP64 path; FP32 copies drive the
 // mixed-precision bulk iterations.
 #pragma once
+#include <algorithm>
 #include <memory>
 #include <vector>
 #include "devbuf.h"
@@ -113,11 +114,17 @@ struct Mme {
     int precision = -1, seed = -1, solved = 0;
     double uQu = 0.0, e_sse = 0.0;
   } fwd;
-  void drop_carry() {
-    has_last = has_last_resid = false;
-    probe_lam.clear();
-    probe_r_ok.clear();
+  // The operator changed: residual carries and the forward state no longer hold.
+  // keep_solutions leaves the last solutions as starting points of the next solves.
+  void drop_carry(bool keep_solutions = false) {
+    has_last_resid = false;
+    std::fill(probe_r_ok.begin(), probe_r_ok.end(), 0);
     fwd.valid = false;
+    if (!keep_solutions) {
+      has_last = false;
+      probe_lam.clear();
+      probe_r_ok.clear();
+    }
   }
   // persistent solver workspaces, indexed by log2 of the RHS block width
   std::unique_ptr<SolverBase> solvers[8];

@@ -158,6 +158,15 @@ int cbx_mme_create(cbx_handle* h, int64_t n_rec, int64_t p, int64_t q, const dou
                    const int32_t* aid, const int64_t* fx_ptr, const int32_t* fx_col,
                    const double* fx_val);
 
+/* on != 0: an MME created later with the same p and q keeps the previous MME's
+ * last data solution and probe solutions as the starting points of its solves
+ * (the reference keeps last_solution across the iterations of one run,
+ * src/core/vce.cpp:1226-1235); a later cbx_mme_set_qinv_* keeps them too.
+ * Residual carries to a new lambda and the gradient's forward state are
+ * dropped, since they belong to the old operator.  Off by default: every MME
+ * then starts cold, and its results do not depend on earlier MMEs. */
+int cbx_mme_keep_warm(cbx_handle* h, int32_t on);
+
 /* Qinv dense, q x q (DenseMatrixAdapter, src/core/matrix_adapter.h:116-153).
  * Qinv == NULL takes the inverse left on the device by cbx_invert_psd. */
 int cbx_mme_set_qinv_dense(cbx_handle* h, const double* Qinv, int64_t q);
