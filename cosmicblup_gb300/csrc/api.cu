@@ -45,6 +45,9 @@ int cbx_create(int device, cbx_handle** out) {
     h->device = device;
     h->num_sms = prop.multiProcessorCount;
     CBX_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    CBX_CUDA(cudaStreamCreateWithFlags(&h->stream2, cudaStreamNonBlocking));
+    CBX_CUDA(cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming));
+    CBX_CUDA(cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming));
     h->status.resize(4);
     h->status.zero(h->stream);
     CBX_CUDA(cudaStreamSynchronize(h->stream));
@@ -78,6 +81,9 @@ int cbx_destroy(cbx_handle* h) {
     if (tmp->trace_start) cudaEventDestroy(tmp->trace_start);
     if (tmp->timer_a) cudaEventDestroy(tmp->timer_a);
     if (tmp->timer_b) cudaEventDestroy(tmp->timer_b);
+    if (tmp->ev_fork) cudaEventDestroy(tmp->ev_fork);
+    if (tmp->ev_join) cudaEventDestroy(tmp->ev_join);
+    if (tmp->stream2) cudaStreamDestroy(tmp->stream2);
     if (tmp->stream) cudaStreamDestroy(tmp->stream);
   }
   delete h;

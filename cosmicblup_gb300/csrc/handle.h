@@ -17,6 +17,10 @@ struct cbx_handle {
   int device = 0;
   int num_sms = 0;
   cudaStream_t stream = nullptr;
+  // second stream of the PCG operator: the sparse part runs on it beside the
+  // dense block product on `stream` (fork / join events, captured into graphs)
+  cudaStream_t stream2 = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   std::string last_error;
   int64_t launches = 0;
   cbx::DevBuf<int> status;  // device-side error word(s)

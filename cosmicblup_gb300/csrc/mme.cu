@@ -252,6 +252,7 @@ struct Workspace {
   DevBuf<int> active;
   DevBuf<unsigned> done;  // arrival counter of k_scalar_beta_c (reset by its last block)
   int nblk_vec = 0, nblk_spmv = 0;
+  int nblk_dadd = 0;      // blocks of k_dense_add (their pq partials follow k_spmv's)
   int64_t dim = -1, p_ = -1, ng_ = -1, ld_ = -1;
   int nseg_ = -1;
   void alloc(const Mme& m, int num_sms) {
@@ -265,8 +266,9 @@ struct Workspace {
     // (2 blocks per SM ran k_update at about a quarter of HBM bandwidth)
     nblk_vec = (int)grid_for(n, sv::NT, 8 * num_sms);
     nblk_spmv = (int)m.p + (int)grid_for(m.dim - m.p, 8, 6 * num_sms);
+    nblk_dadd = m.has_dense ? (int)grid_for(m.ng * S, sv::NT, 2 * num_sms) : 0;
     part.resize((size_t)nblk_vec * 3 * S);
-    pq_part.resize((size_t)nblk_spmv * S);
+    pq_part.resize((size_t)(nblk_spmv + nblk_dadd) * S);
     rz_fix.resize((size_t)std::max<int64_t>(m.p, 1) * S);
     tol.resize(S);
     col.resize(S);
@@ -398,6 +400,22 @@ static bool use_fx() {
 static bool log_refine() {
   static int v = env_int("CBX_LOG_REFINE", 0);
   return v != 0;
+}
+
+// With CBX_OVERLAP=1 the FP32 operator's sparse part (W'W, the sparse Qinv,
+// the fixed rows) runs on the handle's second stream beside the dense block
+// product, and the block term is added to the genotyped rows afterwards.  Off
+// by default: on GB300 at the 200k-animal / 20k-genotyped ssGBLUP step the
+// co-resident SpMV blocks slowed the block product from 0.82 to 0.68 of the
+// copy bandwidth, and the step from 66.4 to 68.6 ms.  Never on while a launch
+// trace runs, whose per-launch attribution assumes one stream.
+static bool use_overlap() {
+  static int v = env_int("CBX_OVERLAP", 0);
+  return v != 0;
+}
+template <typename T>
+static bool matvec_split(const cbx_handle* h, const sv::OpView<T>& op) {
+  return sizeof(T) == 4 && op.Qd && use_overlap() && !h->trace_on;
 }
 
 // CUDA graphs for the PCG iteration body (environment CBX_GRAPHS=0 launches
@@ -662,12 +680,41 @@ void matvec(cbx_handle* h, const sv::OpView<T>& op, Workspace<T, S>& w, const T*
   } else {
     // FP32: gather the dense-block rows, their FP64 column sums, the product
     // (the populated 32-column groups only)
+    const bool split = matvec_split(h, op);
+    if (split) {
+      // the sparse part on the second stream, beside the block product: k_spmv
+      // without the block term writes every row and its pq partials
+      cudaStream_t s2 = h->stream2;
+      CBX_CUDA(cudaEventRecord(h->ev_fork, s));
+      CBX_CUDA(cudaStreamWaitEvent(s2, h->ev_fork, 0));
+      sv::OpView<T> ops = op;
+      ops.Qd = nullptr;
+      if (use_D && h->mme->nseg > 0) {
+        const Mme& mm = *h->mme;
+        sv::k_fix_seg<T, S><<<mm.nseg, sv::NT, 0, s2>>>(ops, mm.seg_row.p, mm.seg_lo.p, mm.seg_hi.p, X,
+                                                        w.seg_part.p, active, ncp);
+        h->launched("k_fix_seg<f32>");
+      }
+      sv::k_spmv<T, S><<<w.nblk_spmv, sv::NT, 0, s2>>>(ops, X, nullptr, 1, nullptr, 0.0, h->mme->fix_seg_ptr.p,
+                                                        w.seg_part.p, (T)lam, use_D, Y, P, pq_part, active, ncp);
+      h->launched("k_spmv<f32>");
+      CBX_CUDA(cudaEventRecord(h->ev_join, s2));
+    }
     sv::k_gather_t<T, S><<<grid_for(ncp * op.ld, 256, 16 * h->num_sms), 256, 0, s>>>(X, w.Vt.p, op.p, op.ng, op.ld,
                                                                                  op.gmap, active, S, ncp);
     h->launched("k_gather_t<f32>");
     sv::k_colsum_vt<T><<<ncp, 1024, 0, s>>>(w.Vt.p, op.ld, op.ng, w.colsum.p);
     h->launched("k_colsum_vt<f32>");
     tsplit = product_from_vt<T, S>(h, op, w, active, ncols);
+    if (split) {
+      // the block term of the genotyped rows, once both are done
+      CBX_CUDA(cudaStreamWaitEvent(s, h->ev_join, 0));
+      sv::k_dense_add<T, S><<<w.nblk_dadd, sv::NT, 0, s>>>(op, w.Tout.p, tsplit, colsum, tshift, (T)lam, Y, P,
+                                                           pq_part ? pq_part + (size_t)w.nblk_spmv * S : nullptr,
+                                                           active, ncp);
+      h->launched("k_dense_add<f32>");
+      return;
+    }
   }
   if (use_D && h->mme->nseg > 0) {
     const Mme& mm = *h->mme;
@@ -781,7 +828,8 @@ void run_pcg(cbx_handle* h, Mme& m, const sv::OpView<T>& op, Workspace<T, S>& w,
     }
     for (int j = 0; j < CHECK; ++j) {
       matvec<T, S>(h, op, w, w.P.p, w.Q.p, lam, 1, w.P.p, w.pq_part.p, w.active.p, false, ncols);
-      sv::k_scalar_alpha_c<S><<<S, sv::NTC, 0, s>>>(w.col.p, w.pq_part.p, w.nblk_spmv);
+      sv::k_scalar_alpha_c<S><<<S, sv::NTC, 0, s>>>(w.col.p, w.pq_part.p,
+                                                    w.nblk_spmv + (matvec_split(h, op) ? w.nblk_dadd : 0));
       h->launched(sizeof(T) == 4 ? "k_scalar_alpha<f32>" : "k_scalar_alpha<f64>");
       sv::k_update<T, S><<<w.nblk_vec, sv::NT, 0, s>>>(op, w.col.p, X, Xlo, w.R.p, w.Z.p, w.P.p, w.Q.p, w.part.p);
       h->launched(sizeof(T) == 4 ? "k_update<f32>" : "k_update<f64>");

@@ -751,6 +751,38 @@ __device__ __forceinline__ void spmv_random_row(const OpView<T>& op, int64_t i, 
   }
 }
 
+// Dense-block term of the genotyped rows when it is added after the sparse
+// part (k_spmv run with the dense term left out, beside the block product):
+// Y[p + gmap[k]] += lam (sum of the K-split partials of row k + tshift colsum),
+// in a fixed order, and this block's sum_i P[i] (that term) per column into
+// pq_part (thread c = tid % S keeps column c; columns >= ncp are not touched).
+template <typename T, int S>
+__global__ void __launch_bounds__(NT) k_dense_add(OpView<T> op, const T* __restrict__ Tout, int tsplit,
+                                                  const double* __restrict__ colsum, double tshift, T lam,
+                                                  T* __restrict__ Y, const T* __restrict__ P,
+                                                  double* __restrict__ pq_part, const int* __restrict__ active,
+                                                  int ncp) {
+  if (active && *active == 0) return;
+  __shared__ double red[NT];
+  const int c = threadIdx.x % S;
+  DotAcc<T> pq;
+  const double sh = colsum ? tshift * colsum[c] : 0.0;
+  const int64_t total = (int64_t)op.ng * S;
+  if (c < ncp)
+    for (int64_t idx = blockIdx.x * (int64_t)NT + threadIdx.x; idx < total; idx += (int64_t)gridDim.x * NT) {
+      const int64_t k = idx / S;
+      T q = T(0);
+      for (int t = 0; t < tsplit; ++t) q += Tout[((int64_t)t * op.ng + k) * S + c];
+      q += (T)sh;
+      const T d = lam * q;
+      const int64_t i = op.p + op.gmap[k];
+      Y[i * S + c] += d;
+      if (P) pq.add(P[i * S + c], d);
+    }
+  const double t = block_sum_cols<S>(pq.value(), red);
+  if (pq_part && threadIdx.x < S) pq_part[(int64_t)blockIdx.x * S + c] = t;
+}
+
 // Block totals per column of the pq terms left by spmv_random_row: blk[c] for
 // every c < S (fixed order: lanes, then warps).
 template <int S>
