@@ -31,10 +31,12 @@ struct cbx_handle {
   int64_t G_n = 0;
   cbx::DevBuf<double> Ginv;
   int64_t Ginv_n = 0;
+  int64_t Ginv_gen = 0;  // counts the writes of Ginv
   // dense block of the single-step H^-1 (G_blend^-1 - A22^-1, ng x ng) left on
   // the device by cbx_ssgblup_qinv
   cbx::DevBuf<double> Hd;
   int64_t Hd_n = 0;
+  int64_t Hd_gen = 0;    // counts the writes of Hd
   // Rademacher probe vectors of the trace estimator's stream (q x count,
   // column-major) for seed probe_z_seed and order probe_z_q: deterministic, so
   // each 16-probe batch is drawn on the host once and later MMEs of the handle

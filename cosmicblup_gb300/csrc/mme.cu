@@ -1279,22 +1279,39 @@ double record_residual(cbx_handle* h, const double* sol_dev, double* e_dev) {
 
 // ---------------------------------------------------------------------------
 // host assembly helpers
-template <typename T>
-static void upload_csr(cudaStream_t s, int64_t rows, const std::vector<int32_t>& ptr, const std::vector<int32_t>& col,
-                       const std::vector<double>& val, Csr<T>& out) {
-  out.rows = (int32_t)rows;
-  out.nnz = (int64_t)col.size();
-  out.ptr.resize(rows + 1);
-  out.col.resize(std::max<size_t>(col.size(), 1));
-  out.val.resize(std::max<size_t>(val.size(), 1));
-  CBX_CUDA(cudaMemcpyAsync(out.ptr.p, ptr.data(), (rows + 1) * sizeof(int32_t), cudaMemcpyHostToDevice, s));
-  if (!col.empty()) {
-    CBX_CUDA(cudaMemcpyAsync(out.col.p, col.data(), col.size() * sizeof(int32_t), cudaMemcpyHostToDevice, s));
-    std::vector<T> tv(val.begin(), val.end());
-    CBX_CUDA(cudaMemcpyAsync(out.val.p, tv.data(), tv.size() * sizeof(T), cudaMemcpyHostToDevice, s));
-    CBX_CUDA(cudaStreamSynchronize(s));
-  }
+__global__ void k_d2f(const double* __restrict__ a, int64_t n, float* __restrict__ b) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    b[i] = (float)a[i];
 }
+
+// A CSR straight from the caller's arrays (page-locked ones are copied by DMA)
+// into its FP64 copy, and on the device into the FP32 copy.
+static void upload_csr_pair(cbx_handle* h, int64_t rows, const std::vector<int32_t>& ptr, const int32_t* col,
+                            const double* val, Csr<double>& d, Csr<float>& f) {
+  cudaStream_t s = h->stream;
+  const int64_t nnz = ptr[rows];
+  d.rows = (int32_t)rows;
+  d.nnz = nnz;
+  f.rows = (int32_t)rows;
+  f.nnz = nnz;
+  d.ptr.resize(rows + 1);
+  f.ptr.resize(rows + 1);
+  d.col.resize(std::max<int64_t>(nnz, 1));
+  f.col.resize(std::max<int64_t>(nnz, 1));
+  d.val.resize(std::max<int64_t>(nnz, 1));
+  f.val.resize(std::max<int64_t>(nnz, 1));
+  CBX_CUDA(cudaMemcpyAsync(d.ptr.p, ptr.data(), (rows + 1) * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+  CBX_CUDA(cudaMemcpyAsync(f.ptr.p, d.ptr.p, (rows + 1) * sizeof(int32_t), cudaMemcpyDeviceToDevice, s));
+  if (nnz > 0) {
+    CBX_CUDA(cudaMemcpyAsync(d.col.p, col, nnz * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+    CBX_CUDA(cudaMemcpyAsync(f.col.p, d.col.p, nnz * sizeof(int32_t), cudaMemcpyDeviceToDevice, s));
+    CBX_CUDA(cudaMemcpyAsync(d.val.p, val, nnz * sizeof(double), cudaMemcpyHostToDevice, s));
+    k_d2f<<<grid_for(nnz, 256, 4 * h->num_sms), 256, 0, s>>>(d.val.p, nnz, f.val.p);
+    h->launched("k_d2f");
+  }
+  CBX_CUDA(cudaStreamSynchronize(s));  // the caller's arrays are read before return
+}
+
 
 // W'W as CSR and W'y from the records (mme_builder.cpp:107-176, 321-387) on
 // host threads: every record emits its triplets (fixed x fixed pairs, fixed x
@@ -1541,8 +1558,7 @@ extern "C" int cbx_mme_create(cbx_handle* h, int64_t n_rec, int64_t p, int64_t q
       }
       CBX_CUDA(cudaStreamSynchronize(s));
     }
-    upload_csr<double>(s, dim, ptr, col, val, m->D64);
-    upload_csr<float>(s, dim, ptr, col, val, m->D32);
+    upload_csr_pair(h, dim, ptr, col.data(), val.data(), m->D64, m->D32);
     m->diagD.resize(dim);
     CBX_CUDA(cudaMemcpyAsync(m->diagD.p, diag.data(), dim * sizeof(double), cudaMemcpyHostToDevice, s));
     m->rhs.resize(dim);
@@ -1622,6 +1638,14 @@ extern "C" int cbx_mme_create(cbx_handle* h, int64_t n_rec, int64_t p, int64_t q
       m->fx_bdig = std::move(o.fx_bdig);
       m->fx_cexp = std::move(o.fx_cexp);
       m->fx_part = std::move(o.fx_part);
+      // the copies stay tied to their source block (upload_dense keeps them when
+      // the new MME takes the same, unchanged block)
+      m->ng = o.ng;
+      m->ld = o.ld;
+      m->qshift = o.qshift;
+      m->fx_rows_ok = o.fx_rows_ok;
+      m->planes_src = o.planes_src;
+      m->planes_gen = o.planes_gen;
       if (o.dim == m->dim)
         for (int i = 0; i < 8; ++i)
           if (o.solvers[i]) {
@@ -1655,8 +1679,15 @@ extern "C" int cbx_mme_create(cbx_handle* h, int64_t n_rec, int64_t p, int64_t q
 // The dense block on the device: the FP64 copy (pitch ld) and the shifted
 // low-precision copies (see Mme::qshift).  The shift
 // is the mean off-diagonal entry, summed in a fixed order.
-static void upload_dense(cbx_handle* h, Mme& m, const double* src, int64_t ng) {
+// gen >= 0: src is a device block of the handle at that generation; an MME
+// whose copies were made from it keeps them.
+static void upload_dense(cbx_handle* h, Mme& m, const double* src, int64_t ng, int64_t gen = -1) {
   cudaStream_t s = h->stream;
+  if (gen >= 0 && m.planes_src == src && m.planes_gen == gen && m.ng == ng && m.Qd64.p && m.Qd32.p &&
+      m.Qlo32.p && (m.Qbf.p != nullptr) == (use_bf16() && m.ld % 8 == 0))
+    return;
+  m.planes_src = nullptr;
+  m.planes_gen = -1;
   m.ng = ng;
   m.ld = (ng + 3) / 4 * 4;
   m.Qd64.resize((size_t)ng * m.ld);
@@ -1689,6 +1720,10 @@ static void upload_dense(cbx_handle* h, Mme& m, const double* src, int64_t ng) {
   } else {
     m.Qbf.release();
   }
+  if (gen >= 0) {
+    m.planes_src = src;
+    m.planes_gen = gen;
+  }
 }
 
 // Dense Qinv (q x q, symmetric, row- or column-major alike).  Qinv == NULL uses
@@ -1710,7 +1745,7 @@ extern "C" int cbx_mme_set_qinv_dense(cbx_handle* h, const double* Qinv, int64_t
       CBX_REQUIRE(h->Ginv.p && h->Ginv_n == q, CBX_ERR_STATE, "no device G inverse of matching order");
       src = h->Ginv.p;
     }
-    upload_dense(h, m, src, q);
+    upload_dense(h, m, src, q, Qinv ? -1 : h->Ginv_gen);
     std::vector<int32_t> idm(q);
     for (int64_t i = 0; i < q; ++i) idm[i] = (int32_t)i;
     m.gmap.resize(q);
@@ -1744,17 +1779,19 @@ extern "C" int cbx_mme_set_qinv_split(cbx_handle* h, const int64_t* a_ptr, const
     CBX_CUDA(cudaSetDevice(h->device));
     cudaStream_t s = h->stream;
     const int64_t q = m.q;
-    std::vector<int32_t> ptr(q + 1), col(a_col, a_col + a_ptr[q]);
-    std::vector<double> val(a_val, a_val + a_ptr[q]);
-    for (int64_t i = 0; i <= q; ++i) ptr[i] = (int32_t)a_ptr[i];
+    CBX_REQUIRE(a_ptr[q] < (int64_t)INT32_MAX, CBX_ERR_UNSUPPORTED, "A^-1 has more than 2^31 entries");
+    std::vector<int32_t> ptr(q + 1);
     std::vector<double> diag(q, 0.0);
-    for (int64_t i = 0; i < q; ++i)
+    for (int64_t i = 0; i < q; ++i) {
+      CBX_REQUIRE(a_ptr[i + 1] >= a_ptr[i], CBX_ERR_ARG, "A^-1 row pointers not monotone");
+      ptr[i] = (int32_t)a_ptr[i];
       for (int64_t j = a_ptr[i]; j < a_ptr[i + 1]; ++j) {
         CBX_REQUIRE(a_col[j] >= 0 && a_col[j] < q, CBX_ERR_ARG, "A^-1 column out of range");
         if (a_col[j] == i) diag[i] += a_val[j];
       }
-    upload_csr<double>(s, q, ptr, col, val, m.Qs64);
-    upload_csr<float>(s, q, ptr, col, val, m.Qs32);
+    }
+    ptr[q] = (int32_t)a_ptr[q];
+    upload_csr_pair(h, q, ptr, a_col, a_val, m.Qs64, m.Qs32);
     m.has_sparse = true;
     m.has_dense = ng > 0;
     m.drop_carry(h->keep_warm);
@@ -1781,7 +1818,7 @@ extern "C" int cbx_mme_set_qinv_split(cbx_handle* h, const int64_t* a_ptr, const
                                  cudaMemcpyDeviceToHost, s));
       CBX_CUDA(cudaStreamSynchronize(s));
       for (int64_t k = 0; k < ng; ++k) diag[gmap[k]] += dd[k];
-      upload_dense(h, m, src, ng);
+      upload_dense(h, m, src, ng, Gd ? -1 : h->Hd_gen);
       m.gmap.resize(ng);
       m.ginv.resize(q);
       CBX_CUDA(cudaMemcpyAsync(m.gmap.p, gmap, ng * sizeof(int32_t), cudaMemcpyHostToDevice, s));

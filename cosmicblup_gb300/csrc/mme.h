@@ -59,6 +59,11 @@ struct Mme {
   DevBuf<float> Qlo32;             // fl32(Qd - qshift - Qd32): with Qd32 the float-float block
   double qshift = 0.0;
   DevBuf<uint16_t> Qbf;            // bf16(Qd - qshift), ng x ld (only with CBX_BF16=1)
+  // the handle's device block these copies were made from (G^-1 of
+  // cbx_invert_psd or the H^-1 block of cbx_ssgblup_qinv) and its generation
+  // there; a later MME built from the same, unchanged block keeps them
+  const void* planes_src = nullptr;
+  int64_t planes_gen = -1;
   // row scales of the Qd32 / Qlo32 planes for the fixed-point tensor-core
   // refinement product (valid while fx_rows_ok), and its scratch
   DevBuf<int32_t> fx_rowexp;

@@ -393,6 +393,7 @@ extern "C" int cbx_ssgblup_qinv(cbx_handle* h, int64_t n, const int64_t* dam, co
     // the block stays on the device for later MMEs of this handle
     h->Hd = std::move(Gd);
     h->Hd_n = ng;
+    ++h->Hd_gen;
     if (int rc = cbx_mme_set_qinv_split(h, ap.data(), ac.data(), av.data(), nullptr, ng, gmap); rc != CBX_OK)
       throw Error(rc, h->last_error);
   });

@@ -1718,6 +1718,7 @@ extern "C" int cbx_invert_psd(cbx_handle* h, const double* M, int64_t n, double 
       sp = h->G.p;
     }
     h->Ginv.resize((size_t)n * n);
+    ++h->Ginv_gen;
     invert_psd_device(h, sp, n, ridge, h->Ginv.p);
     h->Ginv_n = n;
     if (Minv) CBX_CUDA(cudaMemcpyAsync(Minv, h->Ginv.p, (size_t)n * n * sizeof(double), cudaMemcpyDeviceToHost, s));
