@@ -73,6 +73,7 @@ int cbx_destroy(cbx_handle* h) {
     tmp->Ginv.release();
     tmp->mme.reset();
     tmp->dense_slot.reset();
+    tmp->wtw_slot.reset();
     tmp->libs_slot.reset();
     tmp->status.release();
     for (auto& r : tmp->prof) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }

@@ -54,6 +54,8 @@ struct cbx_handle {
   // library handles (cuSOLVER / cuBLAS) and dense exact AI state, owned here
   std::shared_ptr<void> libs_slot;
   std::shared_ptr<void> dense_slot;
+  // scratch of the device W'W assembly (wtw.cu), kept between MMEs
+  std::shared_ptr<void> wtw_slot;
   // genotypes kept on the device by cbx_geno_attach (matrix-free Z / Z^T products)
   std::shared_ptr<void> geno_slot;
   // device address of the static scratch array of cbx_dense_apply_noalloc,

@@ -1320,12 +1320,36 @@ static void upload_csr_pair(cbx_handle* h, int64_t rows, const std::vector<int32
 // record order within each row, so each row's entries come out as from one
 // sequential pass (a stable counting sort).  Each row is then sorted stably by
 // column and its duplicates summed in that order, so W'W does not depend on the
-// number of threads.  W'y and y'y are summed in record order.
+// number of threads.
 struct WtW {
   std::vector<int32_t> ptr, col;
-  std::vector<double> val, rhs;
-  double yty = 0.0;
+  std::vector<double> val;
 };
+
+// The records' checks, W'y and y'y (mme_builder.cpp:321-387), in record order.
+static void records_rhs(int64_t n_rec, int64_t p, int64_t q, const double* y, const int32_t* aid,
+                        const int64_t* fx_ptr, const int32_t* fx_col, const double* fx_val, std::vector<double>& rhs,
+                        double& yty) {
+  rhs.assign(p + q, 0.0);
+  yty = 0.0;
+  for (int64_t i = 0; i < n_rec; ++i) {
+    CBX_REQUIRE(fx_ptr[i + 1] >= fx_ptr[i], CBX_ERR_ARG, "fx_ptr not monotone");
+    CBX_REQUIRE(std::isfinite(y[i]), CBX_ERR_NONFINITE, "non-finite phenotype");
+    for (int64_t a = fx_ptr[i]; a < fx_ptr[i + 1]; ++a) {
+      CBX_REQUIRE(fx_col[a] >= 0 && fx_col[a] < p, CBX_ERR_ARG, "fixed-effect column out of range");
+      rhs[fx_col[a]] += fx_val[a] * y[i];
+    }
+    const int32_t an = aid[i];
+    if (an > 0 && an <= q) rhs[p + an - 1] += y[i];
+    yty += y[i] * y[i];
+  }
+  CBX_REQUIRE(fx_ptr[n_rec] < (int64_t)INT32_MAX, CBX_ERR_UNSUPPORTED, "more than 2^31 fixed-effect entries");
+}
+
+// W'W on the device from the uploaded records (wtw.cu); the host assembly below
+// builds the same CSR bit for bit and runs when the environment sets CBX_WTW_HOST=1.
+void wtw_device(cbx_handle* h, Mme& m, std::vector<int32_t>& ptr_fix, std::vector<double>& A11);
+static bool use_host_wtw() { return env_int("CBX_WTW_HOST", 0) != 0; }
 
 static void assemble_wtw(int64_t n_rec, int64_t p, int64_t q, const double* y, const int32_t* aid,
                          const int64_t* fx_ptr, const int32_t* fx_col, const double* fx_val, WtW& out) {
@@ -1397,14 +1421,6 @@ static void assemble_wtw(int64_t n_rec, int64_t p, int64_t q, const double* y, c
     }
   });
   for (const Part& pt : part) CBX_REQUIRE(pt.err == CBX_OK, pt.err, pt.what);
-  out.rhs.assign(dim, 0.0);
-  out.yty = 0.0;
-  for (int64_t i = 0; i < n_rec; ++i) {
-    for (int64_t a = fx_ptr[i]; a < fx_ptr[i + 1]; ++a) out.rhs[fx_col[a]] += fx_val[a] * y[i];
-    const int32_t an = aid[i];
-    if (an > 0 && an <= q) out.rhs[p + an - 1] += y[i];
-    out.yty += y[i] * y[i];
-  }
   // 2. row starts; each thread's offsets in a row follow the earlier threads'
   // (row ranges in parallel: offsets within the range, then the range bases)
   std::vector<int64_t> start(dim + 1, 0), base(T + 1, 0);
@@ -1521,21 +1537,47 @@ extern "C" int cbx_mme_create(cbx_handle* h, int64_t n_rec, int64_t p, int64_t q
     auto m = std::make_unique<Mme>();
     m->n_rec = n_rec; m->p = p; m->q = q; m->dim = p + q;
     const int64_t dim = p + q;
-    // W'W and W'y (mme_builder.cpp:107-176, 321-387), assembled on host threads
-    WtW wtw;
-    assemble_wtw(n_rec, p, q, y, aid, fx_ptr, fx_col, fx_val, wtw);
-    std::vector<int32_t>& ptr = wtw.ptr;
-    std::vector<int32_t>& col = wtw.col;
-    std::vector<double>& val = wtw.val;
-    std::vector<double>& rhs = wtw.rhs;
-    const double yty = wtw.yty;
-    std::vector<double> A11((size_t)p * p, 0.0);
-    std::vector<double> diag(dim, 0.0);
-    for (int64_t i = 0; i < dim; ++i)
-      for (int32_t j = ptr[i]; j < ptr[i + 1]; ++j) {
-        if (col[j] == i) diag[i] = val[j];
-        if (i < p && col[j] < p) A11[i * p + col[j]] = val[j];
-      }
+    // checks, W'y and y'y on the host (record order)
+    std::vector<double> rhs;
+    double yty = 0.0;
+    records_rhs(n_rec, p, q, y, aid, fx_ptr, fx_col, fx_val, rhs, yty);
+    // records
+    m->y.resize(n_rec);
+    CBX_CUDA(cudaMemcpyAsync(m->y.p, y, n_rec * sizeof(double), cudaMemcpyHostToDevice, s));
+    m->aid.resize(n_rec);
+    CBX_CUDA(cudaMemcpyAsync(m->aid.p, aid, n_rec * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+    std::vector<int32_t> xp(n_rec + 1);
+    for (int64_t i = 0; i <= n_rec; ++i) xp[i] = (int32_t)fx_ptr[i];
+    const int64_t nx = fx_ptr[n_rec];
+    m->x_ptr.resize(n_rec + 1);
+    CBX_CUDA(cudaMemcpyAsync(m->x_ptr.p, xp.data(), (n_rec + 1) * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+    m->x_col.resize(std::max<int64_t>(nx, 1));
+    m->x_val.resize(std::max<int64_t>(nx, 1));
+    if (nx > 0) {
+      CBX_CUDA(cudaMemcpyAsync(m->x_col.p, fx_col, nx * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+      CBX_CUDA(cudaMemcpyAsync(m->x_val.p, fx_val, nx * sizeof(double), cudaMemcpyHostToDevice, s));
+    }
+    // W'W (mme_builder.cpp:107-176): its CSR, diagonal, fixed block X'X and the
+    // row pointers of the fixed rows
+    std::vector<int32_t> ptr;
+    std::vector<double> A11;
+    if (use_host_wtw()) {
+      WtW wtw;
+      assemble_wtw(n_rec, p, q, y, aid, fx_ptr, fx_col, fx_val, wtw);
+      std::vector<double> diag(dim, 0.0);
+      A11.assign((size_t)p * p, 0.0);
+      for (int64_t i = 0; i < dim; ++i)
+        for (int32_t j = wtw.ptr[i]; j < wtw.ptr[i + 1]; ++j) {
+          if (wtw.col[j] == i) diag[i] = wtw.val[j];
+          if (i < p && wtw.col[j] < p) A11[i * p + wtw.col[j]] = wtw.val[j];
+        }
+      upload_csr_pair(h, dim, wtw.ptr, wtw.col.data(), wtw.val.data(), m->D64, m->D32);
+      m->diagD.resize(dim);
+      CBX_CUDA(cudaMemcpyAsync(m->diagD.p, diag.data(), dim * sizeof(double), cudaMemcpyHostToDevice, s));
+      ptr.assign(wtw.ptr.begin(), wtw.ptr.begin() + p + 1);
+    } else {
+      wtw_device(h, *m, ptr, A11);
+    }
     {
       // segments of the fixed-effect rows (sv::FIX_SEG entries at most)
       std::vector<int32_t> srow, slo, shi, sptr(p + 1, 0);
@@ -1558,9 +1600,6 @@ extern "C" int cbx_mme_create(cbx_handle* h, int64_t n_rec, int64_t p, int64_t q
       }
       CBX_CUDA(cudaStreamSynchronize(s));
     }
-    upload_csr_pair(h, dim, ptr, col.data(), val.data(), m->D64, m->D32);
-    m->diagD.resize(dim);
-    CBX_CUDA(cudaMemcpyAsync(m->diagD.p, diag.data(), dim * sizeof(double), cudaMemcpyHostToDevice, s));
     m->rhs.resize(dim);
     CBX_CUDA(cudaMemcpyAsync(m->rhs.p, rhs.data(), dim * sizeof(double), cudaMemcpyHostToDevice, s));
     // block-Jacobi fixed block: (X'X + ridge I)^-1, ridge = max(1e-8 max|diag|, 1e-6) (pcg_solver.h:78-85)
@@ -1592,28 +1631,15 @@ extern "C" int cbx_mme_create(cbx_handle* h, int64_t n_rec, int64_t p, int64_t q
       if (!ok) {
         // reference fallback: diagonal scaling of the fixed block (pcg_solver.h:108-116)
         M.assign((size_t)p * p, 0.0);
-        for (int64_t i = 0; i < p; ++i) M[i * p + i] = std::fabs(diag[i]) > 1e-14 ? 1.0 / diag[i] : 1.0;
+        for (int64_t i = 0; i < p; ++i) {
+          const double d = A11[i * p + i];
+          M[i * p + i] = std::fabs(d) > 1e-14 ? 1.0 / d : 1.0;
+        }
         CBX_CUDA(cudaMemcpyAsync(m->A11inv64.p, M.data(), M.size() * sizeof(double), cudaMemcpyHostToDevice, s));
       }
       m->A11inv32.resize((size_t)p * p);
       k_convert<double, float><<<grid_for(p * p, 256, 1024), 256, 0, s>>>(m->A11inv64.p, m->A11inv32.p, p * p);
       h->launched("k_convert");
-    }
-    // records
-    m->y.resize(n_rec);
-    CBX_CUDA(cudaMemcpyAsync(m->y.p, y, n_rec * sizeof(double), cudaMemcpyHostToDevice, s));
-    m->aid.resize(n_rec);
-    CBX_CUDA(cudaMemcpyAsync(m->aid.p, aid, n_rec * sizeof(int32_t), cudaMemcpyHostToDevice, s));
-    std::vector<int32_t> xp(n_rec + 1);
-    for (int64_t i = 0; i <= n_rec; ++i) xp[i] = (int32_t)fx_ptr[i];
-    const int64_t nx = fx_ptr[n_rec];
-    m->x_ptr.resize(n_rec + 1);
-    CBX_CUDA(cudaMemcpyAsync(m->x_ptr.p, xp.data(), (n_rec + 1) * sizeof(int32_t), cudaMemcpyHostToDevice, s));
-    m->x_col.resize(std::max<int64_t>(nx, 1));
-    m->x_val.resize(std::max<int64_t>(nx, 1));
-    if (nx > 0) {
-      CBX_CUDA(cudaMemcpyAsync(m->x_col.p, fx_col, nx * sizeof(int32_t), cudaMemcpyHostToDevice, s));
-      CBX_CUDA(cudaMemcpyAsync(m->x_val.p, fx_val, nx * sizeof(double), cudaMemcpyHostToDevice, s));
     }
     m->y_host.assign(y, y + n_rec);
     m->yty = yty;

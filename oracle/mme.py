@@ -53,7 +53,12 @@ def build_fixed_design(cats, nums=None):
 
 
 class MME:
-    """Dense-matrix restatement of the single-component MME (small sizes only)."""
+    """Dense-matrix restatement of the single-component MME (small sizes only).
+
+    W'W = W^T W.  For records whose fixed-effect columns are distinct (every
+    design FixedDesignG builds: one column per factor level or covariate) this is
+    the reference's triplet assembly (src/core/mme_builder.cpp:107-176), which
+    emits a record's (c_a, c_b) product once per pair a <= b."""
 
     def __init__(self, y, aid, rows, p, q):
         self.y = np.asarray(y, dtype=np.float64)
