@@ -409,10 +409,7 @@ static bool log_refine() {
 // co-resident SpMV blocks slowed the block product from 0.82 to 0.68 of the
 // copy bandwidth, and the step from 66.4 to 68.6 ms.  Never on while a launch
 // trace runs, whose per-launch attribution assumes one stream.
-static bool use_overlap() {
-  static int v = env_int("CBX_OVERLAP", 0);
-  return v != 0;
-}
+static bool use_overlap() { return env_int("CBX_OVERLAP", 0) != 0; }
 template <typename T>
 static bool matvec_split(const cbx_handle* h, const sv::OpView<T>& op) {
   return sizeof(T) == 4 && op.Qd && use_overlap() && !h->trace_on;

@@ -276,3 +276,26 @@ def test_fused_iteration_matches_separate_kernels(handle, gblup, monkeypatch):
         assert true_relres(A, X1[:, c], B[:, c]) < 1e-10, c
         assert rel(X1[:, c], X0[:, c]) < 1e-8, c
 
+
+
+def test_overlapped_sparse_part_matches(handle, gblup, monkeypatch):
+    """The FP32 operator with its sparse part on the second stream beside the
+    block product and the block term added afterwards (CBX_OVERLAP=1): the same
+    operator with its sums in another order, so the solutions agree to 1e-8 and
+    reach true relres < 1e-10."""
+    om, lam = gblup["mme"], 2.0
+    A = om.lhs(gblup["Gi"], lam)
+    rng = np.random.default_rng(92)
+    k = 17
+    B = np.zeros((om.dim, k))
+    B[om.p:, :] = rng.choice([-1.0, 1.0], size=(om.q, k))
+    B[:, 0] = om.rhs()
+    dm = dev_mme(handle, gblup)
+    X0, _, _ = dm.pcg_solve(lam, B, precision=MIXED)
+    monkeypatch.setenv("CBX_OVERLAP", "1")
+    dm1 = dev_mme(handle, gblup)
+    X1, _, _ = dm1.pcg_solve(lam, B, precision=MIXED)
+    monkeypatch.delenv("CBX_OVERLAP")
+    for c in range(k):
+        assert true_relres(A, X1[:, c], B[:, c]) < 1e-10, c
+        assert rel(X1[:, c], X0[:, c]) < 1e-8, c
