@@ -911,10 +911,20 @@ __global__ void __launch_bounds__(NT) k_fixed(OpView<T> op, const T* __restrict_
   const int64_t f = blockIdx.x;
   constexpr int G = NT / S;
   const int tid = threadIdx.x, c = tid % S, g = tid / S;
-  T acc = T(0);
   const int64_t kend = (col == nullptr || col[c].active) ? op.p : 0;  // inactive columns: nothing to do
-  for (int64_t k = g; k < kend; k += G) acc += op.A11inv[f * op.p + k] * R[k * S + c];
-  redT[tid] = acc;
+  // four independent partial sums (k = g + 4 G j + G u) keep four loads in
+  // flight; they are combined in a fixed order
+  T a0 = T(0), a1 = T(0), a2 = T(0), a3 = T(0);
+  const T* __restrict__ arow = op.A11inv + f * op.p;
+  int64_t k = g;
+  for (; k + 3 * G < kend; k += 4 * G) {
+    a0 += arow[k] * R[k * S + c];
+    a1 += arow[k + G] * R[(k + G) * S + c];
+    a2 += arow[k + 2 * G] * R[(k + 2 * G) * S + c];
+    a3 += arow[k + 3 * G] * R[(k + 3 * G) * S + c];
+  }
+  for (; k < kend; k += G) a0 += arow[k] * R[k * S + c];
+  redT[tid] = (a0 + a1) + (a2 + a3);
   __syncthreads();
   if (tid < S) {
     T s = T(0);
