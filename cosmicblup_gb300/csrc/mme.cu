@@ -828,7 +828,7 @@ void run_pcg(cbx_handle* h, Mme& m, const sv::OpView<T>& op, Workspace<T, S>& w,
       sv::k_scalar_alpha_c<S><<<S, sv::NTC, 0, s>>>(w.col.p, w.pq_part.p,
                                                     w.nblk_spmv + (matvec_split(h, op) ? w.nblk_dadd : 0));
       h->launched(sizeof(T) == 4 ? "k_scalar_alpha<f32>" : "k_scalar_alpha<f64>");
-      sv::k_update<T, S><<<w.nblk_vec, sv::NT, 0, s>>>(op, w.col.p, X, Xlo, w.R.p, w.Z.p, w.P.p, w.Q.p, w.part.p);
+      sv::k_update<T, S><<<w.nblk_vec, sv::NT, 0, s>>>(op, w.col.p, X, Xlo, w.R.p, w.P.p, w.Q.p, w.part.p);
       h->launched(sizeof(T) == 4 ? "k_update<f32>" : "k_update<f64>");
       if (m.p > 0) {
         sv::k_fixed<T, S><<<(unsigned)m.p, sv::NT, 0, s>>>(op, w.R.p, w.Z.p, w.col.p, w.rz_fix.p);
@@ -837,8 +837,8 @@ void run_pcg(cbx_handle* h, Mme& m, const sv::OpView<T>& op, Workspace<T, S>& w,
       sv::k_scalar_beta_c<S><<<S, sv::NTC, 0, s>>>(w.col.p, w.part.p, w.nblk_vec, w.rz_fix.p, m.p, w.tol.p, abs_tol,
                                                    maxit, w.active.p, w.done.p);
       h->launched(sizeof(T) == 4 ? "k_scalar_beta<f32>" : "k_scalar_beta<f64>");
-      sv::k_pupdate<T, S><<<grid_for(m.dim * S, sv::NT, 16 * h->num_sms), sv::NT, 0, s>>>(m.dim, w.col.p, w.Z.p,
-                                                                                           w.P.p);
+      sv::k_pupdate<T, S><<<grid_for(m.dim * S, sv::NT, 16 * h->num_sms), sv::NT, 0, s>>>(
+          m.dim, m.p, op.dinv, w.col.p, w.R.p, w.Z.p, w.P.p);
       h->launched(sizeof(T) == 4 ? "k_pupdate<f32>" : "k_pupdate<f64>");
     }
   };

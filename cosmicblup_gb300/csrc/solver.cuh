@@ -936,15 +936,17 @@ __global__ void __launch_bounds__(NT) k_fixed(OpView<T> op, const T* __restrict_
   }
 }
 
-// x += alpha p, r -= alpha q (active, non-skipped columns), z = Jacobi r on random
-// rows; partial sums of r'r and r'z (random rows).  With Xlo (FP32 only) the
+// x += alpha p, r -= alpha q (active, non-skipped columns); partial sums of r'r
+// and r'z over the random rows, z = Jacobi r there (computed, not stored: the
+// direction update forms it again from r, so Z holds only the fixed rows' z,
+// written by k_fixed, after the initial residual).  With Xlo (FP32 only) the
 // iterate is a float-float pair x = Xs + Xlo: alpha p is formed exactly as a
 // product and its rounding error, and added with a two-sum, so x carries about
 // 48 bits although r, z, p and q stay FP32.
 template <typename T, int S>
 __global__ void __launch_bounds__(NT) k_update(OpView<T> op, const Col* __restrict__ col,
                                                T* __restrict__ Xs, T* __restrict__ Xlo, T* __restrict__ R,
-                                               T* __restrict__ Z, const T* __restrict__ P,
+                                               const T* __restrict__ P,
                                                const T* __restrict__ Q,
                                                double* __restrict__ part /*[grid][2][S]*/) {
   __shared__ double red[NT];
@@ -984,16 +986,7 @@ __global__ void __launch_bounds__(NT) k_update(OpView<T> op, const Col* __restri
       R[idx] = r;
     }
     arr.add(r, r);
-    if (i >= op.p) {
-      // z is loaded for every column (a load on one side of a branch that differs
-      // between the lanes of a warp measured twice as slow)
-      T z = Z[idx];
-      if (upd) {
-        z = op.dinv[i - op.p] * r;
-        Z[idx] = z;
-      }
-      arz.add(r, z);
-    }
+    if (i >= op.p) arz.add(r, op.dinv[i - op.p] * r);
   }
   const double rr = arr.value(), rz = arz.value();
   double t = block_sum_cols<S>(rr, red);
@@ -1002,17 +995,22 @@ __global__ void __launch_bounds__(NT) k_update(OpView<T> op, const Col* __restri
   if (threadIdx.x < S) part[((int64_t)blockIdx.x * 2 + 1) * S + c] = t;
 }
 
-// p = z + beta p (active columns).
+// p = z + beta p (active columns); z = Z on the fixed rows (k_fixed), Jacobi r on
+// the random rows (the same product k_update sums).
 template <typename T, int S>
-__global__ void __launch_bounds__(NT) k_pupdate(int64_t dim, const Col* __restrict__ col,
+__global__ void __launch_bounds__(NT) k_pupdate(int64_t dim, int64_t nfix, const T* __restrict__ dinv,
+                                                const Col* __restrict__ col, const T* __restrict__ R,
                                                 const T* __restrict__ Z, T* __restrict__ P) {
   const int c = threadIdx.x % S;
   if (!col[c].active) return;
   const T beta = (T)col[c].beta;
   const int64_t total = dim * S;
   for (int64_t idx = blockIdx.x * (int64_t)NT + threadIdx.x; idx < total;
-       idx += (int64_t)gridDim.x * NT)
-    P[idx] = Z[idx] + beta * P[idx];
+       idx += (int64_t)gridDim.x * NT) {
+    const int64_t i = idx / S;
+    const T z = i < nfix ? Z[idx] : dinv[i - nfix] * R[idx];
+    P[idx] = z + beta * P[idx];
+  }
 }
 
 // Sum of part[b * stride + c] over b < nblk for every column c < S, by all
