@@ -743,7 +743,7 @@ void run_pcg(cbx_handle* h, Mme& m, const sv::OpView<T>& op, Workspace<T, S>& w,
   sv::k_init_resid<T, S><<<w.nblk_vec, sv::NT, 0, s>>>(op, B, w.Q.p, use_x0 ? 1 : 0, w.R.p, w.Z.p, w.part.p);
   h->launched(sizeof(T) == 4 ? "k_init_resid<f32>" : "k_init_resid<f64>");
   if (m.p > 0) {
-    sv::k_fixed<T, S><<<(unsigned)m.p, sv::NT, 0, s>>>(op, w.R.p, w.Z.p, nullptr, w.rz_fix.p);
+    sv::k_fixed<T, S><<<(unsigned)m.p, sv::NT_FIXED, 0, s>>>(op, w.R.p, w.Z.p, nullptr, w.rz_fix.p);
     h->launched(sizeof(T) == 4 ? "k_fixed<f32>" : "k_fixed<f64>");
   }
   std::vector<double> tolv(S, 1.0);
@@ -831,7 +831,7 @@ void run_pcg(cbx_handle* h, Mme& m, const sv::OpView<T>& op, Workspace<T, S>& w,
       sv::k_update<T, S><<<w.nblk_vec, sv::NT, 0, s>>>(op, w.col.p, X, Xlo, w.R.p, w.P.p, w.Q.p, w.part.p);
       h->launched(sizeof(T) == 4 ? "k_update<f32>" : "k_update<f64>");
       if (m.p > 0) {
-        sv::k_fixed<T, S><<<(unsigned)m.p, sv::NT, 0, s>>>(op, w.R.p, w.Z.p, w.col.p, w.rz_fix.p);
+        sv::k_fixed<T, S><<<(unsigned)m.p, sv::NT_FIXED, 0, s>>>(op, w.R.p, w.Z.p, w.col.p, w.rz_fix.p);
         h->launched(sizeof(T) == 4 ? "k_fixed<f32>" : "k_fixed<f64>");
       }
       sv::k_scalar_beta_c<S><<<S, sv::NTC, 0, s>>>(w.col.p, w.part.p, w.nblk_vec, w.rz_fix.p, m.p, w.tol.p, abs_tol,

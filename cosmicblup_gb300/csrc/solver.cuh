@@ -902,29 +902,27 @@ __global__ void __launch_bounds__(NT) k_init_resid(OpView<T> op, const T* __rest
   if (threadIdx.x < S) part[((int64_t)blockIdx.x * 3 + 2) * S + c] = t;
 }
 
-// Fixed rows: z_f = A11inv r_f, partial r_f'z_f per row.  One block per fixed row.
+// Fixed rows: z_f = A11inv r_f and the partial r_f'z_f.  One block per fixed row,
+// of NT_FIXED threads: its NT_FIXED / S groups take every (NT_FIXED / S)-th k and
+// are combined in a fixed order.  The kernel is bound by the length of each
+// thread's chain of loads: at p = 500, S = 128 (the 200k-animal ssGBLUP step)
+// 1024-thread blocks (chains of p / 8) took the step from 65.1 to 63.7 ms against
+// 256-thread blocks (chains of p / 2), and one block per 8 rows (chains of p,
+// each r_k reused for four rows) made it 68.5 ms.
+constexpr int NT_FIXED = 1024;
+
 template <typename T, int S>
-__global__ void __launch_bounds__(NT) k_fixed(OpView<T> op, const T* __restrict__ R,
-                                              T* __restrict__ Z, const Col* __restrict__ col,
-                                              double* __restrict__ rz_fix /*[p][S]*/) {
-  __shared__ T redT[NT];
+__global__ void __launch_bounds__(NT_FIXED) k_fixed(OpView<T> op, const T* __restrict__ R,
+                                                    T* __restrict__ Z, const Col* __restrict__ col,
+                                                    double* __restrict__ rz_fix /*[p][S]*/) {
+  __shared__ T redT[NT_FIXED];
   const int64_t f = blockIdx.x;
-  constexpr int G = NT / S;
+  constexpr int G = NT_FIXED / S;
   const int tid = threadIdx.x, c = tid % S, g = tid / S;
+  T acc = T(0);
   const int64_t kend = (col == nullptr || col[c].active) ? op.p : 0;  // inactive columns: nothing to do
-  // four independent partial sums (k = g + 4 G j + G u) keep four loads in
-  // flight; they are combined in a fixed order
-  T a0 = T(0), a1 = T(0), a2 = T(0), a3 = T(0);
-  const T* __restrict__ arow = op.A11inv + f * op.p;
-  int64_t k = g;
-  for (; k + 3 * G < kend; k += 4 * G) {
-    a0 += arow[k] * R[k * S + c];
-    a1 += arow[k + G] * R[(k + G) * S + c];
-    a2 += arow[k + 2 * G] * R[(k + 2 * G) * S + c];
-    a3 += arow[k + 3 * G] * R[(k + 3 * G) * S + c];
-  }
-  for (; k < kend; k += G) a0 += arow[k] * R[k * S + c];
-  redT[tid] = (a0 + a1) + (a2 + a3);
+  for (int64_t k = g; k < kend; k += G) acc += op.A11inv[f * op.p + k] * R[k * S + c];
+  redT[tid] = acc;
   __syncthreads();
   if (tid < S) {
     T s = T(0);
