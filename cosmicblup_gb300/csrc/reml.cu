@@ -17,6 +17,7 @@
 #include <memory>
 #include <random>
 #include <thread>
+#include <cstdlib>
 #include <vector>
 #include <cublas_v2.h>
 #include <cusolverDn.h>
@@ -1471,8 +1472,20 @@ __global__ void k_add_lowrank(double* __restrict__ A, int64_t n, const double* _
 //  * otherwise only the eigenpairs below eps are computed (syevdx), M is raised
 //    to M + sum (eps - lambda_i) u_i u_i^T, whose eigenvalues are all >= eps,
 //    and that is inverted by Cholesky.
+//  * when the all-ones direction is (nearly) null -- every VanRaden G, whose
+//    centred columns sum to zero -- the one eigenpair below eps is found by
+//    inverse iteration instead (deflate_ones below), without syevdx.
 // The full eigendecomposition (syevd, scaled columns, GEMM) remains for the
-// other cases.  The three forms are the same matrix in exact arithmetic.
+// other cases.  The four forms are the same matrix in exact arithmetic.
+static int env_int_reml(const char* name, int def) {
+  const char* e = std::getenv(name);
+  return (e && *e) ? std::atoi(e) : def;
+}
+
+// The one-null-direction path of the eigen-bending inverse (environment
+// CBX_DEFLATE_ONES=0 takes the syevdx path instead).
+static bool use_deflate_ones() { return env_int_reml("CBX_DEFLATE_ONES", 1) != 0; }
+
 static void invert_psd_full(cbx_handle* h, const double* M_dev, int64_t n, double ridge, double* out_dev) {
   cudaStream_t s = h->stream;
   Libs& L = libs(h);
@@ -1511,6 +1524,59 @@ static void invert_psd_full(cbx_handle* h, const double* M_dev, int64_t n, doubl
                        &zero, out_dev, (int)n));
 }
 
+// One eigenvalue of Mr (M + ridge I, in out_dev) below eps, along a direction
+// close to v = 1/sqrt(n) (v'Mr v < eps):
+//  1. u from eight steps of inverse iteration with the Cholesky factor of
+//     Mr + eps I (each step shrinks the other eigenvectors' share by
+//     (lambda_1 + eps) / (lambda_i + eps));
+//  2. check: Mr + c u u^T - 100 eps I (c = ||Mr||_inf + 1) has a Cholesky factor,
+//     so every eigenvalue off u is above 100 eps and u is the only one raised;
+//     the gap also bounds u's error after step 1 by (0.1 * 2 / 101)^8;
+//  3. Mr + (eps - u'Mr u) u u^T, the raised matrix, inverted by Cholesky.
+// Returns false, with out_dev untouched, when step 1 or 2 fails.
+static bool deflate_ones(cbx_handle* h, const double* M_dev, int64_t n, double ridge, double eps, double rinf,
+                         double* out_dev) {
+  cudaStream_t s = h->stream;
+  Libs& L = libs(h);
+  const int ni = (int)n;
+  DevBuf<double> T, u, y, w;
+  T.resize((size_t)n * n);
+  u.resize(n);
+  y.resize(n);
+  w.resize(1);
+  k_add_ridge_copy<<<gridn(n * n, 256, 8 * h->num_sms), 256, 0, s>>>(out_dev, n, eps, T.p);
+  h->launched("k_add_ridge_copy");
+  if (!potrf(h, T.p, n)) return false;
+  std::vector<double> x(n, 1.0 / std::sqrt((double)n));
+  CBX_CUDA(cudaMemcpyAsync(u.p, x.data(), n * sizeof(double), cudaMemcpyHostToDevice, s));
+  for (int it = 0; it < 8; ++it) {
+    potrs(h, T.p, n, u.p, 1);
+    double nrm = 0.0;
+    CBX_BLAS(cublasDnrm2(L.blas, ni, u.p, 1, &nrm));
+    if (!(nrm > 0.0) || !std::isfinite(nrm)) return false;
+    const double sc = 1.0 / nrm;
+    CBX_BLAS(cublasDscal(L.blas, ni, &sc, u.p, 1));
+  }
+  const double one = 1.0, zero = 0.0;
+  CBX_BLAS(cublasDgemv(L.blas, CUBLAS_OP_N, ni, ni, &one, out_dev, ni, u.p, 1, &zero, y.p, 1));
+  double rho = 0.0;
+  CBX_BLAS(cublasDdot(L.blas, ni, u.p, 1, y.p, 1, &rho));
+  if (!(rho < eps)) return false;
+  const double c = rinf + 1.0;
+  k_add_ridge_copy<<<gridn(n * n, 256, 8 * h->num_sms), 256, 0, s>>>(out_dev, n, -100.0 * eps, T.p);
+  h->launched("k_add_ridge_copy");
+  CBX_CUDA(cudaMemcpyAsync(w.p, &c, sizeof(double), cudaMemcpyHostToDevice, s));
+  k_add_lowrank<<<gridn(n * n, 256, 8 * h->num_sms), 256, 0, s>>>(T.p, n, u.p, w.p, 1);
+  h->launched("k_add_lowrank");
+  if (!potrf(h, T.p, n)) return false;
+  const double raise = eps - rho;
+  CBX_CUDA(cudaMemcpyAsync(w.p, &raise, sizeof(double), cudaMemcpyHostToDevice, s));
+  k_add_lowrank<<<gridn(n * n, 256, 8 * h->num_sms), 256, 0, s>>>(out_dev, n, u.p, w.p, 1);
+  h->launched("k_add_lowrank");
+  if (!chol_inverse_device(h, out_dev, n)) invert_psd_full(h, M_dev, n, ridge, out_dev);
+  return true;
+}
+
 void invert_psd_device(cbx_handle* h, const double* M_dev, int64_t n, double ridge, double* out_dev) {
   cudaStream_t s = h->stream;
   const double r = ridge > 0 ? ridge : 0.0;
@@ -1530,6 +1596,21 @@ void invert_psd_device(cbx_handle* h, const double* M_dev, int64_t n, double rid
     return;
   }
   const double eps = 1e-6;
+  if (n > 1 && use_deflate_ones()) {
+    // the all-ones direction nearly null: M - eps I cannot be positive definite
+    Libs& L = libs(h);
+    const int ni = (int)n;
+    DevBuf<double> v, y;
+    v.resize(n);
+    y.resize(n);
+    std::vector<double> vh(n, 1.0 / std::sqrt((double)n));
+    CBX_CUDA(cudaMemcpyAsync(v.p, vh.data(), n * sizeof(double), cudaMemcpyHostToDevice, s));
+    const double one = 1.0, zero = 0.0;
+    CBX_BLAS(cublasDgemv(L.blas, CUBLAS_OP_N, ni, ni, &one, out_dev, ni, v.p, 1, &zero, y.p, 1));
+    double rho0 = 0.0;
+    CBX_BLAS(cublasDdot(L.blas, ni, v.p, 1, y.p, 1, &rho0));
+    if (rho0 < eps && deflate_ones(h, M_dev, n, ridge, eps, rinf, out_dev)) return;
+  }
   DevBuf<double> T;
   T.resize((size_t)n * n);
   // no eigenvalue below eps: M - eps I is positive definite
