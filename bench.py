@@ -71,9 +71,11 @@ CONFIGS = {
     "c5": dict(name="batch96_gblup_n500-8000_m5000-40000", kind="batch", nprob=96, n_lo=500, n_hi=8000,
                m_lo=5000, m_hi=40000, levels=10, max_iter=3, workers=16, seed=5000, mt_n=10000, mt_m=20000),
 }
-# DRAM bytes per launch of k_dense_tf32<64> from an ncu capture at n = 8,192
-# (1.0125 x the algorithmic bytes), scaled to a 20,000-row block by the block's bytes
-TRAFFIC_BYTES = {20000: 1.635e9}
+# DRAM bytes (read + written) per launch of the block product from ncu captures at
+# n = 8,192, scaled to a 20,000-row block by the block's bytes (x (20000 / 8192)^2):
+# k_dense_tf32<64> (the GBLUP iteration's block, 33 columns) 282.9 MB -> 1.686e9, and
+# k_dense_tf32<128, 80> (the iteration + gradient block, 65 columns) 278.4 MB -> 1.659e9
+TRAFFIC_BYTES = {(20000, 64): 1.686e9, (20000, 128): 1.659e9}
 # the reference's adaptive estimator with one thread checks after two batches of 16
 REF_EM_PROBES = 32
 
@@ -766,10 +768,12 @@ def run_gpu(args, cfg):
         "e2e": e2e,
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm",
-                     "kernel": ("k_dense_tf32 (tcgen05 3xTF32, dense H^-1 / G^-1 block x the populated columns of "
-                                "the block, up to 80 of a 128-wide block)"),
+                     "kernel": (("k_dense_tf32<128, 80>" if G_PROBES else "k_dense_tf32<64>")
+                                + " (tcgen05 3xTF32, dense H^-1 / G^-1 block x the populated columns of the "
+                                  "solver block)"),
                      "achieved": ach, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": (ach / hbm_peak) if ach else None, "traffic": TRAFFIC_BYTES.get(n),
+                     "frac": (ach / hbm_peak) if ach else None,
+                     "traffic": TRAFFIC_BYTES.get((n, 128 if G_PROBES else 64)),
                      "peak_source": peak_src, "launches": dl, "avg_launch_ms": dms / dl if dl else None,
                      "step_dense_bytes_GBps": (dbytes + ffbytes) / (ms_local * 1e-3) / 1e9,
                      "step_hbm_frac": (dbytes + ffbytes) / (ms_local * 1e-3) / 1e9 / hbm_peak,
