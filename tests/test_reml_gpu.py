@@ -1,6 +1,6 @@
 """GPU parity tests of the REML path against the oracle restatement of AI_REML.
 
-Bar (the benchmark spec's): variance components within 1e-6 relative of the FP64
+Bar: variance components within 1e-6 relative of the FP64
 oracle; the Hutchinson probe count identical (same probe vectors, same adaptive
 stop); the eigen-bending inverse within 1e-9 of the oracle's.
 """
